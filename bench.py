@@ -1,0 +1,275 @@
+"""Benchmark of the tt_eigb sweep hot path on one GB300.
+
+Workload (one "step"): the block eigensolver tt_eigb on the d=20 open-boundary
+spin-1/2 Heisenberg chain (TT-matrix n=2, rank 5 -- the operator of the
+reference fixture Heisen_20.sdv), B=5 lowest eigenpairs, random N(0,1) start
+block with ranks 16 (seed 0), ranks capped at 64, eps=1e-8, max_full_size=200,
+swept to convergence.  Metric: wall time of one full solve (lower is better).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--method plain|split]
+
+GPU arm: times K solves through the C-ABI with CUDA events on the library's
+stream (value), the same solves end to end from pinned host buffers (e2e),
+the dominant kernel's roofline from a local-matvec microbenchmark timed with
+CUDA events, SM clocks sampled by nvidia-smi during the timed region, and the
+CPU oracle timed on the host cores (cpu_baseline).  Reference arm: the CPU
+restatement of tt_eigb (oracle/eigb.py, numpy + OpenBLAS on all host cores).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "tt-fort_gb300")]
+
+import numpy as np  # noqa: E402
+
+D, B, R0, RMAX, EPS, MFS = 20, 5, 16, 64, 1e-8, 200
+
+
+def workload():
+    from ttgpu.operators import xxz_mpo, random_tt
+    n, m, ra, crA = xxz_mpo(D)
+    _, ry, cr = random_tt(D, 2, R0, last=B, seed=0)
+    return n, m, ra, crA, ry, cr
+
+
+def config():
+    return {"workload": f"tt_eigb heisenberg d={D} n=2 ra=5 B={B} start_rank={R0} rmax={RMAX} "
+                        f"eps={EPS:g} max_full_size={MFS}",
+            "d": D, "B": B, "rmax": RMAX, "eps": EPS, "n": 2, "ra": 5,
+            "l2": "inputs < L2: 256 MiB buffer written between timed steps"}
+
+
+def bfun3_flops(rx1, m, rx2, ry1, n, ry2, ra1, ra2):
+    return 2 * rx1 * m * rx2 * ra2 * ry2 + 2 * ra1 * n * m * ra2 * ry2 * rx1 + 2 * ry1 * n * ry2 * rx1 * ra1
+
+
+class ClockSampler:
+    def __init__(self):
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 3 + k and r[3 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return json.load(open(p)), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def fp64_peak_tflops(torch):
+    """cuBLAS DGEMM 4096^3 (torch.matmul float64), best of 5: the FP64 roof."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = 1e9
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return 2 * 4096 ** 3 / best / 1e12
+
+
+def matvec_roofline(torch, ctx, split=False):
+    """Local matvec at the workload's largest local problem (r=64, n=2, ra=5,
+    block of B vectors): average launch duration from CUDA events."""
+    import ttgpu
+    r, n, ra = RMAX, 2, 5
+    rng = np.random.default_rng(0)
+    phi1 = torch.from_numpy(rng.standard_normal(r * r * ra)).cuda()
+    A = torch.from_numpy(rng.standard_normal(ra * n * n * ra)).cuda()
+    phi2 = torch.from_numpy(rng.standard_normal(r * ra * r)).cuda()
+    X = torch.from_numpy(rng.standard_normal(r * n * r * B)).cuda()
+    Y = torch.zeros(r * n * r * B, dtype=torch.float64, device="cuda")
+    ctx.bind_torch_stream()
+    for _ in range(5):
+        ttgpu.dbfun3(r, n, r, r, n, r, ra, ra, phi1, A, phi2, X, Y, nvec=B, split=split, ctx=ctx)
+    iters = 200
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(iters):
+        ttgpu.dbfun3(r, n, r, r, n, r, ra, ra, phi1, A, phi2, X, Y, nvec=B, split=split, ctx=ctx)
+    e1.record()
+    torch.cuda.synchronize()
+    dt = e0.elapsed_time(e1) / 1e3 / iters
+    flops = bfun3_flops(r, n, r, r, n, r, ra, ra) * B
+    return flops, dt
+
+
+def run_reference(args):
+    from oracle.eigb import tt_eigb as oracle_eigb
+    n, m, ra, crA, ry, cr = workload()
+    steps = max(1, min(args.steps, 2))
+    warm = min(args.warmup, 1)
+    for _ in range(warm):
+        oracle_eigb(D, n, m, ra, crA, cr, ry, EPS, RMAX, B, nswp=20, max_full_size=MFS)
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        out = oracle_eigb(D, n, m, ra, crA, cr, ry, EPS, RMAX, B, nswp=20, max_full_size=MFS)
+        ts.append(time.perf_counter() - t0)
+    v = float(np.mean(ts))
+    cores = os.cpu_count()
+    line = {"metric": "tt_eigb sweep time to convergence (d=20 Heisenberg, B=5)",
+            "value": v, "unit": "s", "n_gpus": args.gpus, "steps": steps, "warmup": warm,
+            "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+            "config": config(),
+            "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
+                             "sample": f"{steps} full solve(s) of the workload with the oracle "
+                                       "restatement (numpy + OpenBLAS threads)"},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "lambda": out["lambda"].tolist()}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours")
+    ap.add_argument("--method", default="plain")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    import torch
+    import ttgpu
+    if args.gpus > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    ctx = ttgpu.Context(torch.cuda.current_device())
+    ctx.bind_torch_stream()
+    n, m, ra, crA, ry, cr = workload()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    def solve():
+        return ttgpu.tt_eigb(D, n, m, ra, crA, cr, ry, EPS, RMAX, B, nswp=20, max_full_size=MFS,
+                             method=args.method, ctx=ctx)
+
+    for _ in range(max(3, args.warmup)):
+        solve()
+    # timed region
+    times, walls = [], []
+    launches0 = ttgpu.launch_count()
+    if args.gpus > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler() as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            w0 = time.perf_counter()
+            e0.record()
+            lam, cores, ry_out = solve()
+            e1.record()
+            torch.cuda.synchronize()
+            walls.append(time.perf_counter() - w0)
+            times.append(e0.elapsed_time(e1) / 1e3)
+    launches = (ttgpu.launch_count() - launches0) // max(1, args.steps)
+    st = ctx.stats()
+    t = float(np.mean(times))
+    tw = float(np.mean(walls))
+    if args.gpus > 1:
+        tt = torch.tensor([t, tw], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t, tw = tt.tolist()
+    if rank != 0:
+        return
+    peaks, kind = measured_peaks()
+    fl, dt = matvec_roofline(torch, ctx, split=(args.method == "split"))
+    if args.method == "split":
+        peak, unit, bound = peaks["bf16_tflops"], "TFLOP/s", "tensor"
+        peak_note = f"bf16 dense burst, {kind}"
+    else:
+        peak, unit, bound = fp64_peak_tflops(torch), "TFLOP/s", "tensor"
+        peak_note = "fp64: cuBLAS DGEMM 4096^3 measured in this run"
+    ach = fl / dt / 1e12
+    h2d = (len(crA) + len(cr)) * 8 + (len(n) * 3 + 2 * len(ry)) * 8
+    d2h = len(cores) * 8 + B * 8
+    cpu = None
+    if not args.no_cpu:
+        from oracle.eigb import tt_eigb as oracle_eigb
+        t0 = time.perf_counter()
+        ref = oracle_eigb(D, n, m, ra, crA, cr, ry, EPS, RMAX, B, nswp=20, max_full_size=MFS)
+        tc = time.perf_counter() - t0
+        cpu = {"value": tc, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "one full solve of the workload with the oracle restatement "
+                         "(numpy + OpenBLAS threads)",
+               "lambda_maxrel_vs_gpu": float(np.max(np.abs(ref["lambda"] - lam) / np.abs(ref["lambda"])))}
+    line = {"metric": "tt_eigb sweep time to convergence (d=20 Heisenberg, B=5)",
+            "value": t, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": t * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.method == "plain" else "bf16x3/f64",
+            "data": "synthetic (seeded)", "method": args.method, "config": config(),
+            "e2e": {"value": tw, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches),
+            "roofline": {"kernel": "local matvec bfun3 (r=64, n=2, ra=5, block 5)",
+                         "bound": bound, "achieved": ach, "peak": peak, "unit": unit,
+                         "frac": ach / peak, "traffic": None, "peak_source": peak_note,
+                         "launch_us": dt * 1e6, "flops_per_launch": fl},
+            "clocks": clk.summary(), "cpu_baseline": cpu,
+            "solve": {"lambda": lam.tolist(), "matvecs": st["matvecs"], "sweeps": st["sweeps"],
+                      "max_rank": max(ry_out[:D])}}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

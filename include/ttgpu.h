@@ -1,0 +1,166 @@
+/*
+ * ttgpu.h -- C-ABI of the GB300 tensor-train sweep library (libttgpu.so).
+ *
+ * Drop-in boundary for the hot path of oseledets/tt-fort: the ALS/AMEn/KSL
+ * sweep.  A Fortran host binds these symbols through ISO_C_BINDING (the
+ * interface module is in INTEGRATION.md); C and Python (ctypes) callers use
+ * them directly.
+ *
+ * Conventions
+ *   - integers are 64-bit (ttg_int), fixed for every build (the reference's
+ *     i4/i8 presets, Makefile.in:7-106, become one documented width);
+ *   - all arrays are flat column-major, exactly the reference layouts;
+ *   - complex arrays are interleaved (re, im) double pairs, i.e. Fortran
+ *     complex(8) / C99 double _Complex;
+ *   - every call returns an int status (TTG_OK = 0, negative = error) and
+ *     never stops the process (the reference prints and `stop`s,
+ *     ttamen.f90:140,144; expokit.f:483);
+ *   - kernel-level entry points take DEVICE pointers and run on the context's
+ *     stream; driver entry points take HOST pointers;
+ *   - one context per host thread: the context replaces the reference's
+ *     module globals (tt_eigb.f90:1-50, tt_ksl.f90:1-166) and module result
+ *     arrays (result_core tt_eigb.f90:57, zresult_core tt_ksl.f90:171).
+ */
+#ifndef TTGPU_H
+#define TTGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int64_t ttg_int;
+typedef struct ttg_ctx ttg_ctx;
+
+enum {
+  TTG_OK = 0,
+  TTG_ERR_ARG = -1,         /* inconsistent sizes / ranks / null pointers   */
+  TTG_ERR_CUDA = -2,        /* a CUDA runtime call failed                  */
+  TTG_ERR_NOMEM = -3,       /* device allocation failed                    */
+  TTG_ERR_NOCONV = -4,      /* an iteration cap was reached                */
+  TTG_ERR_NAN = -5,         /* non-finite value detected                   */
+  TTG_ERR_UNSUPPORTED = -7  /* shape outside what a kernel supports        */
+};
+
+enum {
+  TTG_METHOD_PLAIN = 0,     /* FP64 contractions, the reference's arithmetic */
+  TTG_METHOD_SPLIT = 1      /* BF16x3 tensor-core contractions, FP32 accumulate,
+                               FP64 Rayleigh-Ritz / QR / SVD / Pade          */
+};
+
+/* ---------------------------------------------------------------- context */
+int ttg_create(int device, ttg_ctx** ctx);
+int ttg_destroy(ttg_ctx* ctx);
+const char* ttg_last_error(const ttg_ctx* ctx);
+/* run on a caller-owned cudaStream_t from now on (NULL = the legacy default
+ * stream); the context's own stream is released */
+int ttg_set_stream(ttg_ctx* ctx, void* cuda_stream);
+int ttg_synchronize(ttg_ctx* ctx);
+int ttg_version(void);
+
+/* ------------------------------------------------ local operator (device) */
+/* y = Phi1 * A * Phi2 * x for nvec vectors stored back to back.
+ * Replaces dbfun3 ttals.f90:9-32 (also d2d_mv ttlocsolve.f90:49-88, the
+ * bind(c) dbfun3 tt_linalg.f90:127-159) and the per-vector loop of
+ * primme_matvec tt_eigb.f90:15-27. */
+int ttg_dbfun3(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ry1, ttg_int n,
+               ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi1, const double* A,
+               const double* phi2, const double* x, double* y, ttg_int nvec);
+/* Same product on the tensor cores: BF16x3 split operands, FP32 accumulation
+ * (tcgen05.mma, accumulators in TMEM).  The chosen form's local matvec. */
+int ttg_dbfun3_split(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ry1,
+                     ttg_int n, ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi1,
+                     const double* A, const double* phi2, const double* x, double* y,
+                     ttg_int nvec);
+/* Complex product, zbfun3 ttals.f90:34-57. */
+int ttg_zbfun3(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ry1, ttg_int n,
+               ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi1, const double* A,
+               const double* phi2, const double* x, double* y, ttg_int nvec);
+/* Adjoint product for the 1-norm estimate, zbfun3_transp ttals.f90:85-108. */
+int ttg_zbfun3_transp(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ry1,
+                      ttg_int n, ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi1,
+                      const double* A, const double* phi2, const double* x, double* y,
+                      ttg_int nvec);
+
+/* ------------------------------------------------- interface updates (device) */
+/* phi1_new (ry2, rx2, ra2): dphi_left ttals.f90:203-227 */
+int ttg_dphi_left(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ry1, ttg_int n,
+                  ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi1_old,
+                  const double* A, const double* x, const double* y, double* phi1_new);
+/* phi2_new (rx1, ra1, ry1): dphi_right ttals.f90:150-173 */
+int ttg_dphi_right(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ry1, ttg_int n,
+                   ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi2_old,
+                   const double* A, const double* x, const double* y, double* phi2_new);
+/* complex, y conjugated: zphi_left ttals.f90:229-256, zphi_right :176-200 */
+int ttg_zphi_left(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ry1, ttg_int n,
+                  ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi1_old,
+                  const double* A, const double* x, const double* y, double* phi1_new);
+int ttg_zphi_right(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ry1, ttg_int n,
+                   ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi2_old,
+                   const double* A, const double* x, const double* y, double* phi2_new);
+/* Y'X projections: dphi2_left ttals.f90:296-314, dphi2_right :260-277 */
+int ttg_dphi2_left(ttg_ctx* ctx, ttg_int rx1, ttg_int rx2, ttg_int ry1, ttg_int n,
+                   ttg_int ry2, const double* phi1_old, const double* x, const double* y,
+                   double* phi1_new);
+int ttg_dphi2_right(ttg_ctx* ctx, ttg_int rx1, ttg_int rx2, ttg_int ry1, ttg_int n,
+                    ttg_int ry2, const double* phi2_old, const double* x, const double* y,
+                    double* phi2_new);
+/* dense local matrix, d2d_fullmat tt_eigb.f90:88-105 / ttlocsolve.f90:133-150 */
+int ttg_d2d_fullmat(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ra1,
+                    ttg_int ra2, const double* phi1, const double* A, const double* phi2,
+                    double* B);
+
+/* ------------------------------------------------ dense algebra (device) */
+/* A (n x m) -> Q (n x min(n,m)) in place, R (min(n,m) x m): dqr
+ * matrix_util.f90:37-61 (bind(c) twin tt_linalg.f90:30); zqr :64-90. */
+int ttg_dqr(ttg_ctx* ctx, ttg_int n, ttg_int m, double* A, double* R);
+int ttg_zqr(ttg_ctx* ctx, ttg_int n, ttg_int m, double* A, double* R);
+/* symmetric eigen, ascending; eigenvectors overwrite A (dsyev 'V','U',
+ * tt_eigb.f90:238).  k <= 512. */
+int ttg_dsyev(ttg_ctx* ctx, ttg_int k, double* A, double* w);
+/* thin SVD M (p x q) = U diag(s) Vt, descending s (dgesvd tt_eigb.f90:312,361). */
+int ttg_dgesvd(ttg_ctx* ctx, ttg_int p, ttg_int q, const double* M, double* U, double* s,
+               double* Vt);
+/* rank kept by my_chop3 (matrix_util.f90:254-275) for n singular values
+ * (host array). */
+ttg_int ttg_my_chop3(ttg_int n, const double* s, double eps);
+/* maxvol row selection of a tall n x r matrix (maxvol0_d maxvol.f90:27-119
+ * and maxvol_d :197-288): writes r row indices (0-based) to p (device) and
+ * the coefficient matrix Z = A * A(p,:)^{-1} (n x r) when Z != NULL. */
+int ttg_dmaxvol(ttg_ctx* ctx, ttg_int n, ttg_int r, const double* A, ttg_int* p, double* Z,
+                double tol, ttg_int maxiters);
+
+/* ---------------------------------------------------------- drivers (host) */
+/* Block eigensolver, tt_eigb tt_eigb.f90:110-436.  ry (d+1) is updated in
+ * place, ry[d] = B on input and output; lambda receives B eigenvalues; the
+ * cores are kept in the context (ttg_result_*).  method = TTG_METHOD_*. */
+int ttg_eigb(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m, const ttg_int* ra,
+             const double* crA, const double* crY0, ttg_int* ry, double eps, ttg_int rmax,
+             double* lambda, ttg_int B, ttg_int nswp, ttg_int max_full_size, int verb,
+             int method);
+/* One symmetric KSL step, ztt_ksl tt_ksl.f90:431-668 (complex, interleaved). */
+int ttg_ksl_z(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m, const ttg_int* ra,
+              const double* crA, const double* crY0, ttg_int* ry, double tau, ttg_int rmax,
+              int verb, int typ, int order, int method);
+/* AMEn linear solve A x = y, tt_amen_solve tt_adapt_als.f90:513-1132
+ * (argument order follows it; rx updated in place). */
+int ttg_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
+                   const ttg_int* ry, const ttg_int* ra, const double* crA, const double* crY,
+                   const double* crX0, ttg_int* rx, double eps, ttg_int rmax, ttg_int kickrank,
+                   ttg_int nswp, int verb, int method);
+/* Results of the last driver call. */
+int ttg_result_size(const ttg_ctx* ctx, ttg_int* nelem);
+int ttg_result_copy(const ttg_ctx* ctx, double* out, ttg_int nelem);   /* real */
+int ttg_zresult_copy(const ttg_ctx* ctx, double* out, ttg_int nelem);  /* complex */
+int ttg_free_result(ttg_ctx* ctx);      /* deallocate_result tt_eigb.f90:60-64 */
+/* counters of the last driver call: total local matvecs, sweeps, residual */
+int ttg_stats(const ttg_ctx* ctx, ttg_int* matvecs, ttg_int* sweeps, double* res,
+              ttg_int* launches);
+/* kernel launches issued by the library since it was loaded (all contexts) */
+ttg_int ttg_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TTGPU_H */

@@ -1,0 +1,212 @@
+// Shared definitions of the tt-fort GB300 sweep library (libttgpu).
+//
+// Layout conventions follow the reference Fortran (column-major, flat arrays):
+//   x    (rx1, m, rx2)        b1, j, b2
+//   y    (ry1, n, ry2)        c1, i, c2
+//   A    (ra1, n, m, ra2)     a1, i, j, a2
+//   phi1 (ry1, rx1, ra1)      c1, b1, a1
+//   phi2 (rx2, ra2, ry2)      b2, a2, c2
+// (ttals.f90:9-32 index comments).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+#include <complex>
+
+#include "../../include/ttgpu.h"
+
+namespace ttg {
+
+using i64 = long long;
+
+// -------------------------------------------------------------------------
+// errors
+// -------------------------------------------------------------------------
+struct Error {
+  int code;
+  std::string msg;
+};
+
+#define TTG_CUDA(call)                                                          \
+  do {                                                                          \
+    cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess) {                                                    \
+      throw ::ttg::Error{TTG_ERR_CUDA, std::string(#call) + ": " +              \
+                                           cudaGetErrorString(e_)};             \
+    }                                                                           \
+  } while (0)
+
+// every kernel launch site is followed by TTG_CHECK_LAUNCH(); it also counts
+// the launches (reported as gpu_launches by the benchmark)
+extern long long g_launches;
+#define TTG_CHECK_LAUNCH()                                                      \
+  do {                                                                          \
+    ++::ttg::g_launches;                                                        \
+    TTG_CUDA(cudaGetLastError());                                               \
+  } while (0)
+
+#define TTG_REQUIRE(cond, msg)                                                  \
+  do {                                                                          \
+    if (!(cond)) throw ::ttg::Error{TTG_ERR_ARG, std::string(msg)};             \
+  } while (0)
+
+// -------------------------------------------------------------------------
+// device workspace: a bump allocator over one growing cudaMalloc block.
+// Allocation happens only at sizing points (never inside a timed inner loop).
+// -------------------------------------------------------------------------
+struct Workspace {
+  char* base = nullptr;
+  size_t cap = 0;
+  size_t top = 0;
+  void reserve(size_t bytes);   // may reallocate: only when nothing is live
+  void* take(size_t bytes);     // 256-byte aligned
+  template <class T> T* takeT(size_t count) { return (T*)take(count * sizeof(T)); }
+  void reset() { top = 0; }
+  void release();
+};
+
+}  // namespace ttg
+
+// The opaque context handed across the C-ABI.  One context per host thread;
+// it replaces the reference's module-level globals (tt_eigb.f90:1-50,
+// tt_ksl.f90:1-166) and module result arrays (result_core, zresult_core).
+struct ttg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  ttg::Workspace ws;          // scratch for kernel-level calls
+  std::string last_error;
+  int verb = 0;
+  // driver results (host copies), freed by ttg_free_result
+  std::vector<double> result_core;
+  std::vector<std::complex<double>> zresult_core;
+  std::vector<long long> result_ry;
+  // counters of the last driver call
+  long long stat_matvecs = 0;
+  long long stat_sweeps = 0;
+  long long stat_launches = 0;
+  double stat_res = 0.0;
+};
+
+namespace ttg {
+
+static inline int ceil_div(i64 a, i64 b) { return (int)((a + b - 1) / b); }
+
+// ---------------------------------------------------------------------------
+// FP64 generic strided batched GEMM (ttg_gemm_f64.cu)
+//   C[m,n] = alpha * sum_k A[m*sAm + k*sAk] * B[k*sBk + n*sBn] + beta * C[...]
+//   batch index b = b1 + nb1*b2, operand offset = b1*s?1 + b2*s?2
+// ---------------------------------------------------------------------------
+struct GemmF64 {
+  int M = 0, N = 0, K = 0;
+  const double* A = nullptr; i64 sAm = 0, sAk = 0;
+  const double* B = nullptr; i64 sBk = 0, sBn = 0;
+  double* C = nullptr;       i64 sCm = 0, sCn = 0;
+  double alpha = 1.0, beta = 0.0;
+  int nb1 = 1, nb2 = 1;
+  i64 bA1 = 0, bA2 = 0, bB1 = 0, bB2 = 0, bC1 = 0, bC2 = 0;
+  int splitk = 1;   // > 1: K split over CTAs, C accumulated with FP64 atomics
+};
+void gemm_f64(const GemmF64& g, cudaStream_t s);
+
+// complex128 variant (KSL path); same strides in units of complex elements.
+struct GemmZ {
+  int M = 0, N = 0, K = 0;
+  const double2* A = nullptr; i64 sAm = 0, sAk = 0; bool conjA = false;
+  const double2* B = nullptr; i64 sBk = 0, sBn = 0; bool conjB = false;
+  double2* C = nullptr;       i64 sCm = 0, sCn = 0;
+  double2 alpha = {1.0, 0.0}, beta = {0.0, 0.0};
+  int nb1 = 1, nb2 = 1;
+  i64 bA1 = 0, bA2 = 0, bB1 = 0, bB2 = 0, bC1 = 0, bC2 = 0;
+  int splitk = 1;
+};
+void gemm_z(const GemmZ& g, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Local operator kernels (ttg_local.cu)
+// ---------------------------------------------------------------------------
+struct LocalDims {
+  i64 rx1, m, rx2, ry1, n, ry2, ra1, ra2;
+  i64 xsize() const { return rx1 * m * rx2; }
+  i64 ysize() const { return ry1 * n * ry2; }
+  i64 t1size() const { return rx1 * m * ra2 * ry2; }
+  i64 t2size() const { return rx1 * ra1 * n * ry2; }
+};
+
+// bfun3 for nvec vectors (x: xsize*nvec contiguous, y: ysize*nvec).
+// scratch: (t1size + t2size) * nvec doubles.
+void bfun3_f64(const LocalDims& L, const double* phi1, const double* A, const double* phi2,
+               const double* x, double* y, int nvec, double* scratch, cudaStream_t s);
+size_t bfun3_f64_scratch(const LocalDims& L, int nvec);
+
+void phi_left_f64(const LocalDims& L, const double* phi1_old, const double* A,
+                  const double* x, const double* y, double* phi1_new, double* scratch,
+                  cudaStream_t s);
+void phi_right_f64(const LocalDims& L, const double* phi2_old, const double* A,
+                   const double* x, const double* y, double* phi2_new, double* scratch,
+                   cudaStream_t s);
+size_t phi_f64_scratch(const LocalDims& L);
+
+void phi2_left_f64(i64 rx1, i64 rx2, i64 ry1, i64 n, i64 ry2, const double* phi1_old,
+                   const double* x, const double* y, double* phi1_new, double* scratch,
+                   cudaStream_t s);
+void phi2_right_f64(i64 rx1, i64 rx2, i64 ry1, i64 n, i64 ry2, const double* phi2_old,
+                    const double* x, const double* y, double* phi2_new, double* scratch,
+                    cudaStream_t s);
+
+// Dense local matrix B[(c1,i,c2),(b1,j,b2)] (d2d_fullmat, tt_eigb.f90:88-105).
+void fullmat_f64(i64 rx1, i64 m, i64 rx2, i64 ra1, i64 ra2, const double* phi1,
+                 const double* A, const double* phi2, double* Bmat, cudaStream_t s);
+
+// complex versions (tt_ksl.f90 K- and S-steps)
+void bfun3_z(const LocalDims& L, const double2* phi1, const double2* A, const double2* phi2,
+             const double2* x, double2* y, int nvec, double2* scratch, cudaStream_t s);
+void bfun3_transp_z(const LocalDims& L, const double2* phi1, const double2* A,
+                    const double2* phi2, const double2* x, double2* y, int nvec,
+                    double2* scratch, cudaStream_t s);
+void phi_left_z(const LocalDims& L, const double2* phi1_old, const double2* A,
+                const double2* x, const double2* y, double2* phi1_new, double2* scratch,
+                cudaStream_t s);
+void phi_right_z(const LocalDims& L, const double2* phi2_old, const double2* A,
+                 const double2* x, const double2* y, double2* phi2_new, double2* scratch,
+                 cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Split-precision (BF16x3, FP32 accumulate) tensor-core local operator
+// (ttg_tc.cu).  Operands are prepared once per local problem.
+// ---------------------------------------------------------------------------
+struct SplitOp;   // opaque prepared operator
+size_t split_op_bytes(const LocalDims& L, int nvec_max);
+void split_op_prepare(SplitOp** op, const LocalDims& L, int nvec_max, const double* phi1,
+                      const double* A, const double* phi2, void* mem, cudaStream_t s);
+void split_op_apply(SplitOp* op, const double* x, double* y, int nvec, cudaStream_t s);
+bool split_op_supported(const LocalDims& L);
+
+// ---------------------------------------------------------------------------
+// Dense FP64 linear algebra (ttg_linalg.cu)
+// ---------------------------------------------------------------------------
+// Symmetric eigen (cyclic Jacobi, one CTA): A (k x k, lda) overwritten,
+// eigenvalues ascending in w, eigenvectors in V (k x k, ldv).  status: iters
+void syev_jacobi(int k, double* A, int lda, double* w, double* V, int ldv, int* status,
+                 cudaStream_t s);
+// One-sided Jacobi SVD of M (p x q, p >= q, ldm = p), in place.  Outputs:
+// sigma (q, descending), U (p x q), Vt (q x q, rows = right singular vectors).
+size_t svd_scratch(int p, int q);
+void svd_jacobi(int p, int q, const double* M, double* U, double* sigma, double* Vt,
+                double* scratch, int* status, cudaStream_t s);
+// Householder QR with LAPACK's convention: A (n x m) -> Q (n x min), R (min x m).
+void qr_householder(int n, int m, double* A, double* R, double* tau, cudaStream_t s);
+void qr_householder_z(int n, int m, double2* A, double2* R, double2* tau, cudaStream_t s);
+
+// small helpers
+void transpose_f64(i64 rows, i64 cols, const double* in, double* out, cudaStream_t s);
+void transpose_z(i64 rows, i64 cols, const double2* in, double2* out, cudaStream_t s);
+void copy_rows_f64(i64 rows_in, i64 rows_out, i64 cols, const double* in, double* out,
+                   cudaStream_t s);   // drow_cut: keep the first rows_out rows
+void scale_cols_f64(i64 rows, i64 cols, double* A, i64 lda, const double* s, cudaStream_t st);
+void scale_rows_f64(i64 rows, i64 cols, double* A, i64 lda, const double* s, cudaStream_t st);
+void fill_f64(double* p, i64 n, double v, cudaStream_t s);
+
+}  // namespace ttg

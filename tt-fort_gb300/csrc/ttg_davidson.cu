@@ -1,0 +1,432 @@
+// Device block Davidson (GD+k).  Step-by-step twin of oracle/davidson.py.
+#include "ttg_davidson.cuh"
+#include <algorithm>
+#include <cmath>
+
+namespace ttg {
+
+static constexpr double CHOL_DROP = 1e-14;
+static constexpr double RESTART_DROP = 1e-10;
+
+int splitk_for(i64 K) { return (int)std::max<i64>(1, std::min<i64>(1024, K / 512)); }
+
+// R[:, j] = AX[:, j] - theta_j X[:, j];  rn2[j] += ||R[:, j]||^2 (rn2 pre-zeroed)
+__global__ void residual_kernel(i64 N, const double* __restrict__ AX, const double* __restrict__ X,
+                                const double* __restrict__ theta, double* __restrict__ R,
+                                double* __restrict__ rn2) {
+  const int j = blockIdx.y;
+  const double th = theta[j];
+  double acc = 0.0;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += (i64)gridDim.x * blockDim.x) {
+    double r = AX[i + N * j] - th * X[i + N * j];
+    R[i + N * j] = r;
+    acc = fma(r, r, acc);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) atomicAdd(&rn2[j], t);
+  }
+}
+
+void residual_cols(i64 N, int nb, const double* AX, const double* X, const double* theta,
+                   double* R, double* rn2, cudaStream_t s) {
+  TTG_CUDA(cudaMemsetAsync(rn2, 0, sizeof(double) * nb, s));
+  int bx = (int)std::max<i64>(1, std::min<i64>(256, (N + 1023) / 1024));
+  residual_kernel<<<dim3(bx, nb), 256, 0, s>>>(N, AX, X, theta, R, rn2);
+  TTG_CHECK_LAUNCH();
+}
+
+__global__ void gather_cols_kernel(i64 N, int t, const int* idx, const double* src, double* dst) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < N * t; e += (i64)gridDim.x * blockDim.x) {
+    i64 i = e % N;
+    int c = (int)(e / N);
+    dst[e] = src[i + N * idx[c]];
+  }
+}
+
+void gather_cols(i64 N, int t, const int* idx, const double* src, double* dst, cudaStream_t s) {
+  int blocks = (int)std::min<i64>(4096, (N * t + 255) / 256);
+  gather_cols_kernel<<<blocks, 256, 0, s>>>(N, t, idx, src, dst);
+  TTG_CHECK_LAUNCH();
+}
+
+// Cholesky with dropping of dependent columns (oracle.davidson.chol_drop).
+// G (t x t, ld t).  Writes Mfull (t x t, ld t): rows of dropped columns are
+// zero, the first nk columns hold L_k^{-T} scattered to the kept rows; kept[t]
+// receives nk.  One thread: t <= 32.
+__global__ void chol_drop_kernel(int t, const double* G, double* Mfull, int* kept, double tol) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double L[32][32];
+  int kp[32];
+  int nk = 0;
+  for (int j = 0; j < t; ++j) {
+    for (int i = 0; i < t; ++i) L[i][j] = 0.0;
+  }
+  for (int j = 0; j < t; ++j) {
+    double gjj = G[j + t * j];
+    double d = gjj;
+    for (int q = 0; q < nk; ++q) d -= L[j][kp[q]] * L[j][kp[q]];
+    if (!(gjj > 0.0) || d <= tol * gjj) continue;
+    double ljj = sqrt(d);
+    L[j][j] = ljj;
+    for (int i = j + 1; i < t; ++i) {
+      double v = G[i + t * j];
+      for (int q = 0; q < nk; ++q) v -= L[i][kp[q]] * L[j][kp[q]];
+      L[i][j] = v / ljj;
+    }
+    kp[nk++] = j;
+  }
+  // Lk = L[kp, kp] (lower), Minv = Lk^{-T} (upper): solve Lk^T Minv = I
+  double Mi[32][32];
+  for (int c = 0; c < nk; ++c) {
+    // column c of Lk^{-T}: x with Lk^T x = e_c  (back substitution)
+    for (int r = nk - 1; r >= 0; --r) {
+      double v = (r == c) ? 1.0 : 0.0;
+      for (int q = r + 1; q < nk; ++q) v -= L[kp[q]][kp[r]] * Mi[q][c];
+      Mi[r][c] = v / L[kp[r]][kp[r]];
+    }
+  }
+  for (int e = 0; e < t * t; ++e) Mfull[e] = 0.0;
+  for (int c = 0; c < nk; ++c)
+    for (int r = 0; r < nk; ++r) Mfull[kp[r] + t * c] = Mi[r][c];
+  kept[t] = nk;
+  for (int q = 0; q < nk; ++q) kept[q] = kp[q];
+}
+
+// GD+k restart coefficients (oracle.davidson.restart_coeffs), one CTA.
+// S (k x k, ld ldS): current Ritz vectors; Sprev (kprev x nb, ld ldP).
+// C (k x kc, ld k) and out[0] = kc.
+__global__ void restart_coeffs_kernel(int k, const double* S, int ldS, int kr, const double* Sprev,
+                                      int kprev, int nb, int ldP, double* C, int* out) {
+  extern __shared__ double sh[];
+  double* Cs = sh;                  // k x (kr + nb)
+  double* p = sh + (size_t)k * (kr + nb);
+  __shared__ double red[33];
+  __shared__ int kc_s;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < k * kr; e += blockDim.x) Cs[e] = S[(e % k) + (size_t)ldS * (e / k)];
+  if (tid == 0) kc_s = kr;
+  __syncthreads();
+  for (int b = 0; b < nb && Sprev; ++b) {
+    for (int i = tid; i < k; i += blockDim.x) p[i] = i < kprev ? Sprev[i + (size_t)ldP * b] : 0.0;
+    __syncthreads();
+    const int kc = kc_s;
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int c = 0; c < kc; ++c) {
+        // dot = C_c . p  (block reduction)
+        double t = 0.0;
+        for (int i = tid; i < k; i += blockDim.x) t += Cs[i + (size_t)k * c] * p[i];
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if ((tid & 31) == 0) red[tid >> 5] = t;
+        __syncthreads();
+        if (tid < 32) {
+          double u = tid < (int)(blockDim.x >> 5) ? red[tid] : 0.0;
+          for (int o = 16; o > 0; o >>= 1) u += __shfl_xor_sync(0xffffffffu, u, o);
+          if (tid == 0) red[32] = u;
+        }
+        __syncthreads();
+        double dot = red[32];
+        for (int i = tid; i < k; i += blockDim.x) p[i] -= Cs[i + (size_t)k * c] * dot;
+        __syncthreads();
+      }
+    }
+    double t = 0.0;
+    for (int i = tid; i < k; i += blockDim.x) t += p[i] * p[i];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((tid & 31) == 0) red[tid >> 5] = t;
+    __syncthreads();
+    if (tid < 32) {
+      double u = tid < (int)(blockDim.x >> 5) ? red[tid] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) u += __shfl_xor_sync(0xffffffffu, u, o);
+      if (tid == 0) red[32] = u;
+    }
+    __syncthreads();
+    double nrm = sqrt(red[32]);
+    if (nrm > RESTART_DROP) {
+      for (int i = tid; i < k; i += blockDim.x) Cs[i + (size_t)k * kc] = p[i] / nrm;
+      __syncthreads();
+      if (tid == 0) kc_s = kc + 1;
+    }
+    __syncthreads();
+  }
+  const int kc = kc_s;
+  for (int e = tid; e < k * kc; e += blockDim.x) C[e] = Cs[e];
+  if (tid == 0) out[0] = kc;
+}
+
+// H (ld ldh): H[0:k+t, k:k+t] = Hn; H[k:k+t, 0:k] = Hn[0:k,:]^T; H[k:,k:] sym.
+__global__ void h_update_kernel(int k, int t, const double* Hn, double* H, int ldh) {
+  const int K = k + t;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < K * t; e += gridDim.x * blockDim.x) {
+    int r = e % K, c = e / K;
+    double v = Hn[r + K * c];
+    if (r < k) {
+      H[r + ldh * (k + c)] = v;
+      H[(k + c) + ldh * r] = v;
+    } else {
+      double w = Hn[(k + c) + K * (r - k)];
+      H[r + ldh * (k + c)] = 0.5 * (v + w);
+    }
+  }
+}
+
+// H = 0.5 (H + H^T), k x k (ld ldh)
+__global__ void symmetrize_kernel(int k, double* H, int ldh) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < k * k; e += gridDim.x * blockDim.x) {
+    int r = e % k, c = e / k;
+    if (r < c) {
+      double v = 0.5 * (H[r + ldh * c] + H[c + ldh * r]);
+      H[r + ldh * c] = v;
+      H[c + ldh * r] = v;
+    }
+  }
+}
+
+__global__ void copy_mat_kernel(int rows, int cols, const double* src, int lds, double* dst, int ldd) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < rows * cols; e += gridDim.x * blockDim.x) {
+    int r = e % rows, c = e / rows;
+    dst[r + ldd * c] = src[r + lds * c];
+  }
+}
+
+static void copy_mat(int rows, int cols, const double* src, int lds, double* dst, int ldd,
+                     cudaStream_t s) {
+  if (rows * cols <= 0) return;
+  int blocks = std::min(1024, (rows * cols + 255) / 256);
+  copy_mat_kernel<<<blocks, 256, 0, s>>>(rows, cols, src, lds, dst, ldd);
+  TTG_CHECK_LAUNCH();
+}
+
+size_t Davidson::bytes(i64 N, int B, int maxb) {
+  size_t nm = (size_t)N * maxb;
+  size_t b = (size_t)maxb * maxb;
+  size_t tot = 0;
+  auto add = [&](size_t cnt) { tot += (cnt * sizeof(double) + 255) & ~size_t(255); };
+  add(nm); add(nm); add(nm); add(nm);            // V W Vt Wt
+  add(b); add(b); add(b); add(maxb);             // H Hs S theta
+  add((size_t)N * B); add((size_t)N * B); add(64);   // AX R rn2
+  add((size_t)N * B); add((size_t)N * B);        // T T2
+  add((size_t)maxb * B); add(64 * 64); add(64 * 64); add((size_t)maxb * B);   // Ct G Mfull Sprev
+  add(b); add(b);                                // C HC
+  add(64); add(64);                              // ikept idx
+  return tot + 4096;
+}
+
+Davidson::Davidson(i64 N, int B, int maxb, int keep, void* mem, double* hostbuf, cudaStream_t s)
+    : N_(N), B_(B), maxb_(maxb), keep_(keep), s_(s), hbuf_(hostbuf) {
+  char* p = (char*)mem;
+  auto take = [&](size_t cnt) {
+    double* r = (double*)p;
+    p += (cnt * sizeof(double) + 255) & ~size_t(255);
+    return r;
+  };
+  size_t nm = (size_t)N * maxb, b = (size_t)maxb * maxb;
+  V_ = take(nm); W_ = take(nm); Vt_ = take(nm); Wt_ = take(nm);
+  H_ = take(b); Hs_ = take(b); S_ = take(b); theta_ = take(maxb);
+  AX_ = take((size_t)N * B); R_ = take((size_t)N * B); rn2_ = take(64);
+  T_ = take((size_t)N * B); T2_ = take((size_t)N * B);
+  Ct_ = take((size_t)maxb * B); G_ = take(64 * 64); Mfull_ = take(64 * 64); Sprev_ = take((size_t)maxb * B);
+  C_ = take(b); HC_ = take(b);
+  ikept_ = (int*)take(64); idx_ = (int*)take(64);
+}
+
+void Davidson::sync() { TTG_CUDA(cudaStreamSynchronize(s_)); }
+
+// BCGS2 of T (N x t) against V[:, :k_]; result written to out (N x nk).
+int Davidson::orth_block(double* T, int t, double* out) {
+  const int sk = splitk_for(N_);
+  double* cur = T;
+  int tc = t;
+  for (int pass = 0; pass < 2; ++pass) {
+    if (k_ > 0) {
+      GemmF64 g;   // Ct (k x tc) = V^T cur
+      g.M = k_; g.N = tc; g.K = (int)N_;
+      g.A = V_; g.sAm = N_; g.sAk = 1;
+      g.B = cur; g.sBk = 1; g.sBn = N_;
+      g.C = Ct_; g.sCm = 1; g.sCn = k_;
+      g.splitk = sk;
+      gemm_f64(g, s_);
+      GemmF64 h;   // cur -= V Ct
+      h.M = (int)N_; h.N = tc; h.K = k_;
+      h.A = V_; h.sAm = 1; h.sAk = N_;
+      h.B = Ct_; h.sBk = 1; h.sBn = k_;
+      h.C = cur; h.sCm = 1; h.sCn = N_;
+      h.alpha = -1.0; h.beta = 1.0;
+      gemm_f64(h, s_);
+    }
+    {
+      GemmF64 g;   // G (tc x tc) = cur^T cur
+      g.M = tc; g.N = tc; g.K = (int)N_;
+      g.A = cur; g.sAm = N_; g.sAk = 1;
+      g.B = cur; g.sBk = 1; g.sBn = N_;
+      g.C = G_; g.sCm = 1; g.sCn = tc;
+      g.splitk = sk;
+      gemm_f64(g, s_);
+    }
+    chol_drop_kernel<<<1, 32, 0, s_>>>(tc, G_, Mfull_, ikept_, CHOL_DROP);
+    TTG_CHECK_LAUNCH();
+    TTG_CUDA(cudaMemcpyAsync(hbuf_, ikept_ + tc, sizeof(int), cudaMemcpyDeviceToHost, s_));
+    sync();
+    int nk = *(int*)hbuf_;
+    if (nk == 0) return 0;
+    double* dst = (pass == 0) ? (cur == T2_ ? T_ : T2_) : out;
+    GemmF64 g;   // dst (N x nk) = cur (N x tc) * Mfull (tc x nk)
+    g.M = (int)N_; g.N = nk; g.K = tc;
+    g.A = cur; g.sAm = 1; g.sAk = N_;
+    g.B = Mfull_; g.sBk = 1; g.sBn = tc;
+    g.C = dst; g.sCm = 1; g.sCn = N_;
+    gemm_f64(g, s_);
+    cur = dst;
+    tc = nk;
+  }
+  return tc;
+}
+
+DavidsonStats Davidson::solve(const MatvecFn& mv, const double* X0, double tol, int max_matvecs,
+                              double* X, double* theta_host) {
+  DavidsonStats st;
+  const int sk = splitk_for(N_);
+  const int ldh = maxb_;
+  k_ = 0;
+  have_prev_ = false;
+  // initial basis: orth(X0), W = A V, H = V^T W
+  TTG_CUDA(cudaMemcpyAsync(T_, X0, sizeof(double) * N_ * B_, cudaMemcpyDeviceToDevice, s_));
+  int t = orth_block(T_, B_, V_);
+  TTG_REQUIRE(t > 0, "davidson: start block has rank zero");
+  mv(V_, W_, t);
+  st.matvecs = t;
+  k_ = t;
+  {
+    GemmF64 g;
+    g.M = k_; g.N = k_; g.K = (int)N_;
+    g.A = V_; g.sAm = N_; g.sAk = 1;
+    g.B = W_; g.sBk = 1; g.sBn = N_;
+    g.C = H_; g.sCm = 1; g.sCn = ldh;
+    g.splitk = sk;
+    gemm_f64(g, s_);
+    symmetrize_kernel<<<1, 256, 0, s_>>>(k_, H_, ldh);
+    TTG_CHECK_LAUNCH();
+  }
+  double anorm = 0.0;
+  int* status = (int*)(hbuf_ + 200);
+  while (true) {
+    st.iters++;
+    const int k = k_;
+    const int nb = std::min(B_, k);
+    copy_mat(k, k, H_, ldh, Hs_, k, s_);
+    syev_jacobi(k, Hs_, k, theta_, S_, k, ikept_ + 40, s_);
+    {
+      GemmF64 g;   // X = V S[:, :nb]
+      g.M = (int)N_; g.N = nb; g.K = k;
+      g.A = V_; g.sAm = 1; g.sAk = N_;
+      g.B = S_; g.sBk = 1; g.sBn = k;
+      g.C = X; g.sCm = 1; g.sCn = N_;
+      gemm_f64(g, s_);
+      g.A = W_; g.C = AX_;   // AX = W S[:, :nb]
+      gemm_f64(g, s_);
+    }
+    residual_cols(N_, nb, AX_, X, theta_, R_, rn2_, s_);
+    TTG_CUDA(cudaMemcpyAsync(hbuf_, theta_, sizeof(double) * k, cudaMemcpyDeviceToHost, s_));
+    TTG_CUDA(cudaMemcpyAsync(hbuf_ + 128, rn2_, sizeof(double) * nb, cudaMemcpyDeviceToHost, s_));
+    sync();
+    (void)status;
+    const double* th = hbuf_;
+    anorm = std::max(anorm, std::max(std::fabs(th[0]), std::fabs(th[k - 1])));
+    int conv[64];
+    int nconv = 0;
+    double res2 = 0.0;
+    for (int j = 0; j < nb; ++j) {
+      double rn = std::sqrt(std::max(0.0, hbuf_[128 + j]));
+      res2 += rn * rn;
+      conv[j] = rn <= tol * anorm;
+      nconv += conv[j];
+      if (!std::isfinite(rn)) throw Error{TTG_ERR_NAN, "davidson: non-finite residual"};
+    }
+    for (int j = 0; j < nb; ++j) theta_host[j] = th[j];
+    st.res = std::sqrt(res2);
+    st.anorm = anorm;
+    if (nconv == nb || st.matvecs >= max_matvecs || k >= N_) {
+      st.converged = (nconv == nb);
+      return st;
+    }
+    // expansion block: unconverged residual columns, in order
+    int* hidx = (int*)(hbuf_ + 256);
+    int tt = 0;
+    for (int j = 0; j < nb; ++j)
+      if (!conv[j]) hidx[tt++] = j;
+    if (k + tt > maxb_) {
+      // GD+k restart
+      const int kr = std::min(keep_, k);
+      size_t shm = sizeof(double) * ((size_t)k * (kr + B_) + k);
+      restart_coeffs_kernel<<<1, 256, shm, s_>>>(k, S_, k, kr, have_prev_ ? Sprev_ : nullptr,
+                                                 kprev_, have_prev_ ? B_ : 0, maxb_, C_,
+                                                 ikept_ + 48);
+      TTG_CHECK_LAUNCH();
+      TTG_CUDA(cudaMemcpyAsync(hbuf_ + 300, ikept_ + 48, sizeof(int), cudaMemcpyDeviceToHost, s_));
+      sync();
+      const int kc = *(int*)(hbuf_ + 300);
+      GemmF64 g;   // Vt = V C, Wt = W C
+      g.M = (int)N_; g.N = kc; g.K = k;
+      g.A = V_; g.sAm = 1; g.sAk = N_;
+      g.B = C_; g.sBk = 1; g.sBn = k;
+      g.C = Vt_; g.sCm = 1; g.sCn = N_;
+      gemm_f64(g, s_);
+      g.A = W_; g.C = Wt_;
+      gemm_f64(g, s_);
+      std::swap(V_, Vt_);
+      std::swap(W_, Wt_);
+      GemmF64 h;   // HC = H C (k x kc)
+      h.M = k; h.N = kc; h.K = k;
+      h.A = H_; h.sAm = 1; h.sAk = ldh;
+      h.B = C_; h.sBk = 1; h.sBn = k;
+      h.C = HC_; h.sCm = 1; h.sCn = k;
+      gemm_f64(h, s_);
+      GemmF64 q;   // H = C^T HC (kc x kc)
+      q.M = kc; q.N = kc; q.K = k;
+      q.A = C_; q.sAm = k; q.sAk = 1;
+      q.B = HC_; q.sBk = 1; q.sBn = k;
+      q.C = H_; q.sCm = 1; q.sCn = ldh;
+      gemm_f64(q, s_);
+      symmetrize_kernel<<<1, 256, 0, s_>>>(kc, H_, ldh);
+      TTG_CHECK_LAUNCH();
+      have_prev_ = false;
+      k_ = kc;
+      tt = std::max(1, std::min(tt, maxb_ - kc));
+    } else {
+      copy_mat(k, nb, S_, k, Sprev_, maxb_, s_);
+      kprev_ = k;
+      have_prev_ = true;
+    }
+    TTG_CUDA(cudaMemcpyAsync(idx_, hidx, sizeof(int) * tt, cudaMemcpyHostToDevice, s_));
+    gather_cols(N_, tt, idx_, R_, T_, s_);
+    const int kk = k_;
+    int tn = orth_block(T_, tt, V_ + N_ * kk);
+    if (tn == 0) {
+      st.converged = false;
+      return st;
+    }
+    mv(V_ + N_ * kk, W_ + N_ * kk, tn);
+    st.matvecs += tn;
+    {
+      GemmF64 g;   // Hn ((kk+tn) x tn) = V[:, :kk+tn]^T W[:, kk:kk+tn]
+      g.M = kk + tn; g.N = tn; g.K = (int)N_;
+      g.A = V_; g.sAm = N_; g.sAk = 1;
+      g.B = W_ + N_ * kk; g.sBk = 1; g.sBn = N_;
+      g.C = HC_; g.sCm = 1; g.sCn = kk + tn;
+      g.splitk = sk;
+      gemm_f64(g, s_);
+      h_update_kernel<<<1, 256, 0, s_>>>(kk, tn, HC_, H_, ldh);
+      TTG_CHECK_LAUNCH();
+    }
+    k_ = kk + tn;
+  }
+}
+
+}  // namespace ttg

@@ -1,0 +1,59 @@
+// Block generalized-Davidson (GD+k) local eigensolver on the device.
+//
+// Replaces the vendored PRIMME call of tt_eigb (tt_eigb.f90:252-290): the
+// start block is the current TT core (initSize = B), the tolerance is
+// eps/sqrt(d)/10 relative to max|theta|, the matvec budget is maxMatvecs =
+// 500, and the restart keeps the current and the previous Ritz vectors
+// (GD+k, primme/restart_d.c:120).  Expansion is blocked (all unconverged
+// residuals per iteration) so that every matvec call is one batched launch
+// sequence.  The basis is kept orthonormal by BCGS2 (block Gram-Schmidt +
+// Cholesky QR, twice).  Every FP64 product runs on the device; the host only
+// reads B residual norms per iteration to decide convergence.
+#pragma once
+#include "ttg_common.cuh"
+#include <functional>
+
+namespace ttg {
+
+using MatvecFn = std::function<void(const double* X, double* Y, int nvec)>;
+
+struct DavidsonStats {
+  int iters = 0;
+  int matvecs = 0;
+  double res = 0.0;      // 2-norm of the B residual norms
+  double anorm = 0.0;
+  bool converged = false;
+};
+
+class Davidson {
+ public:
+  // N: problem size, B: eigenpairs, maxb: basis limit, keep: restart size
+  static size_t bytes(i64 N, int B, int maxb);
+  Davidson(i64 N, int B, int maxb, int keep, void* mem, double* hostbuf, cudaStream_t s);
+  // X0 (N x B) start block; on return X (N x B) Ritz vectors, theta (B, host)
+  DavidsonStats solve(const MatvecFn& mv, const double* X0, double tol, int max_matvecs,
+                      double* X, double* theta_host);
+
+ private:
+  i64 N_;
+  int B_, maxb_, keep_;
+  cudaStream_t s_;
+  double *V_, *W_, *Vt_, *Wt_;
+  double *H_, *Hs_, *S_, *theta_, *AX_, *R_, *rn2_;
+  double *T_, *T2_, *Ct_, *G_, *Mfull_, *Sprev_, *C_, *HC_;
+  int *ikept_, *idx_;
+  double* hbuf_;
+  int k_ = 0;
+  int kprev_ = 0;
+  bool have_prev_ = false;
+  int orth_block(double* T, int t, double* out);   // returns columns kept
+  void sync();
+};
+
+// small kernels shared with other drivers
+void residual_cols(i64 N, int nb, const double* AX, const double* X, const double* theta,
+                   double* R, double* rn2, cudaStream_t s);
+void gather_cols(i64 N, int t, const int* idx, const double* src, double* dst, cudaStream_t s);
+int splitk_for(i64 K);
+
+}  // namespace ttg

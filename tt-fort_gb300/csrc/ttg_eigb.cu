@@ -1,0 +1,365 @@
+// Block-TT ALS eigensolver driver (tt_eigb, tt_eigb.f90:110-436) on the GPU.
+//
+// Every array of the sweep stays in HBM for the whole call: operator cores,
+// TT cores (each with capacity rank_cap * n * rank_cap * B), interface
+// matrices Phi, the Davidson basis and the SVD workspace are carved out of one
+// allocation made before the first sweep.  The host keeps the reference's
+// control flow (sweep order, turn points, stopping rule) and reads back only
+// scalars: B eigenvalues and residual norms per Davidson iteration and the
+// singular values that my_chop3 needs.
+#include "ttg_davidson.cuh"
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+namespace ttg {
+
+void split_matvec_factory(const LocalDims& L, const double* phi1, const double* A,
+                          const double* phi2, int nvec_max, void* mem, cudaStream_t s,
+                          MatvecFn* out);
+size_t split_matvec_bytes(const LocalDims& L, int nvec_max);
+
+struct DevBlock {
+  char* base = nullptr;
+  size_t top = 0, cap = 0;
+  ~DevBlock() { if (base) cudaFree(base); }
+  void alloc(size_t bytes) {
+    if (cudaMalloc(&base, bytes) != cudaSuccess) {
+      base = nullptr;
+      throw Error{TTG_ERR_NOMEM, "tt_eigb: device allocation failed"};
+    }
+    cap = bytes;
+  }
+  template <class T> T* take(size_t count) {
+    size_t b = (count * sizeof(T) + 255) & ~size_t(255);
+    if (top + b > cap) throw Error{TTG_ERR_NOMEM, "tt_eigb: device block exhausted"};
+    T* p = (T*)(base + top);
+    top += b;
+    return p;
+  }
+};
+
+struct PinnedBuf {
+  double* p = nullptr;
+  explicit PinnedBuf(size_t n) { TTG_CUDA(cudaMallocHost(&p, n * sizeof(double))); }
+  ~PinnedBuf() { if (p) cudaFreeHost(p); }
+};
+
+static inline size_t al(size_t bytes) { return (bytes + 255) & ~size_t(255); }
+
+struct EigbParams {
+  int d;
+  std::vector<i64> n, m, ra, ry;
+  const double* crA;
+  const double* crY0;
+  double eps;
+  i64 rmax;
+  int B;
+  int nswp;
+  i64 max_full_size;
+  int verb;
+  int method;
+};
+
+struct EigbOutput {
+  std::vector<double> lambda;
+  std::vector<double> cores;
+  std::vector<i64> ry;
+  long long matvecs = 0;
+  int sweeps = 0;
+  double res = 0.0;
+};
+
+static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
+  cudaStream_t s = ctx->stream;
+  const int d = P.d, B = P.B;
+  auto& n = P.n;
+  auto& ry = P.ry;
+  TTG_REQUIRE(d >= 2, "tt_eigb: d must be >= 2");
+  TTG_REQUIRE(ry[d] == B, "Inconsistent number of eigenvalues sought and initial guess last rank");
+  TTG_REQUIRE(ry[0] == 1 && P.ra[0] == 1 && P.ra[d] == 1, "boundary ranks must be 1");
+  TTG_REQUIRE(B >= 1 && B <= 32, "B must be in [1, 32]");
+  for (int i = 0; i < d; ++i) TTG_REQUIRE(n[i] == P.m[i], "tt_eigb needs square cores (n == m)");
+  const double eps2 = P.eps / std::sqrt((double)d);
+  const double resid_damp = 10.0;
+  const int max_matvecs = 500;
+
+  // operator offsets (compute_ps, matrix_util.f90:242-251)
+  std::vector<i64> pa(d + 1, 0);
+  for (int i = 0; i < d; ++i) pa[i + 1] = pa[i] + P.ra[i] * n[i] * P.m[i] * P.ra[i + 1];
+  // rank capacities
+  std::vector<i64> Rc(d + 1);
+  Rc[0] = 1;
+  Rc[d] = 1;
+  for (int i = 1; i < d; ++i) Rc[i] = std::max(ry[i], P.rmax);
+  std::vector<i64> capc(d), capphi(d + 1);
+  i64 Nmax = 1, capmax = 1;
+  for (int i = 0; i < d; ++i) {
+    capc[i] = Rc[i] * n[i] * Rc[i + 1] * B;
+    if (i == d - 1) capc[i] = std::max(capc[i], ry[d - 1] * n[d - 1] * B);
+    capmax = std::max(capmax, capc[i]);
+    Nmax = std::max(Nmax, Rc[i] * n[i] * Rc[i + 1]);
+  }
+  for (int i = 0; i <= d; ++i) capphi[i] = Rc[i] * Rc[i] * P.ra[i];
+  size_t svdmax = 0;
+  i64 rmaxsvd = 1;
+  for (int i = 0; i < d; ++i) {
+    int p1 = (int)(B * Rc[i]), q1 = (int)(n[i] * Rc[i + 1]);
+    int p2 = (int)(Rc[i] * n[i]), q2 = (int)(Rc[i + 1] * B);
+    svdmax = std::max({svdmax, svd_scratch(p1, q1), svd_scratch(p2, q2)});
+    rmaxsvd = std::max<i64>(rmaxsvd, std::max(std::min(p1, q1), std::min(p2, q2)));
+  }
+  size_t bf_scr = 0, phi_scr = 0, split_bytes = 0;
+  for (int i = 0; i < d; ++i) {
+    LocalDims L{Rc[i], n[i], Rc[i + 1], Rc[i], n[i], Rc[i + 1], P.ra[i], P.ra[i + 1]};
+    bf_scr = std::max(bf_scr, bfun3_f64_scratch(L, B));
+    phi_scr = std::max(phi_scr, phi_f64_scratch(L));
+    if (P.method == TTG_METHOD_SPLIT) split_bytes = std::max(split_bytes, split_matvec_bytes(L, B));
+  }
+  const i64 dense_max = std::min<i64>(P.max_full_size - 1, 512);
+  const int maxb_cap = (int)std::min<i64>(std::max(4 * B, 32), Nmax);
+  TTG_REQUIRE(maxb_cap <= 128, "davidson basis too large");
+
+  size_t total = al(sizeof(double) * pa[d]);
+  for (int i = 0; i < d; ++i) total += al(sizeof(double) * capc[i]);
+  for (int i = 0; i <= d; ++i) total += al(sizeof(double) * capphi[i]);
+  total += al(sizeof(double) * Nmax * B);          // curcr
+  total += 2 * al(sizeof(double) * capmax);        // tmp, tmp2
+  total += al(svdmax) + al(sizeof(double) * capmax) * 2 + al(sizeof(double) * rmaxsvd * 2);
+  total += al(bf_scr) + al(phi_scr) + al(split_bytes);
+  total += 2 * al(sizeof(double) * dense_max * dense_max) + al(sizeof(double) * 512) + al(256);
+  total += al(Davidson::bytes(Nmax, B, maxb_cap));
+  total += 1 << 16;
+  DevBlock mem;
+  mem.alloc(total);
+  double* dA = mem.take<double>(pa[d]);
+  std::vector<double*> cr(d), phi(d + 1);
+  for (int i = 0; i < d; ++i) cr[i] = mem.take<double>(capc[i]);
+  for (int i = 0; i <= d; ++i) phi[i] = mem.take<double>(capphi[i]);
+  double* curcr = mem.take<double>(Nmax * B);
+  double* tmp = mem.take<double>(capmax);
+  double* tmp2 = mem.take<double>(capmax);
+  double* svd_scr = (double*)mem.take<char>(svdmax);
+  double* sU = mem.take<double>(capmax);
+  double* sVt = mem.take<double>(capmax);
+  double* sS = mem.take<double>(rmaxsvd * 2);
+  double* bfs = (double*)mem.take<char>(bf_scr);
+  double* phs = (double*)mem.take<char>(phi_scr);
+  void* split_mem = split_bytes ? (void*)mem.take<char>(split_bytes) : nullptr;
+  double* dH = mem.take<double>(std::max<i64>(1, dense_max * dense_max));
+  double* dV = mem.take<double>(std::max<i64>(1, dense_max * dense_max));
+  double* dw = mem.take<double>(512);
+  int* dst = mem.take<int>(64);
+  void* dav_mem = mem.take<char>(Davidson::bytes(Nmax, B, maxb_cap));
+  PinnedBuf hb(4096 + rmaxsvd * 2);
+  double* hbuf = hb.p;
+
+  // upload operator and start cores
+  TTG_CUDA(cudaMemcpyAsync(dA, P.crA, sizeof(double) * pa[d], cudaMemcpyHostToDevice, s));
+  {
+    i64 off = 0;
+    for (int i = 0; i < d; ++i) {
+      i64 sz = ry[i] * n[i] * ry[i + 1];
+      TTG_CUDA(cudaMemcpyAsync(cr[i], P.crY0 + off, sizeof(double) * sz, cudaMemcpyHostToDevice, s));
+      off += sz;
+    }
+  }
+  fill_f64(phi[0], 1, 1.0, s);
+  fill_f64(phi[d], 1, 1.0, s);
+  auto A_of = [&](int i) { return dA + pa[i]; };
+  auto dimsL = [&](int i) {
+    return LocalDims{ry[i], n[i], ry[i + 1], ry[i], n[i], ry[i + 1], P.ra[i], P.ra[i + 1]};
+  };
+
+  // QR orthogonalisation left to right, tt_eigb.f90:202-217
+  for (int i = 0; i < d; ++i) {
+    i64 rows = ry[i] * n[i];
+    i64 rnew = std::min(rows, ry[i + 1]);
+    qr_householder((int)rows, (int)ry[i + 1], cr[i], tmp, tmp2, s);
+    if (i < d - 1) {
+      GemmF64 g;   // cr[i+1] = R (rnew x ry[i+1]) * cr[i+1] (ry[i+1] x n ry[i+2])
+      g.M = (int)rnew; g.N = (int)(n[i + 1] * ry[i + 2]); g.K = (int)ry[i + 1];
+      g.A = tmp; g.sAm = 1; g.sAk = rnew;
+      g.B = cr[i + 1]; g.sBk = 1; g.sBn = ry[i + 1];
+      g.C = tmp2; g.sCm = 1; g.sCn = rnew;
+      gemm_f64(g, s);
+      TTG_CUDA(cudaMemcpyAsync(cr[i + 1], tmp2, sizeof(double) * rnew * n[i + 1] * ry[i + 2],
+                               cudaMemcpyDeviceToDevice, s));
+      ry[i + 1] = rnew;
+      phi_left_f64(dimsL(i), phi[i], A_of(i), cr[i], cr[i], phi[i + 1], phs, s);
+    }
+  }
+  ry[d] = 1;
+
+  int i = d - 1, dir = -1, swp = 1;
+  double ermax = 0.0, fvold = 0.0, res = 0.0;
+  std::vector<double> lam(B, 0.0);
+  long long total_mv = 0;
+  while (swp <= P.nswp) {
+    const i64 N = ry[i] * n[i] * ry[i + 1];
+    TTG_REQUIRE(N >= B, "local problem smaller than the block size");
+    int nmv = 0;
+    if (N < P.max_full_size && N <= dense_max) {
+      // dense branch: d2d_fullmat + dsyev, tt_eigb.f90:234-249
+      fullmat_f64(ry[i], n[i], ry[i + 1], P.ra[i], P.ra[i + 1], phi[i], A_of(i), phi[i + 1], dH, s);
+      syev_jacobi((int)N, dH, (int)N, dw, dV, (int)N, dst, s);
+      TTG_CUDA(cudaMemcpyAsync(curcr, dV, sizeof(double) * N * B, cudaMemcpyDeviceToDevice, s));
+      TTG_CUDA(cudaMemcpyAsync(hbuf, dw, sizeof(double) * B, cudaMemcpyDeviceToHost, s));
+      TTG_CUDA(cudaStreamSynchronize(s));
+      for (int j = 0; j < B; ++j) lam[j] = hbuf[j];
+      res = 0.0;
+    } else {
+      LocalDims L = dimsL(i);
+      MatvecFn mv;
+      if (P.method == TTG_METHOD_SPLIT) {
+        split_matvec_factory(L, phi[i], A_of(i), phi[i + 1], B, split_mem, s, &mv);
+      } else {
+        const double* p1 = phi[i];
+        const double* Ai = A_of(i);
+        const double* p2 = phi[i + 1];
+        mv = [=](const double* X, double* Y, int nv) { bfun3_f64(L, p1, Ai, p2, X, Y, nv, bfs, s); };
+      }
+      const int maxb = (int)std::min<i64>(std::max(4 * B, 32), N);
+      const int keep = std::min(B + std::max(1, B / 2), std::max(maxb - B, 1));
+      Davidson dav(N, B, maxb, keep, dav_mem, hbuf, s);
+      DavidsonStats st = dav.solve(mv, cr[i], eps2 / resid_damp, max_matvecs, curcr, lam.data());
+      nmv = st.matvecs;
+      res = st.res;
+    }
+    double fv = 0.0;
+    for (int j = 0; j < B; ++j) fv += lam[j];
+    double erloc = (fvold - fv) / std::fabs(fv);
+    ermax = std::max(ermax, erloc);
+    total_mv += nmv;
+    fvold = fv;
+    if (P.verb > 0)
+      fprintf(stderr, "swp: %d i: [%d/%d] loc_size: %lld matvecs: %d res: %.3e ermax: %.3e\n", swp,
+              i + 1, d, (long long)N, nmv, res, ermax);
+
+    if (dir < 0 && i > 0) {
+      // tt_eigb.f90:305-356
+      const int p = (int)(B * ry[i]), q = (int)(n[i] * ry[i + 1]);
+      const int r = std::min(p, q);
+      transpose_f64(N, B, curcr, tmp, s);                // (B ry_i) x (n ry_{i+1})
+      svd_jacobi(p, q, tmp, sU, sS, sVt, svd_scr, dst, s);
+      TTG_CUDA(cudaMemcpyAsync(hbuf, sS, sizeof(double) * r, cudaMemcpyDeviceToHost, s));
+      TTG_CUDA(cudaStreamSynchronize(s));
+      i64 nn = std::min<i64>(ttg_my_chop3(r, hbuf, eps2), P.rmax);
+      copy_rows_f64(r, nn, q, sVt, cr[i], s);             // core i = Vt(1:nn, :)
+      scale_cols_f64(p, nn, sU, p, sS, s);               // U(:, 1:nn) diag(s)
+      transpose_f64(B, ry[i] * nn, sU, tmp, s);          // ry_i x nn x B
+      GemmF64 g;   // cr[i-1] (ry_{i-1} n_{i-1} x nn B) = cr[i-1] * Ut
+      g.M = (int)(ry[i - 1] * n[i - 1]); g.N = (int)(nn * B); g.K = (int)ry[i];
+      g.A = cr[i - 1]; g.sAm = 1; g.sAk = ry[i - 1] * n[i - 1];
+      g.B = tmp; g.sBk = 1; g.sBn = ry[i];
+      g.C = tmp2; g.sCm = 1; g.sCn = ry[i - 1] * n[i - 1];
+      gemm_f64(g, s);
+      TTG_CUDA(cudaMemcpyAsync(cr[i - 1], tmp2, sizeof(double) * ry[i - 1] * n[i - 1] * nn * B,
+                               cudaMemcpyDeviceToDevice, s));
+      ry[i] = nn;
+      phi_right_f64(dimsL(i), phi[i + 1], A_of(i), cr[i], cr[i], phi[i], phs, s);
+    }
+    if (dir > 0 && i < d - 1) {
+      // tt_eigb.f90:357-394
+      const int p = (int)(ry[i] * n[i]), q = (int)(ry[i + 1] * B);
+      const int r = std::min(p, q);
+      svd_jacobi(p, q, curcr, sU, sS, sVt, svd_scr, dst, s);
+      TTG_CUDA(cudaMemcpyAsync(hbuf, sS, sizeof(double) * r, cudaMemcpyDeviceToHost, s));
+      TTG_CUDA(cudaStreamSynchronize(s));
+      i64 nn = std::min<i64>(ttg_my_chop3(r, hbuf, eps2), P.rmax);
+      TTG_CUDA(cudaMemcpyAsync(cr[i], sU, sizeof(double) * p * nn, cudaMemcpyDeviceToDevice, s));
+      copy_rows_f64(r, nn, q, sVt, tmp, s);               // Vt(1:nn,:)  nn x (ry_{i+1} B)
+      scale_rows_f64(nn, q, tmp, nn, sS, s);              // S Vt
+      transpose_f64(nn * ry[i + 1], B, tmp, tmp2, s);    // B x nn x ry_{i+1}
+      GemmF64 g;   // cur (B nn x n ry_{i+2}) = SVt (B nn x ry_{i+1}) * cr[i+1]
+      g.M = (int)(B * nn); g.N = (int)(n[i + 1] * ry[i + 2]); g.K = (int)ry[i + 1];
+      g.A = tmp2; g.sAm = 1; g.sAk = B * nn;
+      g.B = cr[i + 1]; g.sBk = 1; g.sBn = ry[i + 1];
+      g.C = tmp; g.sCm = 1; g.sCn = B * nn;
+      gemm_f64(g, s);
+      transpose_f64(B, nn * n[i + 1] * ry[i + 2], tmp, cr[i + 1], s);
+      ry[i + 1] = nn;
+      phi_left_f64(dimsL(i), phi[i], A_of(i), cr[i], cr[i], phi[i + 1], phs, s);
+    }
+    if (dir > 0 && i == d - 2) {
+      dir = -1;
+      i = d - 1;
+      if (P.verb > 0) {
+        i64 rm = *std::max_element(ry.begin(), ry.begin() + d);
+        fprintf(stderr, "swp: %d er = %.3e rmax:%lld\n", swp, ermax, (long long)rm);
+      }
+      swp++;
+      if (ermax < P.eps) break;
+      ermax = 0.0;
+    } else if (dir < 0 && i == 1) {
+      dir = 1;
+      i = 0;
+    } else {
+      i += dir;
+    }
+  }
+  ry[d] = B;
+  TTG_CUDA(cudaStreamSynchronize(s));
+  i64 tot = 0;
+  for (int k = 0; k < d; ++k) tot += ry[k] * n[k] * ry[k + 1];
+  out.cores.resize(tot);
+  i64 off = 0;
+  for (int k = 0; k < d; ++k) {
+    i64 sz = ry[k] * n[k] * ry[k + 1];
+    TTG_CUDA(cudaMemcpyAsync(out.cores.data() + off, cr[k], sizeof(double) * sz,
+                             cudaMemcpyDeviceToHost, s));
+    off += sz;
+  }
+  TTG_CUDA(cudaStreamSynchronize(s));
+  out.lambda = lam;
+  out.ry = ry;
+  out.matvecs = total_mv;
+  out.sweeps = swp - 1;
+  out.res = res;
+}
+
+}  // namespace ttg
+
+using namespace ttg;
+
+extern "C" int ttg_eigb(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
+                        const ttg_int* ra, const double* crA, const double* crY0, ttg_int* ry,
+                        double eps, ttg_int rmax, double* lambda, ttg_int B, ttg_int nswp,
+                        ttg_int max_full_size, int verb, int method) {
+  if (!ctx) return TTG_ERR_ARG;
+  try {
+    TTG_CUDA(cudaSetDevice(ctx->device));
+    TTG_REQUIRE(d > 0 && n && m && ra && crA && crY0 && ry && lambda, "null argument");
+    TTG_REQUIRE(method == TTG_METHOD_PLAIN || method == TTG_METHOD_SPLIT, "unknown method");
+    EigbParams P;
+    P.d = (int)d;
+    P.n.assign(n, n + d);
+    P.m.assign(m, m + d);
+    P.ra.assign(ra, ra + d + 1);
+    P.ry.assign(ry, ry + d + 1);
+    P.crA = crA;
+    P.crY0 = crY0;
+    P.eps = eps;
+    P.rmax = rmax;
+    P.B = (int)B;
+    P.nswp = (int)(nswp > 0 ? nswp : 20);
+    P.max_full_size = max_full_size > 0 ? max_full_size : 2000;
+    P.verb = verb;
+    P.method = method;
+    long long l0 = g_launches;
+    EigbOutput out;
+    run_eigb(ctx, P, out);
+    for (int k = 0; k <= d; ++k) ry[k] = out.ry[k];
+    for (int k = 0; k < B; ++k) lambda[k] = out.lambda[k];
+    ctx->result_core = std::move(out.cores);
+    ctx->zresult_core.clear();
+    ctx->stat_matvecs = out.matvecs;
+    ctx->stat_sweeps = out.sweeps;
+    ctx->stat_res = out.res;
+    ctx->stat_launches = g_launches - l0;
+  } catch (const ttg::Error& e) {
+    ctx->last_error = e.msg;
+    return e.code;
+  }
+  return TTG_OK;
+}

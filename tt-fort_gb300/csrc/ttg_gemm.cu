@@ -1,0 +1,265 @@
+// FP64 / complex128 strided batched GEMM for the plain (FP64) sweep path.
+//
+// One kernel template covers every dgemm/zgemm call site of the reference's
+// hot path (ttals.f90:20,24,29,161-169,215-223; tt_eigb.f90:208,348,384;
+// tt_ksl.f90:586,614; PRIMME's tall-skinny V'W / V*S products).  Operands are
+// addressed through explicit (row, column) strides, so the reference's
+// dtransp/ztransp passes (ttals.f90:22,26) fold into the index arithmetic
+// instead of running as separate kernels.  A K-split mode with FP64 atomics
+// serves the tall-skinny reductions (K = local problem size, M,N <= 128).
+//
+// Tiles: 256 threads, BK = 16, register-prefetched global loads, shared
+// memory staged epilogue so that stores are coalesced along whichever output
+// stride is unit.
+#include "ttg_common.cuh"
+
+namespace ttg {
+namespace {
+
+template <class T> struct Ops;
+template <> struct Ops<double> {
+  static __device__ __forceinline__ double zero() { return 0.0; }
+  static __device__ __forceinline__ double fma(double a, double b, double c) { return ::fma(a, b, c); }
+  static __device__ __forceinline__ double conj(double a) { return a; }
+  static __device__ __forceinline__ double mul(double a, double b) { return a * b; }
+  static __device__ __forceinline__ double add(double a, double b) { return a + b; }
+  static __device__ __forceinline__ bool is_zero(double a) { return a == 0.0; }
+  static __device__ __forceinline__ void atomic_add(double* p, double v) { atomicAdd(p, v); }
+};
+template <> struct Ops<double2> {
+  static __device__ __forceinline__ double2 zero() { return make_double2(0.0, 0.0); }
+  static __device__ __forceinline__ double2 fma(double2 a, double2 b, double2 c) {
+    c.x = ::fma(a.x, b.x, c.x);
+    c.x = ::fma(-a.y, b.y, c.x);
+    c.y = ::fma(a.x, b.y, c.y);
+    c.y = ::fma(a.y, b.x, c.y);
+    return c;
+  }
+  static __device__ __forceinline__ double2 conj(double2 a) { return make_double2(a.x, -a.y); }
+  static __device__ __forceinline__ double2 mul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  }
+  static __device__ __forceinline__ double2 add(double2 a, double2 b) {
+    return make_double2(a.x + b.x, a.y + b.y);
+  }
+  static __device__ __forceinline__ bool is_zero(double2 a) { return a.x == 0.0 && a.y == 0.0; }
+  static __device__ __forceinline__ void atomic_add(double2* p, double2 v) {
+    atomicAdd(&p->x, v.x);
+    atomicAdd(&p->y, v.y);
+  }
+};
+
+template <class T> struct Args {
+  int M, N, K;
+  const T* A; i64 sAm, sAk;
+  const T* B; i64 sBk, sBn;
+  T* C; i64 sCm, sCn;
+  T alpha, beta;
+  int nb1;
+  i64 bA1, bA2, bB1, bB2, bC1, bC2;
+  int splitk, kchunk;
+  bool conjA, conjB;
+};
+
+constexpr int BK = 16;
+constexpr int NT = 256;
+
+template <class T, int BM, int BN, int TM, int TN>
+__global__ void __launch_bounds__(NT) gemm_kernel(Args<T> g) {
+  using O = Ops<T>;
+  constexpr int TX = BN / TN;          // threads along n
+  constexpr int TY = BM / TM;          // threads along m
+  static_assert(TX * TY == NT, "tile/thread mismatch");
+  constexpr int A_PER = BM * BK / NT;
+  constexpr int B_PER = BN * BK / NT;
+  constexpr int SMEM_AB = BK * (BM + 1) + BK * (BN + 1);
+  constexpr int SMEM_C = BN * (BM + 1);
+  constexpr int SMEM = SMEM_AB > SMEM_C ? SMEM_AB : SMEM_C;
+  __shared__ T smem[SMEM];
+  T* As = smem;                       // [BK][BM+1]
+  T* Bs = smem + BK * (BM + 1);       // [BK][BN+1]
+
+  const int tid = threadIdx.x;
+  const int tx = tid % TX, ty = tid / TX;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const int zb = blockIdx.z / g.splitk, ks = blockIdx.z % g.splitk;
+  const int b1 = zb % g.nb1, b2 = zb / g.nb1;
+  const T* A = g.A + b1 * g.bA1 + b2 * g.bA2;
+  const T* Bp = g.B + b1 * g.bB1 + b2 * g.bB2;
+  T* C = g.C + b1 * g.bC1 + b2 * g.bC2;
+  const int kbeg = ks * g.kchunk;
+  const int kend = min(g.K, kbeg + g.kchunk);
+
+  const bool a_mfast = (g.sAm == 1);
+  const bool b_kfast = (g.sBk == 1);
+
+  T ra[A_PER], rb[B_PER];
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int r = 0; r < A_PER; ++r) {
+      int e = tid + NT * r;
+      int mm, kk;
+      if (a_mfast) { mm = e % BM; kk = e / BM; } else { kk = e % BK; mm = e / BK; }
+      int gm = m0 + mm, gk = k0 + kk;
+      T v = O::zero();
+      if (gm < g.M && gk < kend) v = A[(i64)gm * g.sAm + (i64)gk * g.sAk];
+      ra[r] = g.conjA ? O::conj(v) : v;
+    }
+#pragma unroll
+    for (int r = 0; r < B_PER; ++r) {
+      int e = tid + NT * r;
+      int nn, kk;
+      if (b_kfast) { kk = e % BK; nn = e / BK; } else { nn = e % BN; kk = e / BN; }
+      int gn = n0 + nn, gk = k0 + kk;
+      T v = O::zero();
+      if (gn < g.N && gk < kend) v = Bp[(i64)gk * g.sBk + (i64)gn * g.sBn];
+      rb[r] = g.conjB ? O::conj(v) : v;
+    }
+  };
+  auto store = [&]() {
+#pragma unroll
+    for (int r = 0; r < A_PER; ++r) {
+      int e = tid + NT * r;
+      int mm, kk;
+      if (a_mfast) { mm = e % BM; kk = e / BM; } else { kk = e % BK; mm = e / BK; }
+      As[kk * (BM + 1) + mm] = ra[r];
+    }
+#pragma unroll
+    for (int r = 0; r < B_PER; ++r) {
+      int e = tid + NT * r;
+      int nn, kk;
+      if (b_kfast) { kk = e % BK; nn = e / BK; } else { nn = e % BN; kk = e / BN; }
+      Bs[kk * (BN + 1) + nn] = rb[r];
+    }
+  };
+
+  T acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = O::zero();
+
+  if (kbeg < kend) load(kbeg);
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+    __syncthreads();
+    store();
+    __syncthreads();
+    if (k0 + BK < kend) load(k0 + BK);
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      T av[TM], bv[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) av[i] = As[kk * (BM + 1) + ty + TY * i];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) bv[j] = Bs[kk * (BN + 1) + tx + TX * j];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = O::fma(av[i], bv[j], acc[i][j]);
+    }
+  }
+  __syncthreads();
+  // stage the tile in shared memory, then store along the unit output stride
+  T* Cs = smem;   // [BN][BM+1] (m fastest)
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) Cs[(tx + TX * j) * (BM + 1) + ty + TY * i] = acc[i][j];
+  __syncthreads();
+  const bool c_mfast = (g.sCm == 1) || (g.sCn != 1 && g.sCm < g.sCn);
+  for (int e = tid; e < BM * BN; e += NT) {
+    int mm, nn;
+    if (c_mfast) { mm = e % BM; nn = e / BM; } else { nn = e % BN; mm = e / BN; }
+    int gm = m0 + mm, gn = n0 + nn;
+    if (gm >= g.M || gn >= g.N) continue;
+    T v = O::mul(g.alpha, Cs[nn * (BM + 1) + mm]);
+    T* p = C + (i64)gm * g.sCm + (i64)gn * g.sCn;
+    if (g.splitk > 1) {
+      O::atomic_add(p, v);
+    } else {
+      if (!O::is_zero(g.beta)) v = O::add(v, O::mul(g.beta, *p));
+      *p = v;
+    }
+  }
+}
+
+template <class T>
+__global__ void scale_kernel(T* C, int M, int N, i64 sCm, i64 sCn, int nb1, i64 bC1, i64 bC2,
+                             T beta) {
+  using O = Ops<T>;
+  int b = blockIdx.z;
+  T* Cb = C + (b % nb1) * bC1 + (b / nb1) * bC2;
+  i64 total = (i64)M * N;
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total;
+       e += (i64)gridDim.x * blockDim.x) {
+    int mm = (int)(e % M), nn = (int)(e / M);
+    T* p = Cb + mm * sCm + nn * sCn;
+    *p = O::is_zero(beta) ? O::zero() : O::mul(beta, *p);
+  }
+}
+
+template <class T>
+void launch(Args<T> a, int nbatch, cudaStream_t s) {
+  if (a.M <= 0 || a.N <= 0 || nbatch <= 0) return;
+  if (a.K <= 0) {
+    // C = beta*C
+    int blocks = std::min<i64>(4096, ((i64)a.M * a.N + 255) / 256);
+    scale_kernel<T><<<dim3(blocks, 1, nbatch), 256, 0, s>>>(a.C, a.M, a.N, a.sCm, a.sCn, a.nb1,
+                                                            a.bC1, a.bC2, a.beta);
+    TTG_CHECK_LAUNCH();
+    return;
+  }
+  if (a.splitk < 1) a.splitk = 1;
+  a.kchunk = ceil_div(ceil_div(a.K, a.splitk), BK) * BK;
+  a.splitk = ceil_div(a.K, a.kchunk);
+  if (a.splitk > 1) {
+    int blocks = std::min<i64>(4096, ((i64)a.M * a.N + 255) / 256);
+    scale_kernel<T><<<dim3(blocks, 1, nbatch), 256, 0, s>>>(a.C, a.M, a.N, a.sCm, a.sCn, a.nb1,
+                                                            a.bC1, a.bC2, a.beta);
+    TTG_CHECK_LAUNCH();
+  }
+  TTG_REQUIRE((i64)nbatch * a.splitk < 65536, "gemm: batch*splitk too large");
+  if (a.N <= 16) {
+    constexpr int BM = 128, BN = 16;
+    dim3 grid(ceil_div(a.M, BM), ceil_div(a.N, BN), nbatch * a.splitk);
+    TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
+    gemm_kernel<T, BM, BN, 4, 2><<<grid, NT, 0, s>>>(a);
+  } else if (a.M <= 16) {
+    constexpr int BM = 16, BN = 128;
+    dim3 grid(ceil_div(a.M, BM), ceil_div(a.N, BN), nbatch * a.splitk);
+    TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
+    gemm_kernel<T, BM, BN, 2, 4><<<grid, NT, 0, s>>>(a);
+  } else {
+    if constexpr (sizeof(T) == 8) {
+      constexpr int BM = 64, BN = 64;
+      dim3 grid(ceil_div(a.M, BM), ceil_div(a.N, BN), nbatch * a.splitk);
+      TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
+      gemm_kernel<T, BM, BN, 4, 4><<<grid, NT, 0, s>>>(a);
+    } else {
+      // complex128: 32x32 tiles keep the static shared memory under 48 KB
+      constexpr int BM = 32, BN = 32;
+      dim3 grid(ceil_div(a.M, BM), ceil_div(a.N, BN), nbatch * a.splitk);
+      TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
+      gemm_kernel<T, BM, BN, 2, 2><<<grid, NT, 0, s>>>(a);
+    }
+  }
+  TTG_CHECK_LAUNCH();
+}
+
+}  // namespace
+
+void gemm_f64(const GemmF64& g, cudaStream_t s) {
+  Args<double> a{g.M, g.N, g.K, g.A, g.sAm, g.sAk, g.B, g.sBk, g.sBn, g.C, g.sCm, g.sCn,
+                 g.alpha, g.beta, g.nb1, g.bA1, g.bA2, g.bB1, g.bB2, g.bC1, g.bC2,
+                 g.splitk, 0, false, false};
+  launch<double>(a, g.nb1 * g.nb2, s);
+}
+
+void gemm_z(const GemmZ& g, cudaStream_t s) {
+  Args<double2> a{g.M, g.N, g.K, g.A, g.sAm, g.sAk, g.B, g.sBk, g.sBn, g.C, g.sCm, g.sCn,
+                  g.alpha, g.beta, g.nb1, g.bA1, g.bA2, g.bB1, g.bB2, g.bC1, g.bC2,
+                  g.splitk, 0, g.conjA, g.conjB};
+  launch<double2>(a, g.nb1 * g.nb2, s);
+}
+
+}  // namespace ttg

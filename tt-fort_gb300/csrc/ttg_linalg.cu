@@ -1,0 +1,593 @@
+// Dense FP64 linear algebra of the sweep, on the device.
+//
+//   syev_jacobi   symmetric eigenproblems: the dense local branch
+//                 (dsyev, tt_eigb.f90:238) and the Rayleigh-Ritz projection of
+//                 the local Davidson solver (dsyev in primme/solve_H_d.c:141).
+//                 Cyclic Jacobi, round-robin parallel ordering, one CTA.
+//   svd_jacobi    truncation SVD (dgesvd, tt_eigb.f90:312,361;
+//                 ttnodeop.f90:254).  One-sided (Hestenes) Jacobi on the
+//                 columns, one warp per column pair, all pairs of a round in
+//                 parallel, rounds separated by a grid-wide barrier of one
+//                 cooperative launch.  High relative accuracy of the small
+//                 singular values, which my_chop3 sums.
+//   qr_householder  dgeqrf+dorgqr (dqr, matrix_util.f90:37-61) and
+//                 zgeqrf+zungqr (zqr, :64-90) with LAPACK's reflector
+//                 convention (beta = -sign(alpha)*||x||), so Q and R match the
+//                 reference's up to rounding.
+#include "ttg_common.cuh"
+#include <cooperative_groups.h>
+#include <cfloat>
+
+namespace cg = cooperative_groups;
+
+namespace ttg {
+
+// ---------------------------------------------------------------------------
+// small element-wise helpers
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void transpose_kernel(i64 rows, i64 cols, const T* __restrict__ in, T* __restrict__ out) {
+  __shared__ T tile[32][33];
+  i64 c0 = (i64)blockIdx.x * 32, r0 = (i64)blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    i64 r = r0 + threadIdx.x, c = c0 + k;
+    if (r < rows && c < cols) tile[k][threadIdx.x] = in[r + rows * c];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    i64 c = c0 + threadIdx.x, r = r0 + k;
+    if (r < rows && c < cols) out[c + cols * r] = tile[threadIdx.x][k];
+  }
+}
+
+void transpose_f64(i64 rows, i64 cols, const double* in, double* out, cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return;
+  dim3 grid(ceil_div(cols, 32), ceil_div(rows, 32));
+  TTG_REQUIRE(grid.y < 65536, "transpose: too many rows");
+  transpose_kernel<double><<<grid, dim3(32, 8), 0, s>>>(rows, cols, in, out);
+  TTG_CHECK_LAUNCH();
+}
+void transpose_z(i64 rows, i64 cols, const double2* in, double2* out, cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return;
+  dim3 grid(ceil_div(cols, 32), ceil_div(rows, 32));
+  TTG_REQUIRE(grid.y < 65536, "transpose: too many rows");
+  transpose_kernel<double2><<<grid, dim3(32, 8), 0, s>>>(rows, cols, in, out);
+  TTG_CHECK_LAUNCH();
+}
+
+__global__ void copy_rows_kernel(i64 rin, i64 rout, i64 cols, const double* in, double* out) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < rout * cols;
+       e += (i64)gridDim.x * blockDim.x) {
+    i64 r = e % rout, c = e / rout;
+    out[e] = in[r + rin * c];
+  }
+}
+void copy_rows_f64(i64 rows_in, i64 rows_out, i64 cols, const double* in, double* out,
+                   cudaStream_t s) {
+  if (rows_out * cols <= 0) return;
+  int blocks = (int)std::min<i64>(4096, (rows_out * cols + 255) / 256);
+  copy_rows_kernel<<<blocks, 256, 0, s>>>(rows_in, rows_out, cols, in, out);
+  TTG_CHECK_LAUNCH();
+}
+
+__global__ void scale_cols_kernel(i64 rows, i64 cols, double* A, i64 lda, const double* sv) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < rows * cols;
+       e += (i64)gridDim.x * blockDim.x) {
+    i64 r = e % rows, c = e / rows;
+    A[r + lda * c] *= sv[c];
+  }
+}
+__global__ void scale_rows_kernel(i64 rows, i64 cols, double* A, i64 lda, const double* sv) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < rows * cols;
+       e += (i64)gridDim.x * blockDim.x) {
+    i64 r = e % rows, c = e / rows;
+    A[r + lda * c] *= sv[r];
+  }
+}
+void scale_cols_f64(i64 rows, i64 cols, double* A, i64 lda, const double* sv, cudaStream_t s) {
+  if (rows * cols <= 0) return;
+  int blocks = (int)std::min<i64>(4096, (rows * cols + 255) / 256);
+  scale_cols_kernel<<<blocks, 256, 0, s>>>(rows, cols, A, lda, sv);
+  TTG_CHECK_LAUNCH();
+}
+void scale_rows_f64(i64 rows, i64 cols, double* A, i64 lda, const double* sv, cudaStream_t s) {
+  if (rows * cols <= 0) return;
+  int blocks = (int)std::min<i64>(4096, (rows * cols + 255) / 256);
+  scale_rows_kernel<<<blocks, 256, 0, s>>>(rows, cols, A, lda, sv);
+  TTG_CHECK_LAUNCH();
+}
+
+__global__ void fill_kernel(double* p, i64 n, double v) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x)
+    p[e] = v;
+}
+void fill_f64(double* p, i64 n, double v, cudaStream_t s) {
+  if (n <= 0) return;
+  int blocks = (int)std::min<i64>(4096, (n + 255) / 256);
+  fill_kernel<<<blocks, 256, 0, s>>>(p, n, v);
+  TTG_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// block reductions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int NT>
+__device__ double block_sum(double v, double* red) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    double t = lane < NT / 32 ? red[lane] : 0.0;
+    t = warp_sum(t);
+    if (lane == 0) red[32] = t;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+// round-robin ("circle") pairing of K (even) players, round r in [0, K-1)
+__device__ __forceinline__ void rr_pair(int K, int r, int i, int& a, int& b) {
+  if (i == 0) { a = r; b = K - 1; }
+  else { a = (r + i) % (K - 1); b = (r - i + K - 1) % (K - 1); }
+}
+
+// ---------------------------------------------------------------------------
+// symmetric eigensolver: cyclic Jacobi in one CTA
+// ---------------------------------------------------------------------------
+constexpr int JAC_NT = 1024;
+constexpr int JAC_MAX_SWEEPS = 40;
+
+__global__ void __launch_bounds__(JAC_NT) syev_jacobi_kernel(int k, double* Ag, int lda,
+                                                             double* w, double* Vg, int ldv,
+                                                             int* status, int smem_mode) {
+  extern __shared__ double dyn[];
+  __shared__ double red[33];
+  __shared__ double cs[512], sn[512];
+  __shared__ int rot_count;
+  const int tid = threadIdx.x;
+  double* A;
+  double* V;
+  int la, lv;
+  if (smem_mode) {
+    A = dyn; V = dyn + (i64)k * k; la = k; lv = k;
+    for (int e = tid; e < k * k; e += JAC_NT) A[e] = Ag[(e % k) + (i64)lda * (e / k)];
+  } else {
+    A = Ag; V = Vg; la = lda; lv = ldv;
+  }
+  for (int e = tid; e < k * k; e += JAC_NT) V[(e % k) + (i64)lv * (e / k)] = (e % k == e / k) ? 1.0 : 0.0;
+  __syncthreads();
+  const int K = (k + 1) & ~1;
+  const int npairs = K / 2;
+  int sweep = 0;
+  double fro2 = 0.0;
+  {
+    double t = 0.0;
+    for (int e = tid; e < k * k; e += JAC_NT) { double v = A[(e % k) + (i64)la * (e / k)]; t += v * v; }
+    fro2 = block_sum<JAC_NT>(t, red);
+  }
+  for (sweep = 0; sweep < JAC_MAX_SWEEPS && k > 1; ++sweep) {
+    if (tid == 0) rot_count = 0;
+    __syncthreads();
+    for (int r = 0; r < K - 1; ++r) {
+      // rotation parameters of every pair of this round
+      for (int pi = tid; pi < npairs; pi += JAC_NT) {
+        int p, q;
+        rr_pair(K, r, pi, p, q);
+        double c = 1.0, s = 0.0;
+        if (p < k && q < k) {
+          double app = A[p + (i64)la * p], aqq = A[q + (i64)la * q], apq = A[p + (i64)la * q];
+          if (apq != 0.0 && fabs(apq) > 1e-18 * sqrt(fro2) &&
+              fabs(apq) > DBL_EPSILON * 0.5 * sqrt(fabs(app) * fabs(aqq))) {
+            double theta = (aqq - app) / (2.0 * apq);
+            double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+            c = 1.0 / sqrt(t * t + 1.0);
+            s = t * c;
+            atomicAdd(&rot_count, 1);
+          }
+        }
+        cs[pi] = c; sn[pi] = s;
+      }
+      __syncthreads();
+      // rows: A <- J^T A
+      for (int e = tid; e < npairs * k; e += JAC_NT) {
+        int pi = e / k, j = e % k;
+        double c = cs[pi], s = sn[pi];
+        if (s == 0.0) continue;
+        int p, q;
+        rr_pair(K, r, pi, p, q);
+        double ap = A[p + (i64)la * j], aq = A[q + (i64)la * j];
+        A[p + (i64)la * j] = c * ap - s * aq;
+        A[q + (i64)la * j] = s * ap + c * aq;
+      }
+      __syncthreads();
+      // columns: A <- A J, V <- V J
+      for (int e = tid; e < npairs * k; e += JAC_NT) {
+        int pi = e / k, i = e % k;
+        double c = cs[pi], s = sn[pi];
+        if (s == 0.0) continue;
+        int p, q;
+        rr_pair(K, r, pi, p, q);
+        double ap = A[i + (i64)la * p], aq = A[i + (i64)la * q];
+        A[i + (i64)la * p] = c * ap - s * aq;
+        A[i + (i64)la * q] = s * ap + c * aq;
+        double vp = V[i + (i64)lv * p], vq = V[i + (i64)lv * q];
+        V[i + (i64)lv * p] = c * vp - s * vq;
+        V[i + (i64)lv * q] = s * vp + c * vq;
+      }
+      __syncthreads();
+    }
+    if (rot_count == 0) break;
+    __syncthreads();
+  }
+  // eigenvalues ascending (stable rank sort), vectors permuted accordingly
+  __shared__ int rank_s[512];
+  double* wtmp = cs;   // k <= 512
+  for (int i = tid; i < k; i += JAC_NT) wtmp[i] = A[i + (i64)la * i];
+  __syncthreads();
+  // when V is the output buffer itself, stash it in A's storage first
+  double* Vsrc = V;
+  int lsrc = lv;
+  if (!smem_mode) {
+    for (int e = tid; e < k * k; e += JAC_NT)
+      A[(e % k) + (i64)la * (e / k)] = V[(e % k) + (i64)lv * (e / k)];
+    Vsrc = A; lsrc = la;
+  }
+  for (int i = tid; i < k; i += JAC_NT) {
+    double wi = wtmp[i];
+    int rk = 0;
+    for (int j = 0; j < k; ++j) {
+      double wj = wtmp[j];
+      rk += (wj < wi) || (wj == wi && j < i);
+    }
+    rank_s[i] = rk;
+  }
+  __syncthreads();
+  for (int e = tid; e < k * k; e += JAC_NT) {
+    int i = e % k, j = e / k;
+    Vg[i + (i64)ldv * rank_s[j]] = Vsrc[i + (i64)lsrc * j];
+  }
+  for (int i = tid; i < k; i += JAC_NT) w[rank_s[i]] = wtmp[i];
+  if (tid == 0 && status) *status = sweep;
+}
+
+void syev_jacobi(int k, double* A, int lda, double* w, double* V, int ldv, int* status,
+                 cudaStream_t s) {
+  if (k <= 0) return;
+  TTG_REQUIRE(k <= 512, "syev_jacobi: k > 512");
+  size_t smem = (size_t)2 * k * k * sizeof(double);
+  int mode = smem <= 200 * 1024 ? 1 : 0;
+  if (mode) {
+    static bool attr_set = false;
+    if (!attr_set) {
+      TTG_CUDA(cudaFuncSetAttribute(syev_jacobi_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      attr_set = true;
+    }
+  } else {
+    smem = 0;
+  }
+  syev_jacobi_kernel<<<1, JAC_NT, smem, s>>>(k, A, lda, w, V, ldv, status, mode);
+  TTG_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------
+// one-sided Jacobi SVD (cooperative launch, grid barrier between rounds)
+// ---------------------------------------------------------------------------
+constexpr int SVD_NT = 256;
+constexpr int SVD_MAX_SWEEPS = 60;
+
+__global__ void __launch_bounds__(SVD_NT) svd_rotate_kernel(int p, int q, double* M, double* V,
+                                                            int* counters, int* status) {
+  cg::grid_group grid = cg::this_grid();
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * SVD_NT + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * SVD_NT) >> 5;
+  const int K = (q + 1) & ~1;
+  const int npairs = K / 2;
+  const double tol = sqrt((double)p) * DBL_EPSILON;
+  // V = I
+  for (i64 e = blockIdx.x * (i64)SVD_NT + threadIdx.x; e < (i64)q * q; e += (i64)gridDim.x * SVD_NT)
+    V[e] = (e % q == e / q) ? 1.0 : 0.0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) { counters[0] = 0; counters[1] = 0; }
+  grid.sync();
+  int sweep = 0;
+  for (sweep = 0; sweep < SVD_MAX_SWEEPS; ++sweep) {
+    int* cnt = counters + (sweep & 1);
+    for (int r = 0; r < K - 1; ++r) {
+      for (int pi = gw; pi < npairs; pi += nw) {
+        int a, b;
+        rr_pair(K, r, pi, a, b);
+        if (a >= q || b >= q) continue;
+        double* ca = M + (i64)p * a;
+        double* cb = M + (i64)p * b;
+        double al = 0.0, be = 0.0, ga = 0.0;
+        for (int i = lane; i < p; i += 32) {
+          double x = ca[i], y = cb[i];
+          al = fma(x, x, al); be = fma(y, y, be); ga = fma(x, y, ga);
+        }
+        al = warp_sum(al); be = warp_sum(be); ga = warp_sum(ga);
+        if (ga == 0.0 || !(fabs(ga) > tol * sqrt(al * be))) continue;
+        double zeta = (be - al) / (2.0 * ga);
+        double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        double c = 1.0 / sqrt(1.0 + t * t);
+        double s = c * t;
+        for (int i = lane; i < p; i += 32) {
+          double x = ca[i], y = cb[i];
+          ca[i] = c * x - s * y;
+          cb[i] = s * x + c * y;
+        }
+        double* va = V + (i64)q * a;
+        double* vb = V + (i64)q * b;
+        for (int i = lane; i < q; i += 32) {
+          double x = va[i], y = vb[i];
+          va[i] = c * x - s * y;
+          vb[i] = s * x + c * y;
+        }
+        if (lane == 0) atomicAdd(cnt, 1);
+      }
+      grid.sync();
+    }
+    int done = (*((volatile int*)cnt) == 0);
+    grid.sync();
+    if (blockIdx.x == 0 && threadIdx.x == 0) counters[(sweep + 1) & 1] = 0;
+    grid.sync();
+    if (done) break;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && status) *status = sweep;
+}
+
+// sigma_j = ||M_j||, rank sort descending, write U (normalised), sigma, Vt
+__global__ void svd_finish_kernel(int p, int q, const double* M, const double* V, double* U,
+                                  double* sigma, double* Vt, double* nrm, int* rank) {
+  // phase 1 (all blocks): column norms, one warp per column
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int j = gw; j < q; j += nw) {
+    double s = 0.0;
+    for (int i = lane; i < p; i += 32) { double x = M[i + (i64)p * j]; s = fma(x, x, s); }
+    s = warp_sum(s);
+    if (lane == 0) nrm[j] = sqrt(s);
+  }
+}
+
+__global__ void svd_rank_kernel(int q, const double* nrm, int* rank) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < q; j += gridDim.x * blockDim.x) {
+    double v = nrm[j];
+    int rk = 0;
+    for (int t = 0; t < q; ++t) rk += (nrm[t] > v) || (nrm[t] == v && t < j);
+    rank[j] = rk;
+  }
+}
+
+__global__ void svd_gather_kernel(int p, int q, const double* M, const double* V,
+                                  const double* nrm, const int* rank, double* U,
+                                  double* sigma, double* Vt) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)p * q;
+       e += (i64)gridDim.x * blockDim.x) {
+    int i = (int)(e % p), j = (int)(e / p);
+    double s = nrm[j];
+    U[i + (i64)p * rank[j]] = s > 0 ? M[e] / s : (i == j ? 1.0 : 0.0);
+  }
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)q * q;
+       e += (i64)gridDim.x * blockDim.x) {
+    int i = (int)(e % q), j = (int)(e / q);
+    // Vt row rank[j] = V column j
+    Vt[rank[j] + (i64)q * i] = V[e];
+  }
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < q; j += gridDim.x * blockDim.x)
+    sigma[rank[j]] = nrm[j];
+}
+
+size_t svd_scratch(int p, int q) {
+  // working copy of M (max(p,q) x min(p,q)), V (min^2), norms, ranks, counters, Ut
+  size_t pp = std::max(p, q), qq = std::min(p, q);
+  return (pp * qq + qq * qq + 2 * qq + 64) * sizeof(double) + pp * qq * sizeof(double);
+}
+
+static void svd_tall(int p, int q, double* Mw, double* U, double* sigma, double* Vt,
+                     double* V, double* nrm, int* rank, int* counters, int* status,
+                     cudaStream_t s) {
+  // Mw (p x q, p >= q) is overwritten
+  int npairs = (q + 1) / 2;
+  int blocks = std::max(1, ceil_div(npairs, SVD_NT / 32));
+  static int max_coop = -1;
+  if (max_coop < 0) {
+    int dev, nsm, per;
+    TTG_CUDA(cudaGetDevice(&dev));
+    TTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    TTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, svd_rotate_kernel, SVD_NT, 0));
+    max_coop = nsm * per;
+  }
+  blocks = std::min(blocks, max_coop);
+  void* args[] = {&p, &q, &Mw, &V, &counters, &status};
+  TTG_CUDA(cudaLaunchCooperativeKernel((void*)svd_rotate_kernel, dim3(blocks), dim3(SVD_NT),
+                                       args, 0, s));
+  ++g_launches;
+  int nb = std::max(1, std::min(1024, ceil_div((i64)q * 32, 256)));
+  svd_finish_kernel<<<nb, 256, 0, s>>>(p, q, Mw, V, U, sigma, Vt, nrm, rank);
+  TTG_CHECK_LAUNCH();
+  svd_rank_kernel<<<ceil_div(q, 256), 256, 0, s>>>(q, nrm, rank);
+  TTG_CHECK_LAUNCH();
+  int gb = (int)std::min<i64>(4096, ((i64)p * q + 255) / 256);
+  svd_gather_kernel<<<gb, 256, 0, s>>>(p, q, Mw, V, nrm, rank, U, sigma, Vt);
+  TTG_CHECK_LAUNCH();
+}
+
+// Thin SVD of M (p x q, column-major):  M = U diag(sigma) Vt
+//   U (p x r), sigma (r), Vt (r x q), r = min(p, q)
+void svd_jacobi(int p, int q, const double* M, double* U, double* sigma, double* Vt,
+                double* scratch, int* status, cudaStream_t s) {
+  if (p <= 0 || q <= 0) return;
+  int r = std::min(p, q);
+  double* Mw = scratch;                                   // max x min
+  double* V = Mw + (size_t)std::max(p, q) * r;            // r x r
+  double* nrm = V + (size_t)r * r;                        // r
+  int* rank = (int*)(nrm + r);                            // r ints (<= r doubles)
+  int* counters = (int*)(nrm + 2 * r);                    // 2 ints
+  double* T = nrm + 2 * r + 64;                           // max x min (for p < q)
+  if (p >= q) {
+    TTG_CUDA(cudaMemcpyAsync(Mw, M, sizeof(double) * (size_t)p * q, cudaMemcpyDeviceToDevice, s));
+    svd_tall(p, q, Mw, U, sigma, Vt, V, nrm, rank, counters, status, s);
+  } else {
+    // M^T = V S U^T: run on the q x p transpose, then U_M = Vt_T^T, Vt_M = U_T^T
+    transpose_f64(p, q, M, Mw, s);                        // Mw: q x p
+    double* UT = T;                                       // q x p   (left vectors of M^T)
+    double* VtT = U;                                      // p x p   written into U's storage
+    svd_tall(q, p, Mw, UT, sigma, VtT, V, nrm, rank, counters, status, s);
+    // U (p x p) = VtT^T ; VtT currently occupies U: transpose through Mw
+    TTG_CUDA(cudaMemcpyAsync(Mw, VtT, sizeof(double) * (size_t)p * p, cudaMemcpyDeviceToDevice, s));
+    transpose_f64(p, p, Mw, U, s);
+    // Vt (p x q) = UT^T
+    transpose_f64(q, p, UT, Vt, s);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Householder QR, one CTA, LAPACK reflector convention (real and complex)
+// ---------------------------------------------------------------------------
+template <class T> struct CT;
+template <> struct CT<double> {
+  static __device__ double conj(double a) { return a; }
+  static __device__ double abs2(double a) { return a * a; }
+  static __device__ double re(double a) { return a; }
+  static __device__ double im(double) { return 0.0; }
+  static __device__ double mk(double r, double) { return r; }
+  static __device__ double mul(double a, double b) { return a * b; }
+  static __device__ double sub(double a, double b) { return a - b; }
+  static __device__ double add(double a, double b) { return a + b; }
+  static __device__ double scal(double a, double s) { return a * s; }
+};
+template <> struct CT<double2> {
+  static __device__ double2 conj(double2 a) { return make_double2(a.x, -a.y); }
+  static __device__ double abs2(double2 a) { return a.x * a.x + a.y * a.y; }
+  static __device__ double re(double2 a) { return a.x; }
+  static __device__ double im(double2 a) { return a.y; }
+  static __device__ double2 mk(double r, double i) { return make_double2(r, i); }
+  static __device__ double2 mul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  }
+  static __device__ double2 sub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+  static __device__ double2 add(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+  static __device__ double2 scal(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+};
+
+__device__ __forceinline__ double2 warp_sum2(double2 v) {
+  v.x = warp_sum(v.x);
+  v.y = warp_sum(v.y);
+  return v;
+}
+__device__ __forceinline__ double warp_sum2(double v) { return warp_sum(v); }
+
+constexpr int QR_NT = 1024;
+
+// complex reciprocal 1/a
+__device__ __forceinline__ double2 crecip(double2 a) {
+  double d = a.x * a.x + a.y * a.y;
+  return make_double2(a.x / d, -a.y / d);
+}
+__device__ __forceinline__ double crecip(double a) { return 1.0 / a; }
+
+template <class T>
+__global__ void __launch_bounds__(QR_NT) qr_kernel(int n, int m, T* A, T* R, T* tau) {
+  using C = CT<T>;
+  __shared__ double red[33];
+  __shared__ T s_tau, s_beta;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int nwarp = QR_NT / 32;
+  const int r = min(n, m);
+  for (int j = 0; j < r; ++j) {
+    T* col = A + (i64)n * j;
+    double t = 0.0;
+    for (int i = j + 1 + tid; i < n; i += QR_NT) t += C::abs2(col[i]);
+    double xnorm2 = block_sum<QR_NT>(t, red);
+    if (tid == 0) {
+      T alpha = col[j];
+      double alphr = C::re(alpha), alphi = C::im(alpha);
+      if (xnorm2 == 0.0 && alphi == 0.0) {
+        s_tau = C::mk(0.0, 0.0);
+        s_beta = alpha;
+      } else {
+        double nrm = sqrt(alphr * alphr + alphi * alphi + xnorm2);
+        double beta = alphr >= 0 ? -nrm : nrm;
+        s_tau = C::mk((beta - alphr) / beta, -alphi / beta);
+        s_beta = C::mk(beta, 0.0);
+      }
+      tau[j] = s_tau;
+    }
+    __syncthreads();
+    T tj = s_tau;
+    T alpha = col[j];
+    if (!(C::re(tj) == 0.0 && C::im(tj) == 0.0)) {
+      T sc = crecip(C::sub(alpha, s_beta));
+      for (int i = j + 1 + tid; i < n; i += QR_NT) col[i] = C::mul(col[i], sc);
+    }
+    __syncthreads();
+    if (tid == 0) col[j] = s_beta;
+    __syncthreads();
+    // apply H^H = I - conj(tau) v v^H to A[j:, j+1:m]   (zgeqr2: zlarf with conjg(tau))
+    T ctau = C::conj(tj);
+    if (!(C::re(tj) == 0.0 && C::im(tj) == 0.0)) {
+      for (int c = j + 1 + wid; c < m; c += nwarp) {
+        T* cc = A + (i64)n * c;
+        T w = lane == 0 ? cc[j] : C::mk(0.0, 0.0);
+        for (int i = j + 1 + lane; i < n; i += 32) w = C::add(w, C::mul(C::conj(col[i]), cc[i]));
+        w = warp_sum2(w);
+        T f = C::mul(ctau, w);
+        if (lane == 0) cc[j] = C::sub(cc[j], f);
+        for (int i = j + 1 + lane; i < n; i += 32) cc[i] = C::sub(cc[i], C::mul(col[i], f));
+      }
+    }
+    __syncthreads();
+  }
+  // R (r x m): upper triangle
+  for (i64 e = tid; e < (i64)r * m; e += QR_NT) {
+    int i = (int)(e % r), c = (int)(e / r);
+    R[e] = (i <= c) ? A[i + (i64)n * c] : C::mk(0.0, 0.0);
+  }
+  __syncthreads();
+  // form Q in place (dorg2r / zung2r), columns 0..r-1
+  for (int j = r - 1; j >= 0; --j) {
+    T* col = A + (i64)n * j;
+    T tj = tau[j];
+    if (j < r - 1) {
+      // apply H(j) = I - tau v v^H to A[j:, j+1:r] from the left, v(j) = 1
+      for (int c = j + 1 + wid; c < r; c += nwarp) {
+        T* cc = A + (i64)n * c;
+        T w = lane == 0 ? cc[j] : C::mk(0.0, 0.0);
+        for (int i = j + 1 + lane; i < n; i += 32) w = C::add(w, C::mul(C::conj(col[i]), cc[i]));
+        w = warp_sum2(w);
+        T f = C::mul(tj, w);
+        if (lane == 0) cc[j] = C::sub(cc[j], f);
+        for (int i = j + 1 + lane; i < n; i += 32) cc[i] = C::sub(cc[i], C::mul(col[i], f));
+      }
+    }
+    __syncthreads();
+    T mt = C::sub(C::mk(0.0, 0.0), tj);
+    for (int i = j + 1 + tid; i < n; i += QR_NT) col[i] = C::mul(col[i], mt);
+    if (tid == 0) col[j] = C::sub(C::mk(1.0, 0.0), tj);
+    for (int i = tid; i < j; i += QR_NT) col[i] = C::mk(0.0, 0.0);
+    __syncthreads();
+  }
+}
+
+void qr_householder(int n, int m, double* A, double* R, double* tau, cudaStream_t s) {
+  if (n <= 0 || m <= 0) return;
+  qr_kernel<double><<<1, QR_NT, 0, s>>>(n, m, A, R, tau);
+  TTG_CHECK_LAUNCH();
+}
+void qr_householder_z(int n, int m, double2* A, double2* R, double2* tau, cudaStream_t s) {
+  if (n <= 0 || m <= 0) return;
+  qr_kernel<double2><<<1, QR_NT, 0, s>>>(n, m, A, R, tau);
+  TTG_CHECK_LAUNCH();
+}
+
+}  // namespace ttg

@@ -1,0 +1,311 @@
+"""Python mirror of the tt-fort sweep interface, backed by libttgpu.so (CUDA).
+
+Driver calls mirror the reference's Fortran entry points and argument meaning:
+
+  tt_eigb(d, n, m, ra, crA, crY0, ry, eps, rmax, B, ...)      tt_eigb.f90:110
+  ztt_ksl(d, n, m, ra, crA, crY0, ry, tau, rmax, ...)        tt_ksl.f90:431
+  tt_amen_solve(d, n, m, ry, ra, crA, crY, crX0, rx, eps, ...) tt_adapt_als.f90:513
+
+They take host (numpy) arrays in the reference's flat column-major layout and
+return the result cores (the reference's module array ``result_core``) with
+the updated ranks.  Kernel-level calls (``dbfun3``, ``dphi_left`` ...) take
+torch CUDA tensors and run on the device.  There is no CPU fallback: every
+call goes through the CUDA library, and importing fails loudly when the
+library has not been built.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import operators  # noqa: F401  (input builders)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libttgpu.so")
+
+TTG_OK = 0
+TTG_ERR_UNSUPPORTED = -7
+METHOD = {"plain": 0, "split": 1}
+
+_i64 = C.c_int64
+_i64p = C.POINTER(C.c_int64)
+_dp = C.c_void_p
+_lib = None
+
+
+class TTGError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"ttgpu error {code}: {msg}")
+        self.code = code
+
+
+def lib():
+    """Load libttgpu.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with tt-fort_gb300/ttgpu/build.py "
+                "(or __graft_entry__.build()); there is no CPU fallback")
+        L = C.CDLL(LIB_PATH)
+        L.ttg_last_error.restype = C.c_char_p
+        L.ttg_last_error.argtypes = [C.c_void_p]
+        L.ttg_my_chop3.restype = _i64
+        L.ttg_my_chop3.argtypes = [_i64, C.c_void_p, C.c_double]
+        L.ttg_launch_count.restype = _i64
+        _lib = L
+    return _lib
+
+
+# every symbol declared in include/ttgpu.h
+EXPORTED = [
+    "ttg_create", "ttg_destroy", "ttg_last_error", "ttg_set_stream", "ttg_synchronize",
+    "ttg_version", "ttg_dbfun3", "ttg_dbfun3_split", "ttg_zbfun3", "ttg_zbfun3_transp",
+    "ttg_dphi_left", "ttg_dphi_right", "ttg_zphi_left", "ttg_zphi_right", "ttg_dphi2_left",
+    "ttg_dphi2_right", "ttg_d2d_fullmat", "ttg_dqr", "ttg_zqr", "ttg_dsyev", "ttg_dgesvd",
+    "ttg_my_chop3", "ttg_dmaxvol", "ttg_eigb", "ttg_ksl_z", "ttg_amen_solve",
+    "ttg_result_size", "ttg_result_copy", "ttg_zresult_copy", "ttg_free_result", "ttg_stats",
+    "ttg_launch_count",
+]
+
+
+class Context:
+    """Owns a ttg_ctx (one per host thread), i.e. the reference's module state."""
+
+    def __init__(self, device=0):
+        self._h = C.c_void_p()
+        rc = lib().ttg_create(C.c_int(device), C.byref(self._h))
+        if rc != TTG_OK:
+            raise TTGError(rc, "ttg_create failed (is a CUDA device visible?)")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def check(self, rc):
+        if rc != TTG_OK:
+            raise TTGError(rc, lib().ttg_last_error(self._h).decode())
+
+    def synchronize(self):
+        self.check(lib().ttg_synchronize(self._h))
+
+    def set_stream(self, stream_ptr):
+        self.check(lib().ttg_set_stream(self._h, C.c_void_p(stream_ptr)))
+        self._stream = stream_ptr
+
+    def bind_torch_stream(self):
+        """Run subsequent calls on torch's current CUDA stream, so that the
+        caching allocator's stream-ordered reuse of tensor memory is safe."""
+        import torch
+        s = torch.cuda.current_stream().cuda_stream
+        if getattr(self, "_stream", None) != s:
+            self.set_stream(s)
+
+    def stats(self):
+        mv, sw, la = _i64(), _i64(), _i64()
+        res = C.c_double()
+        lib().ttg_stats(self._h, C.byref(mv), C.byref(sw), C.byref(res), C.byref(la))
+        return {"matvecs": mv.value, "sweeps": sw.value, "res": res.value, "launches": la.value}
+
+    def close(self):
+        if self._h:
+            lib().ttg_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def launch_count():
+    return int(lib().ttg_launch_count())
+
+
+def _iarr(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.int64))
+
+
+def _darr(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.float64))
+
+
+def _carr(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.complex128))
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _dev(t):
+    """Device pointer of a torch CUDA tensor (contiguous)."""
+    if not getattr(t, "is_cuda", False):
+        raise TypeError("kernel-level calls take torch CUDA tensors")
+    if not t.is_contiguous():
+        raise ValueError("tensor must be contiguous")
+    return C.c_void_p(t.data_ptr())
+
+
+# ------------------------------------------------------------------ drivers
+def tt_eigb(d, n, m, ra, crA, crY0, ry, eps, rmax, B, kickrank=None, nswp=20,
+            max_full_size=2000, verb=0, method="plain", ctx=None):
+    """Block eigensolver (tt_eigb.f90:110).  Returns (lambda, cores, ry).
+
+    ``kickrank`` is accepted and ignored, as in the reference (unused there).
+    """
+    ctx = ctx or default_context()
+    n_, m_, ra_ = _iarr(n), _iarr(m), _iarr(ra)
+    ry_ = _iarr(ry).copy()
+    A_, Y_ = _darr(crA), _darr(crY0)
+    lam = np.zeros(int(B))
+    rc = lib().ttg_eigb(ctx.handle, _i64(d), _p(n_), _p(m_), _p(ra_), _p(A_), _p(Y_), _p(ry_),
+                        C.c_double(eps), _i64(rmax), _p(lam), _i64(B), _i64(nswp),
+                        _i64(max_full_size), C.c_int(verb), C.c_int(METHOD[method]))
+    ctx.check(rc)
+    return lam, _result(ctx, real=True), [int(v) for v in ry_]
+
+
+def ztt_ksl(d, n, m, ra, crA, crY0, ry, tau, rmax, kickrank=None, nswp=None, verb=0, typ=2,
+            order=8, method="plain", ctx=None):
+    """One KSL time step (ztt_ksl, tt_ksl.f90:431).  Returns (cores, ry)."""
+    ctx = ctx or default_context()
+    n_, m_, ra_ = _iarr(n), _iarr(m), _iarr(ra)
+    ry_ = _iarr(ry).copy()
+    A_, Y_ = _carr(crA), _carr(crY0)
+    rc = lib().ttg_ksl_z(ctx.handle, _i64(d), _p(n_), _p(m_), _p(ra_), _p(A_), _p(Y_), _p(ry_),
+                         C.c_double(tau), _i64(rmax), C.c_int(verb), C.c_int(typ),
+                         C.c_int(order), C.c_int(METHOD[method]))
+    ctx.check(rc)
+    return _result(ctx, real=False), [int(v) for v in ry_]
+
+
+def tt_amen_solve(d, n, m, ry, ra, crA, crY, crX0, rx, eps, rmax=1000, kickrank=4, nswp=20,
+                  verb=0, method="plain", ctx=None):
+    """AMEn solve A x = y (tt_amen_solve, tt_adapt_als.f90:513).  Returns (cores, rx)."""
+    ctx = ctx or default_context()
+    n_, m_, ry_, ra_ = _iarr(n), _iarr(m), _iarr(ry), _iarr(ra)
+    rx_ = _iarr(rx).copy()
+    A_, Y_, X_ = _darr(crA), _darr(crY), _darr(crX0)
+    rc = lib().ttg_amen_solve(ctx.handle, _i64(d), _p(n_), _p(m_), _p(ry_), _p(ra_), _p(A_),
+                              _p(Y_), _p(X_), _p(rx_), C.c_double(eps), _i64(rmax),
+                              _i64(kickrank), _i64(nswp), C.c_int(verb),
+                              C.c_int(METHOD[method]))
+    ctx.check(rc)
+    return _result(ctx, real=True), [int(v) for v in rx_]
+
+
+def _result(ctx, real=True):
+    nel = _i64()
+    lib().ttg_result_size(ctx.handle, C.byref(nel))
+    if real:
+        out = np.zeros(nel.value)
+        ctx.check(lib().ttg_result_copy(ctx.handle, _p(out), nel))
+    else:
+        out = np.zeros(nel.value, dtype=np.complex128)
+        ctx.check(lib().ttg_zresult_copy(ctx.handle, _p(out), nel))
+    lib().ttg_free_result(ctx.handle)
+    return out
+
+
+def my_chop3(s, eps):
+    s_ = _darr(s)
+    return int(lib().ttg_my_chop3(_i64(len(s_)), _p(s_), C.c_double(eps)))
+
+
+# ------------------------------------------------------- kernel level (torch)
+def _dims(*v):
+    return [_i64(int(x)) for x in v]
+
+
+def _kctx(ctx):
+    ctx = ctx or default_context()
+    ctx.bind_torch_stream()
+    return ctx
+
+
+def dbfun3(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1, A, phi2, x, y, nvec=1, split=False,
+           ctx=None):
+    """y = Phi1 A Phi2 x on the device (dbfun3, ttals.f90:9); torch CUDA tensors."""
+    ctx = _kctx(ctx)
+    f = lib().ttg_dbfun3_split if split else lib().ttg_dbfun3
+    ctx.check(f(ctx.handle, *_dims(rx1, m, rx2, ry1, n, ry2, ra1, ra2), _dev(phi1), _dev(A),
+                _dev(phi2), _dev(x), _dev(y), _i64(nvec)))
+
+
+def zbfun3(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1, A, phi2, x, y, nvec=1, transp=False,
+           ctx=None):
+    """Complex product zbfun3 (ttals.f90:34) / zbfun3_transp (:85); complex128 tensors."""
+    ctx = _kctx(ctx)
+    f = lib().ttg_zbfun3_transp if transp else lib().ttg_zbfun3
+    ctx.check(f(ctx.handle, *_dims(rx1, m, rx2, ry1, n, ry2, ra1, ra2), _dev(phi1), _dev(A),
+                _dev(phi2), _dev(x), _dev(y), _i64(nvec)))
+
+
+def phi_left(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1_old, A, x, y, out, complex_=False,
+             ctx=None):
+    ctx = _kctx(ctx)
+    f = lib().ttg_zphi_left if complex_ else lib().ttg_dphi_left
+    ctx.check(f(ctx.handle, *_dims(rx1, m, rx2, ry1, n, ry2, ra1, ra2), _dev(phi1_old), _dev(A),
+                _dev(x), _dev(y), _dev(out)))
+
+
+def phi_right(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi2_old, A, x, y, out, complex_=False,
+              ctx=None):
+    ctx = _kctx(ctx)
+    f = lib().ttg_zphi_right if complex_ else lib().ttg_dphi_right
+    ctx.check(f(ctx.handle, *_dims(rx1, m, rx2, ry1, n, ry2, ra1, ra2), _dev(phi2_old), _dev(A),
+                _dev(x), _dev(y), _dev(out)))
+
+
+def phi2_left(rx1, rx2, ry1, n, ry2, phi1_old, x, y, out, ctx=None):
+    ctx = _kctx(ctx)
+    ctx.check(lib().ttg_dphi2_left(ctx.handle, *_dims(rx1, rx2, ry1, n, ry2), _dev(phi1_old),
+                                   _dev(x), _dev(y), _dev(out)))
+
+
+def phi2_right(rx1, rx2, ry1, n, ry2, phi2_old, x, y, out, ctx=None):
+    ctx = _kctx(ctx)
+    ctx.check(lib().ttg_dphi2_right(ctx.handle, *_dims(rx1, rx2, ry1, n, ry2), _dev(phi2_old),
+                                    _dev(x), _dev(y), _dev(out)))
+
+
+def fullmat(rx1, m, rx2, ra1, ra2, phi1, A, phi2, out, ctx=None):
+    ctx = _kctx(ctx)
+    ctx.check(lib().ttg_d2d_fullmat(ctx.handle, *_dims(rx1, m, rx2, ra1, ra2), _dev(phi1),
+                                    _dev(A), _dev(phi2), _dev(out)))
+
+
+def dqr(nrows, ncols, A, R, complex_=False, ctx=None):
+    """In-place QR (dqr matrix_util.f90:37): A -> Q, R written."""
+    ctx = _kctx(ctx)
+    f = lib().ttg_zqr if complex_ else lib().ttg_dqr
+    ctx.check(f(ctx.handle, _i64(nrows), _i64(ncols), _dev(A), _dev(R)))
+
+
+def dsyev(k, A, w, ctx=None):
+    ctx = _kctx(ctx)
+    ctx.check(lib().ttg_dsyev(ctx.handle, _i64(k), _dev(A), _dev(w)))
+
+
+def dgesvd(p, q, M, U, s, Vt, ctx=None):
+    ctx = _kctx(ctx)
+    ctx.check(lib().ttg_dgesvd(ctx.handle, _i64(p), _i64(q), _dev(M), _dev(U), _dev(s), _dev(Vt)))
+
+
+def dmaxvol(nrows, r, A, p, Z=None, tol=1e-2, maxiters=1024, ctx=None):
+    ctx = _kctx(ctx)
+    ctx.check(lib().ttg_dmaxvol(ctx.handle, _i64(nrows), _i64(r), _dev(A), _dev(p),
+                                _dev(Z) if Z is not None else C.c_void_p(), C.c_double(tol),
+                                _i64(maxiters)))
