@@ -73,6 +73,23 @@ int ttg_dbfun3_split(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int 
                      ttg_int n, ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi1,
                      const double* A, const double* phi2, const double* x, double* y,
                      ttg_int nvec);
+/* Allocation-free variant of ttg_dbfun3 (no counterpart in the reference).
+ * For callers that must not allocate device memory during a call: hosts whose
+ * device memory belongs to another allocator, and callers inside a solver
+ * callback that cannot absorb the device synchronisation of cudaMalloc/cudaFree.
+ * The intermediates live in one library-owned device array of
+ * TTG_NOALLOC_SCRATCH_DOUBLES doubles (16 MiB, held by every GPU that loads the
+ * library until exit).  The first call on a device looks up that array's
+ * device address (set-up, once per device).  Sizes with
+ * (rx1*m*ra2*ry2 + rx1*ra1*n*ry2) * nvec > TTG_NOALLOC_SCRATCH_DOUBLES are
+ * rejected with TTG_ERR_ARG.  All calls share the array: calls that overlap on
+ * the GPU race and must be serialised by the caller.  Calls no cudaMalloc,
+ * cudaFree or other allocating routine. */
+#define TTG_NOALLOC_SCRATCH_DOUBLES 2097152
+int ttg_dbfun3_noalloc(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ry1,
+                       ttg_int n, ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi1,
+                       const double* A, const double* phi2, const double* x, double* y,
+                       ttg_int nvec);
 /* Complex product, zbfun3 ttals.f90:34-57. */
 int ttg_zbfun3(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ry1, ttg_int n,
                ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi1, const double* A,

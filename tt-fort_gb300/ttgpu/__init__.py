@@ -60,7 +60,7 @@ def lib():
 # every symbol declared in include/ttgpu.h
 EXPORTED = [
     "ttg_create", "ttg_destroy", "ttg_last_error", "ttg_set_stream", "ttg_synchronize",
-    "ttg_version", "ttg_dbfun3", "ttg_dbfun3_split", "ttg_zbfun3", "ttg_zbfun3_transp",
+    "ttg_version", "ttg_dbfun3", "ttg_dbfun3_split", "ttg_dbfun3_noalloc", "ttg_zbfun3", "ttg_zbfun3_transp",
     "ttg_dphi_left", "ttg_dphi_right", "ttg_zphi_left", "ttg_zphi_right", "ttg_dphi2_left",
     "ttg_dphi2_right", "ttg_d2d_fullmat", "ttg_dqr", "ttg_zqr", "ttg_dsyev", "ttg_dgesvd",
     "ttg_my_chop3", "ttg_dmaxvol", "ttg_eigb", "ttg_ksl_z", "ttg_amen_solve",
