@@ -1,22 +1,561 @@
-// Split-precision (BF16x3) tensor-core local operator -- placeholder until the
-// tcgen05 kernels land; the entry points report TTG_ERR_UNSUPPORTED.
+// Split-precision (BF16x3) tensor-core local operator for sm_103a.
+//
+// y = Phi1 * A * Phi2 * x  (dbfun3, ttals.f90:9-32) as two tcgen05 GEMMs and a
+// CUDA-core contraction with the TT-matrix core:
+//
+//   GEMM1  T1[(b1,j,v), (a2,c2)] = sum_b2 X_v[(b1,j), b2] Phi2[b2, (a2,c2)]
+//          M = rx1*m*nvec (all vectors of the block stacked), N = ra2*ry2, K = rx2
+//   CORE   T2[(i,c2,v), (b1,a1)] = sum_(j,a2) A[(a1,i),(j,a2)] T1[(b1,j,v),(a2,c2)]
+//   GEMM3  Y^T[(i,c2,v), c1]     = sum_(b1,a1) T2[(i,c2,v),(b1,a1)] Phi1[c1,(b1,a1)]
+//          M = n*ry2*nvec, N = ry1, K = rx1*ra1
+//
+// Every FP64 operand a is split as a_hi = bf16(a), a_lo = bf16(a - a_hi) and a
+// product is accumulated as a_hi b_hi + a_hi b_lo + a_lo b_hi in FP32 in
+// tensor memory (the dropped a_lo b_lo term is ~2^-16 relative).  Operands
+// are stored in global memory already in the tcgen05 K-major, no-swizzle
+// canonical layout, tile by tile (128 or BN rows x 64 K-elements, core
+// matrices of 8 rows x 16 bytes), so each pipeline stage is a handful of
+// contiguous cp.async.bulk copies completing on an mbarrier.  One thread
+// issues the MMAs (3 per 16-wide K step), tcgen05.commit releases the smem
+// stage, and four epilogue warps read the FP32 accumulator with tcgen05.ld.
+// Phi1 and Phi2 are split once per local problem (split_op_prepare); X is
+// split per call.
+//
+// Every mbarrier wait is bounded: on timeout the kernel records an error
+// code, waits (bounded) for the MMAs it issued, frees its tensor memory and
+// returns; the host turns the code into TTG_ERR_CUDA.
 #include "ttg_davidson.cuh"
+#include <cuda_bf16.h>
 
 namespace ttg {
+namespace tc {
 
-size_t split_matvec_bytes(const LocalDims&, int) { return 0; }
+constexpr int TM = 128;        // rows of the A tile (MMA M)
+constexpr int TK = 64;         // K elements per pipeline stage (4 MMA K-steps)
+constexpr int NTHREADS = 128;  // 4 warps: all read TMEM in the epilogue
+constexpr long long WAIT_LIMIT = 1ll << 22;
+constexpr int SMEM_PAD = 0;
 
-void split_matvec_factory(const LocalDims&, const double*, const double*, const double*, int,
-                          void*, cudaStream_t, MatvecFn*) {
-  throw Error{TTG_ERR_UNSUPPORTED, "split-precision matvec not built"};
+using bf16 = __nv_bfloat16;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (long long i = 0; i < WAIT_LIMIT; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld_wait() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// K-major, no-swizzle shared memory descriptor: lbo = byte stride between the
+// two 8x16B core matrices along K, sbo = byte stride between 8-row groups.
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;   // descriptor version of sm_100-family tcgen05
+  return d;                 // base offset 0, relative LBO, layout type 0 (no swizzle)
+}
+
+// kind::f16 instruction descriptor: BF16 x BF16 -> FP32, both K-major, M x N
+__host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
+  return (1u << 4)                     // D format F32
+         | (1u << 7)                   // A format BF16
+         | (1u << 10)                  // B format BF16
+         | ((uint32_t)(N >> 3) << 17)  // N / 8
+         | ((uint32_t)(M >> 4) << 24); // M / 16
+}
+
+// byte offset of element (r, k) inside one R x TK tile.  The tile is four
+// 16-wide K slabs of R*32 bytes (one MMA K-step each); inside a slab the 8x8
+// core matrices (8 rows x 16 bytes) of one 8-row group sit side by side
+// (K-direction stride LBO = 128 B) and row groups follow each other
+// (M/N-direction stride SBO = 256 B).  Every address one MMA can form from
+// these two strides stays inside its slab.
+__host__ __device__ __forceinline__ uint32_t tile_offset(int r, int k, int R) {
+  return (uint32_t)((k >> 4) * (R * 32) + (r >> 3) * 256 + ((k >> 3) & 1) * 128 + (r & 7) * 16 +
+                    (k & 7) * 2);
+}
+constexpr uint32_t LBO = 128;   // between the two core matrices along K
+constexpr uint32_t SBO = 256;   // between consecutive 8-row groups
+
+struct Tiled {            // one split operand (hi and lo planes) in tile order
+  bf16* hi;
+  bf16* lo;
+  int rows, cols;         // logical sizes
+  int R;                  // tile rows (128 for A operands, BN for B operands)
+  int rtiles, ktiles;
+  size_t elems() const { return (size_t)rtiles * R * ktiles * TK; }
+};
+
+// element (r, k) -> tile-order element index
+__device__ __forceinline__ size_t tiled_index(int r, int k, int R, int ktiles) {
+  size_t tile = (size_t)(r / R) * ktiles + (k / TK);
+  return tile * (size_t)R * TK + (tile_offset(r % R, k % TK, R) >> 1);
+}
+
+__device__ __forceinline__ void split2(double v, bf16& hi, bf16& lo) {
+  hi = __float2bfloat16_rn((float)v);
+  lo = __float2bfloat16_rn((float)(v - (double)__bfloat162float(hi)));
+}
+
+// split an FP64 matrix into tiled hi/lo planes; element (r, k) is read at
+// src[(r / rv) * vs + (r % rv) * sr + k * sk]; padding is written as zero.
+__global__ void split_kernel(const double* __restrict__ src, i64 rv, i64 vs, i64 sr, i64 sk,
+                             int rows, int cols, int R, int rtiles, int ktiles,
+                             bf16* __restrict__ hi, bf16* __restrict__ lo) {
+  const i64 tr = (i64)rtiles * R, tk = (i64)ktiles * TK;
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tr * tk;
+       e += (i64)gridDim.x * blockDim.x) {
+    int r = (int)(e % tr), k = (int)(e / tr);
+    double v = 0.0;
+    if (r < rows && k < cols) v = src[(r / rv) * vs + (r % rv) * sr + (i64)k * sk];
+    bf16 h, l;
+    split2(v, h, l);
+    size_t idx = tiled_index(r, k, R, ktiles);
+    hi[idx] = h;
+    lo[idx] = l;
+  }
+}
+
+// C[m, n] (m < M, n < N) = sum_k A[m, k] B[n, k], split-3 on tcgen05.
+// Output row m goes to out + (m / rpv) * vstride + (m % rpv) * rstride + n.
+template <int BN, int STAGES, class OutT>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    split_gemm_kernel(const bf16* __restrict__ Ahi, const bf16* __restrict__ Alo,
+                      const bf16* __restrict__ Bhi, const bf16* __restrict__ Blo, int M, int N,
+                      int ktiles, OutT* __restrict__ out, i64 rpv, i64 vstride, i64 rstride,
+                      int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  constexpr uint32_t A_BYTES = TM * TK * 2;
+  constexpr uint32_t B_BYTES = BN * TK * 2;
+  constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+  __shared__ __align__(8) uint64_t full_bar[STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[STAGES];
+  __shared__ __align__(8) uint64_t done_bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int fail;
+
+  // 1024-byte aligned stage area
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int mt = blockIdx.x, nt = blockIdx.y;
+
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(smem_u32(&full_bar[s]), 1);
+      mbar_init(smem_u32(&empty_bar[s]), 1);
+    }
+    mbar_init(smem_u32(&done_bar), 1);
+    fail = 0;
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(smem_u32(&tmem_slot), BN);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t taddr = tmem_slot;
+
+  if (tid == 0) {
+    constexpr uint32_t idesc = make_idesc(TM, BN);
+    const size_t a_tile = (size_t)TM * TK, b_tile = (size_t)BN * TK;
+    auto issue = [&](int c, int s) {
+      unsigned char* st = base + (size_t)s * STAGE_BYTES;
+      uint32_t bar = smem_u32(&full_bar[s]);
+      mbar_expect_tx(bar, STAGE_BYTES);
+      size_t ao = ((size_t)mt * ktiles + c) * a_tile;
+      size_t bo = ((size_t)nt * ktiles + c) * b_tile;
+      bulk_g2s(smem_u32(st), Ahi + ao, A_BYTES, bar);
+      bulk_g2s(smem_u32(st + A_BYTES), Alo + ao, A_BYTES, bar);
+      bulk_g2s(smem_u32(st + 2 * A_BYTES), Bhi + bo, B_BYTES, bar);
+      bulk_g2s(smem_u32(st + 2 * A_BYTES + B_BYTES), Blo + bo, B_BYTES, bar);
+    };
+    int issued = 0;
+    for (int c = 0; c < STAGES && c < ktiles; ++c) { issue(c, c); ++issued; }
+    bool ok = true;
+    for (int c = 0; c < ktiles && ok; ++c) {
+      const int s = c % STAGES;
+      const uint32_t ph = (uint32_t)((c / STAGES) & 1);
+      if (!mbar_wait(smem_u32(&full_bar[s]), ph)) { ok = false; break; }
+      tc_fence_after();
+      unsigned char* st = base + (size_t)s * STAGE_BYTES;
+      const uint32_t a_hi = smem_u32(st), a_lo = smem_u32(st + A_BYTES);
+      const uint32_t b_hi = smem_u32(st + 2 * A_BYTES), b_lo = smem_u32(st + 2 * A_BYTES + B_BYTES);
+#pragma unroll
+      for (int kk = 0; kk < TK / 16; ++kk) {
+        // one 16-wide K slab per MMA
+        const uint32_t aoff = kk * (TM * 32), boff = kk * (BN * 32);
+        const uint64_t dAh = make_desc(a_hi + aoff, LBO, SBO);
+        const uint64_t dAl = make_desc(a_lo + aoff, LBO, SBO);
+        const uint64_t dBh = make_desc(b_hi + boff, LBO, SBO);
+        const uint64_t dBl = make_desc(b_lo + boff, LBO, SBO);
+        mma_bf16(taddr, dAh, dBh, idesc, (c > 0 || kk > 0) ? 1u : 0u);
+        mma_bf16(taddr, dAh, dBl, idesc, 1u);
+        mma_bf16(taddr, dAl, dBh, idesc, 1u);
+      }
+      mma_commit(smem_u32(&empty_bar[s]));
+      const int nc = c + STAGES;
+      if (nc < ktiles) {
+        if (!mbar_wait(smem_u32(&empty_bar[s]), ph)) { ok = false; break; }
+        issue(nc, s);
+        ++issued;
+      }
+    }
+    if (!ok) {
+      fail = 1;
+      atomicExch(err, 1);
+      // let every copy that was issued land before the CTA can exit
+      for (int c = 0; c < issued; ++c) {
+        const int s = c % STAGES;
+        mbar_wait(smem_u32(&full_bar[s]), (uint32_t)((c / STAGES) & 1));
+      }
+    }
+    mma_commit(smem_u32(&done_bar));
+  }
+  __syncwarp();
+  const bool done_ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&done_bar), 0));
+  tc_fence_after();
+  if (!done_ok && lane == 0) atomicExch(err, 2);
+  if (done_ok && !fail) {
+    const int row = mt * TM + warp * 32 + lane;
+    OutT* orow = out + (row / rpv) * vstride + (row % rpv) * rstride;
+    const int n0 = nt * BN;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      uint32_t r[16];
+      tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+      tmem_ld_wait();
+      if (row < M) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const int n = n0 + c0 + q;
+          if (n < N) orow[n] = (OutT)__uint_as_float(r[q]);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(taddr, BN);
+}
+
+// CORE: T2[(i,c2,v),(b1,a1)] = sum_(j,a2) A[(a1,i),(j,a2)] T1[(b1,j,v),(a2,c2)]
+// one thread per (b1, c2, v); writes the split tiled A-operand of GEMM3.
+__global__ void core_kernel(const float* __restrict__ T1, int ldT1, const double* __restrict__ A,
+                            int rx1, int m, int n, int ra1, int ra2, int ry2, int nvec,
+                            int R3, int ktiles3, bf16* __restrict__ hi, bf16* __restrict__ lo) {
+  extern __shared__ float As[];
+  const int asz = ra1 * n * m * ra2;
+  const bool in_smem = asz <= 12288;
+  if (in_smem)
+    for (int e = threadIdx.x; e < asz; e += blockDim.x) As[e] = (float)A[e];
+  __syncthreads();
+  const i64 total = (i64)rx1 * ry2 * nvec;
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total;
+       e += (i64)gridDim.x * blockDim.x) {
+    const int b1 = (int)(e % rx1);
+    const int c2 = (int)((e / rx1) % ry2);
+    const int v = (int)(e / ((i64)rx1 * ry2));
+    for (int a1 = 0; a1 < ra1; ++a1) {
+      for (int i = 0; i < n; ++i) {
+        float acc = 0.f;
+        for (int a2 = 0; a2 < ra2; ++a2) {
+          for (int j = 0; j < m; ++j) {
+            const i64 row = (i64)b1 + (i64)rx1 * j + (i64)rx1 * m * v;
+            const float t = T1[row * ldT1 + a2 + (i64)ra2 * c2];
+            const int ai = a1 + ra1 * (i + n * (j + m * a2));
+            const float a = in_smem ? As[ai] : (float)__ldg(A + ai);
+            acc = fmaf(a, t, acc);
+          }
+        }
+        const int r = i + n * c2 + n * ry2 * v;
+        const int k = b1 + rx1 * a1;
+        bf16 h, l;
+        split2((double)acc, h, l);
+        const size_t idx = tiled_index(r, k, R3, ktiles3);
+        hi[idx] = h;
+        lo[idx] = l;
+      }
+    }
+  }
+}
+
+static int pick_bn(int N) {
+  int best = 64, waste = 1 << 30;
+  for (int bn : {256, 128, 64}) {
+    int w = ceil_div(N, bn) * bn - N;
+    if (w < waste) { waste = w; best = bn; }
+  }
+  return best;
+}
+
+static Tiled make_tiled(int rows, int cols, int R, char*& p) {
+  Tiled t;
+  t.rows = rows; t.cols = cols; t.R = R;
+  t.rtiles = ceil_div(rows, R);
+  t.ktiles = ceil_div(cols, TK);
+  size_t bytes = (t.elems() * sizeof(bf16) + 1023) & ~size_t(1023);
+  t.hi = (bf16*)p; p += bytes;
+  t.lo = (bf16*)p; p += bytes;
+  return t;
+}
+static size_t tiled_bytes(int rows, int cols, int R) {
+  size_t e = (size_t)ceil_div(rows, R) * R * ceil_div(cols, TK) * TK;
+  return 2 * ((e * sizeof(bf16) + 1023) & ~size_t(1023));
+}
+
+static void split_into(const double* src, i64 rv, i64 vs, i64 sr, i64 sk, const Tiled& t,
+                       cudaStream_t s) {
+  i64 total = (i64)t.rtiles * t.R * t.ktiles * TK;
+  int blocks = (int)std::min<i64>(8192, (total + 255) / 256);
+  split_kernel<<<blocks, 256, 0, s>>>(src, rv, vs, sr, sk, t.rows, t.cols, t.R, t.rtiles,
+                                      t.ktiles, t.hi, t.lo);
+  TTG_CHECK_LAUNCH();
+}
+
+template <int BN, class OutT>
+static void gemm_launch_bn(const Tiled& A, const Tiled& B, int M, int N, OutT* out, i64 rpv,
+                           i64 vstride, i64 rstride, int* err, cudaStream_t s) {
+  constexpr int STAGES = BN == 256 ? 2 : (BN == 128 ? 3 : 4);
+  constexpr size_t stage = (size_t)2 * TM * TK * 2 + (size_t)2 * BN * TK * 2;
+  constexpr size_t smem = STAGES * stage + 1024 + SMEM_PAD;
+  auto kern = split_gemm_kernel<BN, STAGES, OutT>;
+  static bool attr = false;
+  if (!attr) {
+    TTG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  dim3 grid(A.rtiles, B.rtiles);
+  kern<<<grid, NTHREADS, smem, s>>>(A.hi, A.lo, B.hi, B.lo, M, N, A.ktiles, out, rpv, vstride,
+                                    rstride, err);
+  TTG_CHECK_LAUNCH();
+}
+
+template <class OutT>
+static void gemm_launch(const Tiled& A, const Tiled& B, int M, int N, OutT* out, i64 rpv,
+                        i64 vstride, i64 rstride, int* err, cudaStream_t s) {
+  TTG_REQUIRE(A.ktiles == B.ktiles, "split gemm: K tiles differ");
+  if (B.R == 256) gemm_launch_bn<256>(A, B, M, N, out, rpv, vstride, rstride, err, s);
+  else if (B.R == 128) gemm_launch_bn<128>(A, B, M, N, out, rpv, vstride, rstride, err, s);
+  else gemm_launch_bn<64>(A, B, M, N, out, rpv, vstride, rstride, err, s);
+}
+
+}  // namespace tc
+
+// prepared split operator of one local problem
+struct SplitOp {
+  LocalDims L;
+  int nvec_max;
+  int bn1, bn3;
+  tc::Tiled X, P2, T2, P1;     // GEMM1 A/B, GEMM3 A/B
+  float* T1;
+  int ldT1;
+  const double* A;
+  int* err;
+};
+
+static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* base) {
+  const int M1 = (int)(L.rx1 * L.m * nvec_max), N1 = (int)(L.ra2 * L.ry2), K1 = (int)L.rx2;
+  const int M3 = (int)(L.n * L.ry2 * nvec_max), N3 = (int)L.ry1, K3 = (int)(L.rx1 * L.ra1);
+  const int bn1 = tc::pick_bn(N1), bn3 = tc::pick_bn(N3);
+  size_t tot = 0;
+  tot += tc::tiled_bytes(M1, K1, tc::TM) + tc::tiled_bytes(N1, K1, bn1);
+  tot += tc::tiled_bytes(M3, K3, tc::TM) + tc::tiled_bytes(N3, K3, bn3);
+  const int ldT1 = ceil_div(N1, 4) * 4;
+  size_t t1 = ((size_t)ceil_div(M1, tc::TM) * tc::TM * ldT1 * sizeof(float) + 1023) & ~size_t(1023);
+  tot += t1 + 1024 + sizeof(SplitOp) + 1024;
+  if (op && base) {
+    char* p = base;
+    op->L = L;
+    op->nvec_max = nvec_max;
+    op->bn1 = bn1; op->bn3 = bn3;
+    op->X = tc::make_tiled(M1, K1, tc::TM, p);
+    op->P2 = tc::make_tiled(N1, K1, bn1, p);
+    op->T2 = tc::make_tiled(M3, K3, tc::TM, p);
+    op->P1 = tc::make_tiled(N3, K3, bn3, p);
+    op->T1 = (float*)p; p += t1;
+    op->ldT1 = ldT1;
+    op->err = (int*)p; p += 1024;
+  }
+  return tot;
+}
+
+size_t split_op_bytes(const LocalDims& L, int nvec_max) { return split_layout(L, nvec_max, nullptr, nullptr); }
+
+bool split_op_supported(const LocalDims& L) {
+  return L.rx1 * L.m * 32 < (1ll << 31) && L.n * L.ry2 * 32 < (1ll << 31);
+}
+
+// prepare: split Phi2 (GEMM1 B: rows (a2,c2), K b2) and Phi1^T (GEMM3 B: rows
+// c1, K (b1,a1)) once per local problem.  The SplitOp header lives in host
+// memory owned by the caller; mem holds the device buffers.
+void split_op_prepare(SplitOp* op, const LocalDims& L, int nvec_max, const double* phi1,
+                      const double* A, const double* phi2, void* mem, cudaStream_t s) {
+  split_layout(L, nvec_max, op, (char*)mem);
+  op->A = A;
+  // Phi2 element (n=(a2,c2), k=b2) at phi2[b2 + rx2*n]
+  tc::split_into(phi2, 1ll << 40, 0, L.rx2, 1, op->P2, s);
+  // Phi1^T element (n=c1, k=(b1,a1)) at phi1[c1 + ry1*k]
+  tc::split_into(phi1, 1ll << 40, 0, 1, L.ry1, op->P1, s);
+  // T2 padding (rows and K columns the CORE kernel never writes) must be zero:
+  // padded K columns meet zero columns of Phi1, and 0 * garbage could be NaN
+  TTG_CUDA(cudaMemsetAsync(op->T2.hi, 0, op->T2.elems() * sizeof(tc::bf16), s));
+  TTG_CUDA(cudaMemsetAsync(op->T2.lo, 0, op->T2.elems() * sizeof(tc::bf16), s));
+  TTG_CUDA(cudaMemsetAsync(op->err, 0, sizeof(int), s));
+}
+
+void split_op_apply(SplitOp* op, const double* x, double* y, int nvec, cudaStream_t s) {
+  const LocalDims& L = op->L;
+  TTG_REQUIRE(nvec >= 1 && nvec <= op->nvec_max, "split matvec: nvec out of range");
+  const int M1 = (int)(L.rx1 * L.m * nvec), N1 = (int)(L.ra2 * L.ry2);
+  const int M3 = (int)(L.n * L.ry2 * nvec), N3 = (int)L.ry1;
+  // X_v element (row (b1,j), k=b2) at x[v*xsize + row + rx1*m*b2]
+  tc::Tiled X = op->X;
+  X.rows = M1;
+  tc::split_into(x, L.rx1 * L.m, L.xsize(), 1, L.rx1 * L.m, X, s);
+  // GEMM1 -> T1 (fp32 row-major, ld ldT1); only the M tiles in use
+  tc::Tiled Xa = X;
+  Xa.rtiles = ceil_div(M1, tc::TM);
+  tc::gemm_launch<float>(Xa, op->P2, M1, N1, op->T1, 1ll << 40, 0, op->ldT1, op->err, s);
+  // CORE -> T2 tiled
+  {
+    tc::Tiled T2 = op->T2;
+    i64 total = L.rx1 * L.ry2 * nvec;
+    int blocks = (int)std::min<i64>(4096, (total + 127) / 128);
+    const int asz = (int)(L.ra1 * L.n * L.m * L.ra2);
+    size_t sm = asz <= 12288 ? (size_t)asz * sizeof(float) : 0;
+    tc::core_kernel<<<blocks, 128, sm, s>>>(op->T1, op->ldT1, op->A, (int)L.rx1, (int)L.m,
+                                            (int)L.n, (int)L.ra1, (int)L.ra2, (int)L.ry2, nvec,
+                                            tc::TM, T2.ktiles, T2.hi, T2.lo);
+    TTG_CHECK_LAUNCH();
+  }
+  // GEMM3 -> y: row (i,c2,v) of Y^T goes to y[v*ysize + ry1*(i + n*c2) + c1]
+  tc::Tiled T2a = op->T2;
+  T2a.rtiles = ceil_div(M3, tc::TM);
+  tc::gemm_launch<double>(T2a, op->P1, M3, N3, y, L.n * L.ry2, L.ysize(), L.ry1, op->err, s);
+}
+
+// Davidson matvec factory for the chosen method (host-side SplitOp header is
+// kept in a small per-thread pool so the functor stays trivially copyable).
+size_t split_matvec_bytes(const LocalDims& L, int nvec_max) {
+  return split_op_bytes(L, nvec_max) + 4096;
+}
+
+void split_matvec_factory(const LocalDims& L, const double* phi1, const double* A,
+                          const double* phi2, int nvec_max, void* mem, cudaStream_t s,
+                          MatvecFn* out) {
+  static thread_local SplitOp op_store;
+  TTG_REQUIRE(split_op_supported(L), "split matvec: local problem too large");
+  split_op_prepare(&op_store, L, nvec_max, phi1, A, phi2, mem, s);
+  SplitOp* op = &op_store;
+  *out = [op, s](const double* X, double* Y, int nv) { split_op_apply(op, X, Y, nv, s); };
 }
 
 }  // namespace ttg
 
-extern "C" int ttg_dbfun3_split(ttg_ctx* ctx, ttg_int, ttg_int, ttg_int, ttg_int, ttg_int,
-                                ttg_int, ttg_int, ttg_int, const double*, const double*,
-                                const double*, const double*, double*, ttg_int) {
-  if (!ctx) return TTG_ERR_ARG;
-  ctx->last_error = "split-precision matvec not built";
-  return TTG_ERR_UNSUPPORTED;
+using namespace ttg;
+
+extern "C" int ttg_dbfun3_split(ttg_ctx* c, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ry1,
+                                ttg_int n, ttg_int ry2, ttg_int ra1, ttg_int ra2,
+                                const double* phi1, const double* A, const double* phi2,
+                                const double* x, double* y, ttg_int nvec) {
+  if (!c) return TTG_ERR_ARG;
+  try {
+    TTG_CUDA(cudaSetDevice(c->device));
+    TTG_REQUIRE(rx1 > 0 && m > 0 && rx2 > 0 && ry1 > 0 && n > 0 && ry2 > 0 && ra1 > 0 && ra2 > 0,
+                "all sizes must be positive");
+    TTG_REQUIRE(phi1 && A && phi2 && x && y && nvec > 0 && nvec <= 32, "bad pointer or nvec");
+    LocalDims L{rx1, m, rx2, ry1, n, ry2, ra1, ra2};
+    TTG_REQUIRE(split_op_supported(L), "local problem too large for the split kernel");
+    size_t bytes = split_op_bytes(L, (int)nvec);
+    c->ws.reset();
+    c->ws.reserve(bytes);
+    void* mem = c->ws.take(bytes);
+    SplitOp op;
+    split_op_prepare(&op, L, (int)nvec, phi1, A, phi2, mem, c->stream);
+    split_op_apply(&op, x, y, (int)nvec, c->stream);
+    int herr = 0;
+    TTG_CUDA(cudaMemcpyAsync(&herr, op.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    TTG_CUDA(cudaStreamSynchronize(c->stream));
+    if (herr) throw Error{TTG_ERR_CUDA, "split gemm: mbarrier wait timed out"};
+  } catch (const ttg::Error& e) {
+    c->last_error = e.msg;
+    return e.code;
+  }
+  return TTG_OK;
 }
