@@ -120,31 +120,34 @@ def fp64_peak_tflops(torch):
     return 2 * 4096 ** 3 / best / 1e12
 
 
-def matvec_roofline(torch, ctx, split=False):
-    """Local matvec at the workload's largest local problem (r=64, n=2, ra=5,
-    block of B vectors): average launch duration from CUDA events."""
+def matvec_roofline(torch, ctx, split=False, r=RMAX, nvec=B):
+    """Local matvec through a prepared operator (the form the solver calls)
+    at the workload's largest local problem (r=64, n=2, ra=5, block of B
+    vectors): average duration from CUDA events on the library's stream."""
     import ttgpu
-    r, n, ra = RMAX, 2, 5
+    n, ra = 2, 5
     rng = np.random.default_rng(0)
     phi1 = torch.from_numpy(rng.standard_normal(r * r * ra)).cuda()
     A = torch.from_numpy(rng.standard_normal(ra * n * n * ra)).cuda()
     phi2 = torch.from_numpy(rng.standard_normal(r * ra * r)).cuda()
-    X = torch.from_numpy(rng.standard_normal(r * n * r * B)).cuda()
-    Y = torch.zeros(r * n * r * B, dtype=torch.float64, device="cuda")
+    X = torch.from_numpy(rng.standard_normal(r * n * r * nvec)).cuda()
+    Y = torch.zeros(r * n * r * nvec, dtype=torch.float64, device="cuda")
     ctx.bind_torch_stream()
+    op = ttgpu.LocalOp(r, n, r, r, n, r, ra, ra, phi1, A, phi2, nvec_max=nvec,
+                       method="split" if split else "plain", ctx=ctx)
     for _ in range(5):
-        ttgpu.dbfun3(r, n, r, r, n, r, ra, ra, phi1, A, phi2, X, Y, nvec=B, split=split, ctx=ctx)
+        op.apply(X, Y, nvec)
     iters = 200
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(iters):
-        ttgpu.dbfun3(r, n, r, r, n, r, ra, ra, phi1, A, phi2, X, Y, nvec=B, split=split, ctx=ctx)
+        op.apply(X, Y, nvec)
     e1.record()
     torch.cuda.synchronize()
     dt = e0.elapsed_time(e1) / 1e3 / iters
-    flops = bfun3_flops(r, n, r, r, n, r, ra, ra) * B
-    return flops, dt
+    op.close()
+    return bfun3_flops(r, n, r, r, n, r, ra, ra) * nvec, dt
 
 
 def run_reference(args):
@@ -180,8 +183,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours")
-    ap.add_argument("--method", default="plain")
+    ap.add_argument("--method", default="split", choices=["split", "plain"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
@@ -199,49 +203,68 @@ def main():
     n, m, ra, crA, ry, cr = workload()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
-    def solve():
+    def solve(method):
         return ttgpu.tt_eigb(D, n, m, ra, crA, cr, ry, EPS, RMAX, B, nswp=20, max_full_size=MFS,
-                             method=args.method, ctx=ctx)
+                             method=method, ctx=ctx)
 
-    for _ in range(max(3, args.warmup)):
-        solve()
-    # timed region
-    times, walls = [], []
-    launches0 = ttgpu.launch_count()
-    if args.gpus > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler() as clk:
-        for _ in range(args.steps):
+    def timed(method, steps):
+        """steps solves, L2 flushed before each (untimed); CUDA events on the
+        library's stream (bound to torch's current stream) and wall clock."""
+        times, walls = [], []
+        launches0 = ttgpu.launch_count()
+        if args.gpus > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        out = None
+        for _ in range(steps):
             flush.fill_(1.0)
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             w0 = time.perf_counter()
             e0.record()
-            lam, cores, ry_out = solve()
+            out = solve(method)
             e1.record()
             torch.cuda.synchronize()
             walls.append(time.perf_counter() - w0)
             times.append(e0.elapsed_time(e1) / 1e3)
-    launches = (ttgpu.launch_count() - launches0) // max(1, args.steps)
-    st = ctx.stats()
-    t = float(np.mean(times))
-    tw = float(np.mean(walls))
+        launches = (ttgpu.launch_count() - launches0) // max(1, steps)
+        return float(np.mean(times)), float(np.mean(walls)), launches, out, ctx.stats()
+
+    meth = args.method
+    for _ in range(max(3, args.warmup)):
+        solve(meth)
+    with ClockSampler() as clk:
+        t, tw, launches, (lam, cores, ry_out), st = timed(meth, args.steps)
     if args.gpus > 1:
         tt = torch.tensor([t, tw], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         t, tw = tt.tolist()
+    plain = None
+    if meth != "plain" and not args.no_plain:
+        solve("plain")
+        tp, twp, lp, (lam_p, _, _), stp = timed("plain", max(1, min(args.steps, 2)))
+        plain = {"value": tp, "unit": "s", "e2e": twp, "gpu_launches": int(lp),
+                 "matvecs": stp["matvecs"], "plain_over_chosen": tp / t,
+                 "lambda_maxrel_vs_chosen": float(np.max(np.abs(lam_p - lam) / np.abs(lam_p)))}
     if rank != 0:
         return
     peaks, kind = measured_peaks()
-    fl, dt = matvec_roofline(torch, ctx, split=(args.method == "split"))
-    if args.method == "split":
+    split = meth == "split"
+    fl, dt = matvec_roofline(torch, ctx, split=split)
+    if split:
         peak, unit, bound = peaks["bf16_tflops"], "TFLOP/s", "tensor"
-        peak_note = f"bf16 dense burst, {kind}"
+        peak_note = (f"bf16 dense burst ({kind}); the BF16x3 matvec issues 3 bf16 products "
+                     "per algorithmic product, so the attainable algorithmic rate is peak/3")
     else:
         peak, unit, bound = fp64_peak_tflops(torch), "TFLOP/s", "tensor"
         peak_note = "fp64: cuBLAS DGEMM 4096^3 measured in this run"
     ach = fl / dt / 1e12
+    big = None
+    if split:
+        flb, dtb = matvec_roofline(torch, ctx, split=True, r=256, nvec=8)
+        big = {"kernel": "local matvec r=256 n=2 ra=5 block 8 (the d=100 XXZ local size)",
+               "achieved": flb / dtb / 1e12, "bf16_issued": 3 * flb / dtb / 1e12,
+               "frac": flb / dtb / 1e12 / peak, "launch_us": dtb * 1e6}
     h2d = (len(crA) + len(cr)) * 8 + (len(n) * 3 + 2 * len(ry)) * 8
     d2h = len(cores) * 8 + B * 8
     cpu = None
@@ -257,15 +280,17 @@ def main():
     line = {"metric": "tt_eigb sweep time to convergence (d=20 Heisenberg, B=5)",
             "value": t, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": t * 1e3, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.method == "plain" else "bf16x3/f64",
-            "data": "synthetic (seeded)", "method": args.method, "config": config(),
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if meth == "plain" else "bf16x3+f64",
+            "data": "synthetic (seeded)", "method": meth, "config": config(),
             "e2e": {"value": tw, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
-            "roofline": {"kernel": "local matvec bfun3 (r=64, n=2, ra=5, block 5)",
+            "roofline": {"kernel": f"local matvec bfun3 ({'BF16x3 tcgen05' if split else 'FP64'}, "
+                                   f"r=64, n=2, ra=5, block 5)",
                          "bound": bound, "achieved": ach, "peak": peak, "unit": unit,
                          "frac": ach / peak, "traffic": None, "peak_source": peak_note,
-                         "launch_us": dt * 1e6, "flops_per_launch": fl},
-            "clocks": clk.summary(), "cpu_baseline": cpu,
+                         "launch_us": dt * 1e6, "flops_per_launch": fl, "large_local": big},
+            "clocks": clk.summary(), "cpu_baseline": cpu, "plain": plain,
             "solve": {"lambda": lam.tolist(), "matvecs": st["matvecs"], "sweeps": st["sweeps"],
                       "max_rank": max(ry_out[:D])}}
     print(json.dumps(line))

@@ -90,6 +90,17 @@ int ttg_dbfun3_noalloc(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_in
                        ttg_int n, ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi1,
                        const double* A, const double* phi2, const double* x, double* y,
                        ttg_int nvec);
+/* Prepared local operator: the GPU counterpart of init_bfun_sizes +
+ * init_bfun_main + primme_matvec (tt_eigb.f90:15-49, tt_ksl.f90:1-84).
+ * create() binds Phi1, A, Phi2 (device pointers, kept by reference) for up to
+ * nvec_max vectors per apply and, for TTG_METHOD_SPLIT, splits Phi1/Phi2 into
+ * BF16 hi/lo tiles once; apply() is asynchronous on the context's stream. */
+typedef struct ttg_localop ttg_localop;
+int ttg_localop_create(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ry1, ttg_int n,
+                       ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi1, const double* A,
+                       const double* phi2, ttg_int nvec_max, int method, ttg_localop** op);
+int ttg_localop_apply(ttg_localop* op, const double* x, double* y, ttg_int nvec);
+int ttg_localop_destroy(ttg_localop* op);
 /* Complex product, zbfun3 ttals.f90:34-57. */
 int ttg_zbfun3(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ry1, ttg_int n,
                ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi1, const double* A,

@@ -56,12 +56,15 @@ def orth_block(V, T):
     return T
 
 
-def restart_coeffs(S, kr, Sprev):
-    """Coefficients of the GD+k restart: [S[:, :kr], orth(Sprev)] (MGS, twice)."""
+def restart_coeffs(S, kr, Sprev, maxkc):
+    """Coefficients of the GD+k restart: [S[:, :kr], orth(Sprev)] (MGS, twice),
+    at most ``maxkc`` columns so that one expansion vector still fits."""
     k = S.shape[0]
     C = [S[:, j].copy() for j in range(kr)]
     if Sprev is not None:
         for b in range(Sprev.shape[1]):
+            if len(C) >= maxkc:
+                break
             p = np.zeros(k)
             p[:Sprev.shape[0]] = Sprev[:, b]
             for _ in range(2):
@@ -105,7 +108,7 @@ def davidson(matvec, X0, B, tol, maxb=None, max_matvecs=500, keep=None):
         T = R[:, ~conv]
         if k + T.shape[1] > maxb:
             kr = min(keep, k)
-            C = restart_coeffs(S, kr, Sprev)
+            C = restart_coeffs(S, kr, Sprev, maxb - 1)
             V = V @ C
             W = W @ C
             H = C.T @ H @ C

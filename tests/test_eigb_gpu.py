@@ -66,3 +66,21 @@ def test_eigb_heisen20_config(ctx):
                                        max_full_size=200, ctx=ctx)
     assert np.allclose(lam, gold["lambda"], rtol=1e-9, atol=0)
     assert np.allclose(lam, ed[:B], rtol=0, atol=5e-7)
+
+
+@pytest.mark.parametrize("d,B,r,rmax", [(10, 5, 8, 64), (12, 3, 8, 64)])
+def test_eigb_chosen_matches_plain(ctx, d, B, r, rmax):
+    """Chosen form (BF16x3 tensor-core matvecs + FP64 Jacobi-Davidson judge)
+    reaches the plain method's eigenvalues to 1e-10 relative.  The ranks are
+    exact (rmax covers every bond), so both sweeps converge to the same fixed
+    point and the comparison is meaningful at 1e-10."""
+    import ttgpu
+    n, m, ra, crA = xxz_mpo(d, delta=0.9)
+    _, ry, cr = random_tt(d, 2, r, last=B, seed=11)
+    lam_p, _, ry_p = ttgpu.tt_eigb(d, n, m, ra, crA, cr, ry, 1e-10, rmax, B, nswp=10,
+                                   max_full_size=100, ctx=ctx)
+    lam_s, cores, ry_s = ttgpu.tt_eigb(d, n, m, ra, crA, cr, ry, 1e-10, rmax, B, nswp=10,
+                                       max_full_size=100, method="split", ctx=ctx)
+    assert np.allclose(lam_s, lam_p, rtol=REL, atol=0)
+    w = np.linalg.eigvalsh(_dense(d, delta=0.9))[:B]
+    assert np.allclose(lam_s, w, rtol=REL, atol=0)

@@ -47,3 +47,27 @@ def test_dbfun3_split_vs_oracle(torch_cuda, ctx, shape):
         sl = slice(v * ry1 * n * ry2, (v + 1) * ry1 * n * ry2)
         err = np.linalg.norm(y[sl] - ref[sl]) / np.linalg.norm(ref[sl])
         assert err < TOL_SPLIT, (v, err)
+
+
+@pytest.mark.parametrize("method,tol", [("plain", 1e-12), ("split", TOL_SPLIT)])
+def test_prepared_localop(torch_cuda, ctx, method, tol):
+    import ttgpu
+    torch = torch_cuda
+    rx1, m, rx2, ry1, n, ry2, ra1, ra2 = 24, 2, 40, 24, 2, 40, 5, 4
+    rng = np.random.default_rng(9)
+    t = lambda a: torch.from_numpy(a).cuda()
+    phi1 = t(rng.standard_normal(ry1 * rx1 * ra1))
+    A = t(rng.standard_normal(ra1 * n * m * ra2))
+    phi2 = t(rng.standard_normal(rx2 * ra2 * ry2))
+    op = ttgpu.LocalOp(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1, A, phi2, nvec_max=4,
+                       method=method, ctx=ctx)
+    for nvec in (4, 1, 3):     # the operator is reused for several block sizes
+        X = rng.standard_normal(rx1 * m * rx2 * nvec)
+        ref = ops.bfun3_block(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1.cpu().numpy(),
+                              A.cpu().numpy(), phi2.cpu().numpy(), X, nvec)
+        Y = torch.zeros(ry1 * n * ry2 * nvec, dtype=torch.float64, device="cuda")
+        op.apply(t(X), Y, nvec)
+        ctx.synchronize()
+        y = Y.cpu().numpy()
+        assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < tol
+    op.close()

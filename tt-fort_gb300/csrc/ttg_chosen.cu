@@ -1,0 +1,215 @@
+// Chosen-form local eigensolver: split-precision tensor-core matvecs with an
+// FP64 judge.
+//
+// Phase A: the block Davidson of ttg_davidson.cu driven by the BF16x3
+//          tensor-core operator (ttg_tc.cu) until its residual, measured with
+//          that operator, is below max(tol, 1e-4) * max|theta|.
+// Phase B: Jacobi-Davidson refinement in FP64.  The Rayleigh-Ritz projection,
+//          the residuals and the convergence test use FP64 matvecs; the new
+//          directions solve the correction equation
+//              (I - X X^T)(A~ - theta_j I)(I - X X^T) t_j = -r_j
+//          approximately by a fixed number of CG steps with the split operator
+//          A~ (batched over the unconverged columns, every scalar kept on the
+//          device, no host synchronisation inside).  The projected operator
+//          is positive definite on the complement of the wanted eigenvectors,
+//          so CG applies; each outer step gains about the accuracy of A~
+//          (1e-5) times the conditioning of the correction equation.
+// The FP64 matvecs of phase B are the judge: the returned eigenpairs meet the
+// same FP64 residual test as the plain method.
+#include "ttg_davidson.cuh"
+#include <algorithm>
+
+namespace ttg {
+
+// out[j] = sum_i U[i,j] V[i,j]   (out pre-zeroed)
+__global__ void col_dots_kernel(i64 N, const double* __restrict__ U, const double* __restrict__ V,
+                                double* __restrict__ out) {
+  const int j = blockIdx.y;
+  double acc = 0.0;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += (i64)gridDim.x * blockDim.x)
+    acc = fma(U[i + N * j], V[i + N * j], acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) atomicAdd(&out[j], t);
+  }
+}
+
+static void col_dots(i64 N, int t, const double* U, const double* V, double* out, cudaStream_t s) {
+  TTG_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * t, s));
+  int bx = (int)std::max<i64>(1, std::min<i64>(128, (N + 2047) / 2048));
+  col_dots_kernel<<<dim3(bx, t), 256, 0, s>>>(N, U, V, out);
+  TTG_CHECK_LAUNCH();
+}
+
+// q[:, j] -= theta_j p[:, j]
+__global__ void shift_kernel(i64 N, int t, const double* __restrict__ theta,
+                             const double* __restrict__ p, double* __restrict__ q) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < N * t; e += (i64)gridDim.x * blockDim.x)
+    q[e] -= theta[e / N] * p[e];
+}
+
+// CG step on column j (frozen when inactive or when p^T q <= 0):
+//   alpha = rr/pq; x += alpha p; r -= alpha q; rr_new += |r|^2
+__global__ void cg_update_kernel(i64 N, const double* __restrict__ rr, const double* __restrict__ pq,
+                                 const double* __restrict__ rr0, double tol2,
+                                 const double* __restrict__ p, const double* __restrict__ q,
+                                 double* __restrict__ x, double* __restrict__ r,
+                                 double* __restrict__ rr_new) {
+  const int j = blockIdx.y;
+  const bool active = pq[j] > 0.0 && rr[j] > tol2 * rr0[j];
+  const double alpha = active ? rr[j] / pq[j] : 0.0;
+  double acc = 0.0;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += (i64)gridDim.x * blockDim.x) {
+    const i64 e = i + N * j;
+    double rv = r[e];
+    if (active) {
+      x[e] = fma(alpha, p[e], x[e]);
+      rv = fma(-alpha, q[e], rv);
+      r[e] = rv;
+    }
+    acc = fma(rv, rv, acc);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) atomicAdd(&rr_new[j], t);
+  }
+}
+
+// p = r + beta p, beta = rr_new / rr (0 for frozen columns)
+__global__ void cg_dir_kernel(i64 N, int t, const double* __restrict__ rr,
+                              const double* __restrict__ rr_new, const double* __restrict__ pq,
+                              const double* __restrict__ rr0, double tol2,
+                              const double* __restrict__ r, double* __restrict__ p) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < N * t; e += (i64)gridDim.x * blockDim.x) {
+    const int j = (int)(e / N);
+    const bool active = pq[j] > 0.0 && rr[j] > tol2 * rr0[j];
+    const double beta = (active && rr[j] > 0.0) ? rr_new[j] / rr[j] : 0.0;
+    p[e] = r[e] + beta * p[e];
+  }
+}
+
+void gemm_tn_small(int M, int N, i64 K, const double* A, i64 lda, const double* B, i64 ldb,
+                   double* C, int ldc, double alpha, double beta, cudaStream_t s);
+void gemm_nn_small(i64 R, int N, int K, const double* A, i64 lda, const double* B, int ldb,
+                   double* C, i64 ldc, double alpha, double beta, cudaStream_t s);
+
+struct JdCg {
+  i64 N;
+  int Bmax;
+  int iters;
+  double rel_tol;      // inner residual reduction at which a column freezes
+  MatvecFn low;        // split-precision operator
+  cudaStream_t s;
+  double *x, *r, *p, *q, *sc;   // N x Bmax each; sc: scalars
+
+  static size_t bytes(i64 N, int Bmax) { return (4 * (size_t)N * Bmax + 16 * 64) * sizeof(double) + 4096; }
+
+  void bind(void* mem) {
+    double* m = (double*)mem;
+    x = m; r = x + N * Bmax; p = r + N * Bmax; q = p + N * Bmax; sc = q + N * Bmax;
+  }
+
+  // project out X (N x nb): v -= X (X^T v)
+  void project(double* v, int t, const double* X, int nb) {
+    double* c = sc + 6 * 64;
+    gemm_tn_small(nb, t, N, X, N, v, N, c, nb, 1.0, 0.0, s);
+    gemm_nn_small(N, t, nb, X, N, c, nb, v, N, -1.0, 1.0, s);
+  }
+
+  void operator()(double* T, int t, const double* X, int nb, const double* theta) {
+    double* rr = sc;
+    double* rr_new = sc + 64;
+    double* pq = sc + 2 * 64;
+    double* rr0 = sc + 3 * 64;
+    const double tol2 = rel_tol * rel_tol;
+    const size_t bytes_t = sizeof(double) * N * t;
+    int bx = (int)std::max<i64>(1, std::min<i64>(128, (N + 2047) / 2048));
+    int eb = (int)std::min<i64>(4096, (N * t + 255) / 256);
+    // x = 0, r = -rhs (already orthogonal to X), p = r
+    TTG_CUDA(cudaMemsetAsync(x, 0, bytes_t, s));
+    TTG_CUDA(cudaMemcpyAsync(r, T, bytes_t, cudaMemcpyDeviceToDevice, s));
+    project(r, t, X, nb);
+    scale_cols_neg(r, t);
+    TTG_CUDA(cudaMemcpyAsync(p, r, bytes_t, cudaMemcpyDeviceToDevice, s));
+    col_dots(N, t, r, r, rr, s);
+    TTG_CUDA(cudaMemcpyAsync(rr0, rr, sizeof(double) * t, cudaMemcpyDeviceToDevice, s));
+    for (int it = 0; it < iters; ++it) {
+      low(p, q, t);                                   // q = A~ p
+      shift_kernel<<<eb, 256, 0, s>>>(N, t, theta, p, q);   // q -= theta p
+      TTG_CHECK_LAUNCH();
+      project(q, t, X, nb);                           // q = P q
+      col_dots(N, t, p, q, pq, s);
+      TTG_CUDA(cudaMemsetAsync(rr_new, 0, sizeof(double) * t, s));
+      cg_update_kernel<<<dim3(bx, t), 256, 0, s>>>(N, rr, pq, rr0, tol2, p, q, x, r, rr_new);
+      TTG_CHECK_LAUNCH();
+      cg_dir_kernel<<<eb, 256, 0, s>>>(N, t, rr, rr_new, pq, rr0, tol2, r, p);
+      TTG_CHECK_LAUNCH();
+      std::swap(rr, rr_new);
+    }
+    // keep the correction orthogonal to X (rounding of the split products)
+    project(x, t, X, nb);
+    TTG_CUDA(cudaMemcpyAsync(T, x, bytes_t, cudaMemcpyDeviceToDevice, s));
+  }
+
+  void scale_cols_neg(double* v, int t);
+};
+
+__global__ void neg_kernel(i64 n, double* v) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x)
+    v[e] = -v[e];
+}
+
+void JdCg::scale_cols_neg(double* v, int t) {
+  int eb = (int)std::min<i64>(4096, (N * t + 255) / 256);
+  neg_kernel<<<eb, 256, 0, s>>>(N * t, v);
+  TTG_CHECK_LAUNCH();
+}
+
+size_t chosen_bytes(i64 N, int B) { return JdCg::bytes(N, B); }
+
+// Chosen local solve: phase A (split Davidson) then phase B (FP64 JD + CG on
+// the split operator).  X0, X: N x B.  Returns the FP64-judged statistics.
+DavidsonStats chosen_solve(i64 N, int B, void* dav_mem, double* hbuf, void* jd_mem,
+                           const MatvecFn& mv64, const MatvecFn& mvlow, const double* X0,
+                           double tol, int max_matvecs, double* X, double* theta_host,
+                           cudaStream_t s, DavTimer* timer, int* fp64_matvecs) {
+  const int maxb = (int)std::min<i64>(std::max(4 * B, 32), N);
+  const int keep = std::min(B + std::max(1, B / 2), std::max(maxb - B, 1));
+  DavidsonStats a;
+  {
+    Davidson dav(N, B, maxb, keep, dav_mem, hbuf, s);
+    dav.timer = timer;
+    a = dav.solve(mvlow, X0, std::max(tol, 1e-4), 4 * max_matvecs, X, theta_host);
+  }
+  JdCg jd;
+  jd.N = N; jd.Bmax = B; jd.iters = 12; jd.rel_tol = 1e-3; jd.low = mvlow; jd.s = s;
+  jd.bind(jd_mem);
+  const int maxb2 = (int)std::min<i64>(2 * B, N);
+  Davidson ref(N, B, maxb2, B, dav_mem, hbuf, s);
+  ref.timer = timer;
+  ref.gdk = false;
+  ref.prec = [&jd](double* T, int t, const double* Xr, int nb, const double* th) {
+    jd(T, t, Xr, nb, th);
+  };
+  DavidsonStats b = ref.solve(mv64, X, tol, max_matvecs, X, theta_host);
+  if (fp64_matvecs) *fp64_matvecs = b.matvecs;
+  b.matvecs += a.matvecs;
+  b.iters += a.iters;
+  return b;
+}
+
+}  // namespace ttg

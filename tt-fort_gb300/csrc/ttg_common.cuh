@@ -189,8 +189,10 @@ bool split_op_supported(const LocalDims& L);
 // ---------------------------------------------------------------------------
 // Symmetric eigen (cyclic Jacobi, one CTA): A (k x k, lda) overwritten,
 // eigenvalues ascending in w, eigenvectors in V (k x k, ldv).  status: iters
+// P0 (kp x kp, ldp), optional: eigenvectors of the leading kp x kp block of A
+// (warm start, used when A grew by appending rows and columns).
 void syev_jacobi(int k, double* A, int lda, double* w, double* V, int ldv, int* status,
-                 cudaStream_t s);
+                 cudaStream_t s, const double* P0 = nullptr, int kp = 0, int ldp = 0);
 // One-sided Jacobi SVD of M (p x q, p >= q, ldm = p), in place.  Outputs:
 // sigma (q, descending), U (p x q), Vt (q x q, rows = right singular vectors).
 size_t svd_scratch(int p, int q);

@@ -16,6 +16,17 @@
 namespace ttg {
 
 using MatvecFn = std::function<void(const double* X, double* Y, int nvec)>;
+// Expansion-vector transform: on entry T (N x t) holds residual columns, X
+// (N x nb) the current Ritz vectors and theta (device, t) their Ritz values;
+// on exit T holds the correction directions.
+using PrecFn = std::function<void(double* T, int t, const double* X, int nb, const double* theta)>;
+
+// optional phase timing (host wall clock with stream syncs), TTG_PROFILE
+struct DavTimer {
+  cudaStream_t s = nullptr;
+  double t[8] = {0};
+  long long iters = 0, restarts = 0, jac_sweeps = 0;
+};
 
 struct DavidsonStats {
   int iters = 0;
@@ -33,6 +44,9 @@ class Davidson {
   // X0 (N x B) start block; on return X (N x B) Ritz vectors, theta (B, host)
   DavidsonStats solve(const MatvecFn& mv, const double* X0, double tol, int max_matvecs,
                       double* X, double* theta_host);
+  DavTimer* timer = nullptr;
+  PrecFn prec;          // optional correction-equation solver (JD expansion)
+  bool gdk = true;      // keep the previous Ritz vectors at a restart (GD+k)
 
  private:
   i64 N_;
@@ -40,7 +54,9 @@ class Davidson {
   cudaStream_t s_;
   double *V_, *W_, *Vt_, *Wt_;
   double *H_, *Hs_, *S_, *theta_, *AX_, *R_, *rn2_;
-  double *T_, *T2_, *Ct_, *G_, *Mfull_, *Sprev_, *C_, *HC_;
+  double *T_, *T2_, *Ct_, *G_, *Mfull_, *Sprev_, *C_, *HC_, *S2_;
+  int kwarm_ = 0;
+  double* theta_sel_ = nullptr;   // size of the previous Rayleigh-Ritz solve still valid as a warm start
   int *ikept_, *idx_;
   double* hbuf_;
   int k_ = 0;

@@ -9,7 +9,9 @@
 // singular values that my_chop3 needs.
 #include "ttg_davidson.cuh"
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <numeric>
 
 namespace ttg {
@@ -18,6 +20,11 @@ void split_matvec_factory(const LocalDims& L, const double* phi1, const double* 
                           const double* phi2, int nvec_max, void* mem, cudaStream_t s,
                           MatvecFn* out);
 size_t split_matvec_bytes(const LocalDims& L, int nvec_max);
+size_t chosen_bytes(i64 N, int B);
+DavidsonStats chosen_solve(i64 N, int B, void* dav_mem, double* hbuf, void* jd_mem,
+                           const MatvecFn& mv64, const MatvecFn& mvlow, const double* X0,
+                           double tol, int max_matvecs, double* X, double* theta_host,
+                           cudaStream_t s, DavTimer* timer, int* fp64_matvecs);
 
 struct DevBlock {
   char* base = nullptr;
@@ -66,19 +73,55 @@ struct EigbOutput {
   std::vector<double> cores;
   std::vector<i64> ry;
   long long matvecs = 0;
+  long long fp64_matvecs = 0;
   int sweeps = 0;
   double res = 0.0;
 };
 
+// TTG_PROFILE=1: synchronise after every phase and print where the time went
+struct PhaseTimer {
+  bool on = false;
+  cudaStream_t s = nullptr;
+  double t[8] = {0};
+  std::chrono::steady_clock::time_point t0;
+  void start() {
+    if (!on) return;
+    cudaStreamSynchronize(s);
+    t0 = std::chrono::steady_clock::now();
+  }
+  void stop(int k) {
+    if (!on) return;
+    cudaStreamSynchronize(s);
+    t[k] += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  DavTimer dav;
+  void report() {
+    if (!on) return;
+    const char* nm[8] = {"qr-init", "dense", "davidson", "svd", "fold", "phi", "other", "mv"};
+    for (int k = 0; k < 8; ++k) fprintf(stderr, "[ttg profile] %-9s %8.3f s\n", nm[k], t[k]);
+    const char* dn[7] = {"init", "rr-eig", "ritz+res", "restart", "orth", "matvec", "h-update"};
+    for (int k = 0; k < 7; ++k) fprintf(stderr, "[ttg profile]   dav %-9s %8.3f s\n", dn[k], dav.t[k]);
+    fprintf(stderr, "[ttg profile]   dav iters %lld restarts %lld jacobi sweeps %lld\n", dav.iters,
+            dav.restarts, dav.jac_sweeps);
+    fprintf(stderr, "[ttg profile]   fp64 matvecs %lld of %lld\n", fp64_mv_report, all_mv_report);
+  }
+  long long fp64_mv_report = 0, all_mv_report = 0;
+  void dummy() {
+  }
+};
+
 static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
   cudaStream_t s = ctx->stream;
+  PhaseTimer pt;
+  pt.on = std::getenv("TTG_PROFILE") != nullptr;
+  pt.s = s;
   const int d = P.d, B = P.B;
   auto& n = P.n;
   auto& ry = P.ry;
   TTG_REQUIRE(d >= 2, "tt_eigb: d must be >= 2");
   TTG_REQUIRE(ry[d] == B, "Inconsistent number of eigenvalues sought and initial guess last rank");
   TTG_REQUIRE(ry[0] == 1 && P.ra[0] == 1 && P.ra[d] == 1, "boundary ranks must be 1");
-  TTG_REQUIRE(B >= 1 && B <= 32, "B must be in [1, 32]");
+  TTG_REQUIRE(B >= 1 && B <= 16, "B must be in [1, 16]");
   for (int i = 0; i < d; ++i) TTG_REQUIRE(n[i] == P.m[i], "tt_eigb needs square cores (n == m)");
   const double eps2 = P.eps / std::sqrt((double)d);
   const double resid_damp = 10.0;
@@ -129,6 +172,7 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
   total += al(bf_scr) + al(phi_scr) + al(split_bytes);
   total += 2 * al(sizeof(double) * dense_max * dense_max) + al(sizeof(double) * 512) + al(256);
   total += al(Davidson::bytes(Nmax, B, maxb_cap));
+  if (P.method == TTG_METHOD_SPLIT) total += al(chosen_bytes(Nmax, B));
   total += 1 << 16;
   DevBlock mem;
   mem.alloc(total);
@@ -151,6 +195,7 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
   double* dw = mem.take<double>(512);
   int* dst = mem.take<int>(64);
   void* dav_mem = mem.take<char>(Davidson::bytes(Nmax, B, maxb_cap));
+  void* jd_mem = P.method == TTG_METHOD_SPLIT ? (void*)mem.take<char>(chosen_bytes(Nmax, B)) : nullptr;
   PinnedBuf hb(4096 + rmaxsvd * 2);
   double* hbuf = hb.p;
 
@@ -172,6 +217,7 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
   };
 
   // QR orthogonalisation left to right, tt_eigb.f90:202-217
+  pt.start();
   for (int i = 0; i < d; ++i) {
     i64 rows = ry[i] * n[i];
     i64 rnew = std::min(rows, ry[i + 1]);
@@ -190,15 +236,17 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
     }
   }
   ry[d] = 1;
+  pt.stop(0);
 
   int i = d - 1, dir = -1, swp = 1;
   double ermax = 0.0, fvold = 0.0, res = 0.0;
   std::vector<double> lam(B, 0.0);
-  long long total_mv = 0;
+  long long total_mv = 0, fp64_mv = 0;
   while (swp <= P.nswp) {
     const i64 N = ry[i] * n[i] * ry[i + 1];
     TTG_REQUIRE(N >= B, "local problem smaller than the block size");
     int nmv = 0;
+    pt.start();
     if (N < P.max_full_size && N <= dense_max) {
       // dense branch: d2d_fullmat + dsyev, tt_eigb.f90:234-249
       fullmat_f64(ry[i], n[i], ry[i + 1], P.ra[i], P.ra[i + 1], phi[i], A_of(i), phi[i + 1], dH, s);
@@ -208,23 +256,47 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
       TTG_CUDA(cudaStreamSynchronize(s));
       for (int j = 0; j < B; ++j) lam[j] = hbuf[j];
       res = 0.0;
+      pt.stop(1);
     } else {
       LocalDims L = dimsL(i);
-      MatvecFn mv;
-      if (P.method == TTG_METHOD_SPLIT) {
-        split_matvec_factory(L, phi[i], A_of(i), phi[i + 1], B, split_mem, s, &mv);
-      } else {
-        const double* p1 = phi[i];
-        const double* Ai = A_of(i);
-        const double* p2 = phi[i + 1];
-        mv = [=](const double* X, double* Y, int nv) { bfun3_f64(L, p1, Ai, p2, X, Y, nv, bfs, s); };
+      const double* p1 = phi[i];
+      const double* Ai = A_of(i);
+      const double* p2 = phi[i + 1];
+      MatvecFn mv = [=](const double* X, double* Y, int nv) { bfun3_f64(L, p1, Ai, p2, X, Y, nv, bfs, s); };
+      MatvecFn mvlow;
+      if (P.method == TTG_METHOD_SPLIT) split_matvec_factory(L, p1, Ai, p2, B, split_mem, s, &mvlow);
+      if (pt.on) {
+        PhaseTimer* ptp = &pt;
+        auto wrap = [ptp](MatvecFn inner) {
+          return MatvecFn([inner, ptp](const double* X, double* Y, int nv) {
+            cudaStreamSynchronize(ptp->s);
+            auto a = std::chrono::steady_clock::now();
+            inner(X, Y, nv);
+            cudaStreamSynchronize(ptp->s);
+            ptp->t[7] += std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+          });
+        };
+        mv = wrap(mv);
+        if (mvlow) mvlow = wrap(mvlow);
       }
-      const int maxb = (int)std::min<i64>(std::max(4 * B, 32), N);
-      const int keep = std::min(B + std::max(1, B / 2), std::max(maxb - B, 1));
-      Davidson dav(N, B, maxb, keep, dav_mem, hbuf, s);
-      DavidsonStats st = dav.solve(mv, cr[i], eps2 / resid_damp, max_matvecs, curcr, lam.data());
+      DavidsonStats st;
+      if (P.method == TTG_METHOD_SPLIT) {
+        if (pt.on) pt.dav.s = s;
+        int n64 = 0;
+        st = chosen_solve(N, B, dav_mem, hbuf, jd_mem, mv, mvlow, cr[i], eps2 / resid_damp,
+                          max_matvecs, curcr, lam.data(), s, pt.on ? &pt.dav : nullptr, &n64);
+        fp64_mv += n64;
+      } else {
+        const int maxb = (int)std::min<i64>(std::max(4 * B, 32), N);
+        const int keep = std::min(B + std::max(1, B / 2), std::max(maxb - B, 1));
+        Davidson dav(N, B, maxb, keep, dav_mem, hbuf, s);
+        if (pt.on) { pt.dav.s = s; dav.timer = &pt.dav; }
+        st = dav.solve(mv, cr[i], eps2 / resid_damp, max_matvecs, curcr, lam.data());
+        fp64_mv += st.matvecs;
+      }
       nmv = st.matvecs;
       res = st.res;
+      pt.stop(2);
     }
     double fv = 0.0;
     for (int j = 0; j < B; ++j) fv += lam[j];
@@ -240,10 +312,13 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
       // tt_eigb.f90:305-356
       const int p = (int)(B * ry[i]), q = (int)(n[i] * ry[i + 1]);
       const int r = std::min(p, q);
+      pt.start();
       transpose_f64(N, B, curcr, tmp, s);                // (B ry_i) x (n ry_{i+1})
       svd_jacobi(p, q, tmp, sU, sS, sVt, svd_scr, dst, s);
       TTG_CUDA(cudaMemcpyAsync(hbuf, sS, sizeof(double) * r, cudaMemcpyDeviceToHost, s));
       TTG_CUDA(cudaStreamSynchronize(s));
+      pt.stop(3);
+      pt.start();
       i64 nn = std::min<i64>(ttg_my_chop3(r, hbuf, eps2), P.rmax);
       copy_rows_f64(r, nn, q, sVt, cr[i], s);             // core i = Vt(1:nn, :)
       scale_cols_f64(p, nn, sU, p, sS, s);               // U(:, 1:nn) diag(s)
@@ -257,15 +332,21 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
       TTG_CUDA(cudaMemcpyAsync(cr[i - 1], tmp2, sizeof(double) * ry[i - 1] * n[i - 1] * nn * B,
                                cudaMemcpyDeviceToDevice, s));
       ry[i] = nn;
+      pt.stop(4);
+      pt.start();
       phi_right_f64(dimsL(i), phi[i + 1], A_of(i), cr[i], cr[i], phi[i], phs, s);
+      pt.stop(5);
     }
     if (dir > 0 && i < d - 1) {
       // tt_eigb.f90:357-394
       const int p = (int)(ry[i] * n[i]), q = (int)(ry[i + 1] * B);
       const int r = std::min(p, q);
+      pt.start();
       svd_jacobi(p, q, curcr, sU, sS, sVt, svd_scr, dst, s);
       TTG_CUDA(cudaMemcpyAsync(hbuf, sS, sizeof(double) * r, cudaMemcpyDeviceToHost, s));
       TTG_CUDA(cudaStreamSynchronize(s));
+      pt.stop(3);
+      pt.start();
       i64 nn = std::min<i64>(ttg_my_chop3(r, hbuf, eps2), P.rmax);
       TTG_CUDA(cudaMemcpyAsync(cr[i], sU, sizeof(double) * p * nn, cudaMemcpyDeviceToDevice, s));
       copy_rows_f64(r, nn, q, sVt, tmp, s);               // Vt(1:nn,:)  nn x (ry_{i+1} B)
@@ -279,7 +360,10 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
       gemm_f64(g, s);
       transpose_f64(B, nn * n[i + 1] * ry[i + 2], tmp, cr[i + 1], s);
       ry[i + 1] = nn;
+      pt.stop(4);
+      pt.start();
       phi_left_f64(dimsL(i), phi[i], A_of(i), cr[i], cr[i], phi[i + 1], phs, s);
+      pt.stop(5);
     }
     if (dir > 0 && i == d - 2) {
       dir = -1;
@@ -311,9 +395,13 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
     off += sz;
   }
   TTG_CUDA(cudaStreamSynchronize(s));
+  pt.fp64_mv_report = fp64_mv;
+  pt.all_mv_report = total_mv;
+  pt.report();
   out.lambda = lam;
   out.ry = ry;
   out.matvecs = total_mv;
+  out.fp64_matvecs = fp64_mv;
   out.sweeps = swp - 1;
   out.res = res;
 }

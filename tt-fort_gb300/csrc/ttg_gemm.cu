@@ -210,6 +210,17 @@ void launch(Args<T> a, int nbatch, cudaStream_t s) {
     return;
   }
   if (a.splitk < 1) a.splitk = 1;
+  if (a.splitk == 1 && a.K >= 512) {
+    // FP64 runs at a few GFLOP/s per SM on GB300: when the output tiles do not
+    // cover the SMs, split K so that about two CTAs per SM are busy
+    int bm = a.N <= 16 ? 128 : (a.M <= 16 ? 16 : (sizeof(T) == 8 ? 64 : 32));
+    int bn = a.N <= 16 ? 16 : (a.M <= 16 ? 128 : (sizeof(T) == 8 ? 64 : 32));
+    i64 ctas = (i64)ceil_div(a.M, bm) * ceil_div(a.N, bn) * nbatch;
+    if (ctas < 152) {
+      i64 want = (304 + ctas - 1) / ctas;
+      a.splitk = (int)std::max<i64>(1, std::min<i64>(want, a.K / 256));
+    }
+  }
   a.kchunk = ceil_div(ceil_div(a.K, a.splitk), BK) * BK;
   a.splitk = ceil_div(a.K, a.kchunk);
   if (a.splitk > 1) {

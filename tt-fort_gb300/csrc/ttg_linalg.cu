@@ -147,7 +147,8 @@ constexpr int JAC_MAX_SWEEPS = 40;
 
 __global__ void __launch_bounds__(JAC_NT) syev_jacobi_kernel(int k, double* Ag, int lda,
                                                              double* w, double* Vg, int ldv,
-                                                             int* status, int smem_mode) {
+                                                             int* status, int smem_mode,
+                                                             const double* P0, int kp, int ldp) {
   extern __shared__ double dyn[];
   __shared__ double red[33];
   __shared__ double cs[512], sn[512];
@@ -164,6 +165,47 @@ __global__ void __launch_bounds__(JAC_NT) syev_jacobi_kernel(int k, double* Ag, 
   }
   for (int e = tid; e < k * k; e += JAC_NT) V[(e % k) + (i64)lv * (e / k)] = (e % k == e / k) ? 1.0 : 0.0;
   __syncthreads();
+  if (smem_mode && P0 && kp > 0) {
+    // warm start: V = diag(P0, I), A = V^T A V  (P0: eigenvectors of the
+    // leading kp x kp block from the previous call, so A becomes diagonal
+    // except for its last k - kp rows and columns)
+    double* T = dyn + 2 * (i64)k * k;
+    for (int e = tid; e < kp * kp; e += JAC_NT) V[(e % kp) + (i64)lv * (e / kp)] = P0[(e % kp) + (i64)ldp * (e / kp)];
+    __syncthreads();
+    for (int e = tid; e < k * k; e += JAC_NT) {
+      int i = e % k, j = e / k;
+      double v;
+      if (j < kp) {
+        v = 0.0;
+        for (int l = 0; l < kp; ++l) v = fma(A[i + (i64)la * l], V[l + (i64)lv * j], v);
+      } else {
+        v = A[i + (i64)la * j];
+      }
+      T[e] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < k * k; e += JAC_NT) {
+      int i = e % k, j = e / k;
+      double v;
+      if (i < kp) {
+        v = 0.0;
+        for (int l = 0; l < kp; ++l) v = fma(V[l + (i64)lv * i], T[l + (i64)k * j], v);
+      } else {
+        v = T[e];
+      }
+      A[i + (i64)la * j] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < k * k; e += JAC_NT) {
+      int i = e % k, j = e / k;
+      if (i < j) {
+        double v = 0.5 * (A[i + (i64)la * j] + A[j + (i64)la * i]);
+        A[i + (i64)la * j] = v;
+        A[j + (i64)la * i] = v;
+      }
+    }
+    __syncthreads();
+  }
   const int K = (k + 1) & ~1;
   const int npairs = K / 2;
   int sweep = 0;
@@ -259,10 +301,11 @@ __global__ void __launch_bounds__(JAC_NT) syev_jacobi_kernel(int k, double* Ag, 
 }
 
 void syev_jacobi(int k, double* A, int lda, double* w, double* V, int ldv, int* status,
-                 cudaStream_t s) {
+                 cudaStream_t s, const double* P0, int kp, int ldp) {
   if (k <= 0) return;
   TTG_REQUIRE(k <= 512, "syev_jacobi: k > 512");
-  size_t smem = (size_t)2 * k * k * sizeof(double);
+  const bool warm = P0 && kp > 0 && (size_t)3 * k * k * sizeof(double) <= 200 * 1024;
+  size_t smem = (size_t)(warm ? 3 : 2) * k * k * sizeof(double);
   int mode = smem <= 200 * 1024 ? 1 : 0;
   if (mode) {
     static bool attr_set = false;
@@ -274,14 +317,15 @@ void syev_jacobi(int k, double* A, int lda, double* w, double* V, int ldv, int* 
   } else {
     smem = 0;
   }
-  syev_jacobi_kernel<<<1, JAC_NT, smem, s>>>(k, A, lda, w, V, ldv, status, mode);
+  syev_jacobi_kernel<<<1, JAC_NT, smem, s>>>(k, A, lda, w, V, ldv, status, mode,
+                                             warm ? P0 : nullptr, warm ? kp : 0, ldp);
   TTG_CHECK_LAUNCH();
 }
 
 // ---------------------------------------------------------------------------
 // one-sided Jacobi SVD (cooperative launch, grid barrier between rounds)
 // ---------------------------------------------------------------------------
-constexpr int SVD_NT = 256;
+constexpr int SVD_NT = 32;   // one warp per CTA: FP64 throughput is per SM
 constexpr int SVD_MAX_SWEEPS = 60;
 
 __global__ void __launch_bounds__(SVD_NT) svd_rotate_kernel(int p, int q, double* M, double* V,
@@ -398,7 +442,7 @@ static void svd_tall(int p, int q, double* Mw, double* U, double* sigma, double*
                      cudaStream_t s) {
   // Mw (p x q, p >= q) is overwritten
   int npairs = (q + 1) / 2;
-  int blocks = std::max(1, ceil_div(npairs, SVD_NT / 32));
+  int blocks = std::max(1, npairs);
   static int max_coop = -1;
   if (max_coop < 0) {
     int dev, nsm, per;

@@ -559,3 +559,73 @@ extern "C" int ttg_dbfun3_split(ttg_ctx* c, ttg_int rx1, ttg_int m, ttg_int rx2,
   }
   return TTG_OK;
 }
+
+// ------------------------------------------------------------- prepared operator
+struct ttg_localop {
+  ttg_ctx* ctx;
+  LocalDims L;
+  int method;
+  int nvec_max;
+  const double *phi1, *A, *phi2;
+  void* mem;
+  SplitOp split;
+};
+
+extern "C" int ttg_localop_create(ttg_ctx* c, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int ry1,
+                                  ttg_int n, ttg_int ry2, ttg_int ra1, ttg_int ra2,
+                                  const double* phi1, const double* A, const double* phi2,
+                                  ttg_int nvec_max, int method, ttg_localop** out) {
+  if (!c || !out) return TTG_ERR_ARG;
+  *out = nullptr;
+  ttg_localop* op = nullptr;
+  try {
+    TTG_CUDA(cudaSetDevice(c->device));
+    TTG_REQUIRE(rx1 > 0 && m > 0 && rx2 > 0 && ry1 > 0 && n > 0 && ry2 > 0 && ra1 > 0 && ra2 > 0,
+                "all sizes must be positive");
+    TTG_REQUIRE(phi1 && A && phi2 && nvec_max > 0 && nvec_max <= 64, "bad pointer or nvec_max");
+    TTG_REQUIRE(method == TTG_METHOD_PLAIN || method == TTG_METHOD_SPLIT, "unknown method");
+    LocalDims L{rx1, m, rx2, ry1, n, ry2, ra1, ra2};
+    TTG_REQUIRE(L.xsize() < (1ll << 31) && L.ysize() < (1ll << 31), "local problem too large");
+    op = new ttg_localop();
+    op->ctx = c; op->L = L; op->method = method; op->nvec_max = (int)nvec_max;
+    op->phi1 = phi1; op->A = A; op->phi2 = phi2; op->mem = nullptr;
+    size_t bytes = method == TTG_METHOD_SPLIT ? split_op_bytes(L, (int)nvec_max)
+                                              : bfun3_f64_scratch(L, (int)nvec_max);
+    if (method == TTG_METHOD_SPLIT) TTG_REQUIRE(split_op_supported(L), "too large for split");
+    TTG_CUDA(cudaMalloc(&op->mem, bytes));
+    if (method == TTG_METHOD_SPLIT)
+      split_op_prepare(&op->split, L, (int)nvec_max, phi1, A, phi2, op->mem, c->stream);
+    *out = op;
+  } catch (const ttg::Error& e) {
+    c->last_error = e.msg;
+    if (op) { if (op->mem) cudaFree(op->mem); delete op; }
+    return e.code;
+  }
+  return TTG_OK;
+}
+
+extern "C" int ttg_localop_apply(ttg_localop* op, const double* x, double* y, ttg_int nvec) {
+  if (!op) return TTG_ERR_ARG;
+  ttg_ctx* c = op->ctx;
+  try {
+    TTG_CUDA(cudaSetDevice(c->device));
+    TTG_REQUIRE(x && y && nvec > 0 && nvec <= op->nvec_max, "bad pointer or nvec");
+    if (op->method == TTG_METHOD_SPLIT)
+      split_op_apply(&op->split, x, y, (int)nvec, c->stream);
+    else
+      bfun3_f64(op->L, op->phi1, op->A, op->phi2, x, y, (int)nvec, (double*)op->mem, c->stream);
+  } catch (const ttg::Error& e) {
+    c->last_error = e.msg;
+    return e.code;
+  }
+  return TTG_OK;
+}
+
+extern "C" int ttg_localop_destroy(ttg_localop* op) {
+  if (!op) return TTG_ERR_ARG;
+  cudaSetDevice(op->ctx->device);
+  cudaStreamSynchronize(op->ctx->stream);
+  if (op->mem) cudaFree(op->mem);
+  delete op;
+  return TTG_OK;
+}

@@ -65,7 +65,7 @@ EXPORTED = [
     "ttg_dphi2_right", "ttg_d2d_fullmat", "ttg_dqr", "ttg_zqr", "ttg_dsyev", "ttg_dgesvd",
     "ttg_my_chop3", "ttg_dmaxvol", "ttg_eigb", "ttg_ksl_z", "ttg_amen_solve",
     "ttg_result_size", "ttg_result_copy", "ttg_zresult_copy", "ttg_free_result", "ttg_stats",
-    "ttg_launch_count",
+    "ttg_launch_count", "ttg_localop_create", "ttg_localop_apply", "ttg_localop_destroy",
 ]
 
 
@@ -309,3 +309,34 @@ def dmaxvol(nrows, r, A, p, Z=None, tol=1e-2, maxiters=1024, ctx=None):
     ctx.check(lib().ttg_dmaxvol(ctx.handle, _i64(nrows), _i64(r), _dev(A), _dev(p),
                                 _dev(Z) if Z is not None else C.c_void_p(), C.c_double(tol),
                                 _i64(maxiters)))
+
+
+class LocalOp:
+    """Prepared local operator (init_bfun_main + primme_matvec, tt_eigb.f90:15-49).
+
+    Binds torch CUDA tensors Phi1, A, Phi2; ``apply(X, Y, nvec)`` runs
+    asynchronously on the context's stream (bound to torch's current stream).
+    """
+
+    def __init__(self, rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1, A, phi2, nvec_max=8,
+                 method="plain", ctx=None):
+        self.ctx = _kctx(ctx)
+        self._keep = (phi1, A, phi2)
+        self._h = C.c_void_p()
+        self.ctx.check(lib().ttg_localop_create(
+            self.ctx.handle, *_dims(rx1, m, rx2, ry1, n, ry2, ra1, ra2), _dev(phi1), _dev(A),
+            _dev(phi2), _i64(nvec_max), C.c_int(METHOD[method]), C.byref(self._h)))
+
+    def apply(self, X, Y, nvec=1):
+        self.ctx.check(lib().ttg_localop_apply(self._h, _dev(X), _dev(Y), _i64(nvec)))
+
+    def close(self):
+        if self._h:
+            lib().ttg_localop_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
