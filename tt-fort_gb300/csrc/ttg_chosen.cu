@@ -1,9 +1,10 @@
 // Chosen-form local eigensolver: split-precision tensor-core matvecs with an
 // FP64 judge.
 //
-// Phase A: the block Davidson of ttg_davidson.cu driven by the BF16x3
-//          tensor-core operator (ttg_tc.cu) until its residual, measured with
-//          that operator, is below max(tol, 1e-4) * max|theta|.
+// Phase A: Jacobi-Davidson (basis <= 2B, restarted to the B Ritz vectors
+//          every iteration) driven entirely by the BF16x3 tensor-core
+//          operator (ttg_tc.cu) until its residual, measured with that
+//          operator, is below max(tol, 1e-4) * max|theta|.
 // Phase B: Jacobi-Davidson refinement in FP64.  The Rayleigh-Ritz projection,
 //          the residuals and the convergence test use FP64 matvecs; the new
 //          directions solve the correction equation
@@ -187,24 +188,28 @@ DavidsonStats chosen_solve(i64 N, int B, void* dav_mem, double* hbuf, void* jd_m
                            const MatvecFn& mv64, const MatvecFn& mvlow, const double* X0,
                            double tol, int max_matvecs, double* X, double* theta_host,
                            cudaStream_t s, DavTimer* timer, int* fp64_matvecs) {
-  const int maxb = (int)std::min<i64>(std::max(4 * B, 32), N);
-  const int keep = std::min(B + std::max(1, B / 2), std::max(maxb - B, 1));
-  DavidsonStats a;
-  {
-    Davidson dav(N, B, maxb, keep, dav_mem, hbuf, s);
-    dav.timer = timer;
-    a = dav.solve(mvlow, X0, std::max(tol, 1e-4), 4 * max_matvecs, X, theta_host);
-  }
   JdCg jd;
   jd.N = N; jd.Bmax = B; jd.iters = 12; jd.rel_tol = 1e-3; jd.low = mvlow; jd.s = s;
   jd.bind(jd_mem);
   const int maxb2 = (int)std::min<i64>(2 * B, N);
+  auto jd_prec = [&jd](double* T, int t, const double* Xr, int nb, const double* th) {
+    jd(T, t, Xr, nb, th);
+  };
+  // phase A: Jacobi-Davidson entirely on the split operator (small
+  // Rayleigh-Ritz problems of size <= 2B), to the split operator's accuracy
+  DavidsonStats a;
+  {
+    Davidson dav(N, B, maxb2, B, dav_mem, hbuf, s);
+    dav.timer = timer;
+    dav.gdk = false;
+    dav.prec = jd_prec;
+    a = dav.solve(mvlow, X0, std::max(tol, 1e-4), 4 * max_matvecs, X, theta_host);
+  }
+  // phase B: the same iteration with FP64 matvecs as the judge
   Davidson ref(N, B, maxb2, B, dav_mem, hbuf, s);
   ref.timer = timer;
   ref.gdk = false;
-  ref.prec = [&jd](double* T, int t, const double* Xr, int nb, const double* th) {
-    jd(T, t, Xr, nb, th);
-  };
+  ref.prec = jd_prec;
   DavidsonStats b = ref.solve(mv64, X, tol, max_matvecs, X, theta_host);
   if (fp64_matvecs) *fp64_matvecs = b.matvecs;
   b.matvecs += a.matvecs;
