@@ -167,10 +167,15 @@ int ttg_eigb(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m, const 
              const double* crA, const double* crY0, ttg_int* ry, double eps, ttg_int rmax,
              double* lambda, ttg_int B, ttg_int nswp, ttg_int max_full_size, int verb,
              int method);
-/* One symmetric KSL step, ztt_ksl tt_ksl.f90:431-668 (complex, interleaved). */
+/* KSL time stepping, ztt_ksl tt_ksl.f90:431-668 (complex, interleaved):
+ * nsteps consecutive calls of the reference's one-step routine (nsteps <= 0
+ * means 1) with the state kept on the device; ry updated in place (ranks can
+ * only shrink); the result cores are read with ttg_zresult_copy.  typ 1 =
+ * KSL, 2 = symmetric KSL; order = Krylov dimension (8 in the reference);
+ * rmax is accepted and unused, as in the reference. */
 int ttg_ksl_z(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m, const ttg_int* ra,
               const double* crA, const double* crY0, ttg_int* ry, double tau, ttg_int rmax,
-              int verb, int typ, int order, int method);
+              int verb, int typ, int order, int method, ttg_int nsteps);
 /* AMEn linear solve A x = y, tt_amen_solve tt_adapt_als.f90:513-1132
  * (argument order follows it; rx updated in place). */
 int ttg_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,

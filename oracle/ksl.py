@@ -1,0 +1,156 @@
+"""Projector-splitting (KSL) time step ``ztt_ksl`` restated (oracle).
+
+Test infrastructure only (see ``oracle/__init__.py``).  Follows
+tt_ksl.f90:431-668:
+
+  * QR left->right of cores 1..d-1 with zphi_left updates   tt_ksl.f90:528-550
+  * tau0 = tau/2 for the symmetric scheme (typ = 2)          tt_ksl.f90:557-561
+  * backward half sweep i = d..1: K-step exp(+tau0 A_loc) on core i, then
+    (i > 1) QR of the transposed core, zphi_right, S-step exp(-tau0 S) of
+    the transposed R factor, folded into core i-1            tt_ksl.f90:569-599
+  * forward half sweep i = 1..d: K-step, then (i < d) QR, zphi_left, S-step
+    folded into core i+1                                     tt_ksl.f90:600-625
+  * every exponential through zexp_mv (Krylov order 8, tol 1e-8) with the
+    Higham 1-norm estimate as anorm (usenrm = 1)
+The S operator (sfun_ksl, tt_ksl.f90:142-152) maps S (rx1 x rx2) to
+phi1 (ry1 x rx1*ra) * [S phi2 (rx2 x ra*ry2)]; it is consistent only when the
+QR keeps the rank, which is the case for the reference's own inputs.
+"""
+import numpy as np
+
+from .ops import F, flat, dtransp, compute_ps, bfun3, zbfun3_transp, phi_left, phi_right
+from .expokit import zexp_mv
+from .normest import znormest, Seed
+
+
+def zqr_lapack(n, m, a):
+    """zqr (matrix_util.f90:64-90): zgeqrf + zungqr, LAPACK reflector signs."""
+    import scipy.linalg as sla
+    q, r = sla.qr(F(np.asarray(a, dtype=np.complex128)[: n * m], n, m), mode="economic")
+    return flat(q), flat(r)
+
+
+def sfun(rx1, rx2, ra, ry1, ry2, phi1, phi2):
+    def mv(Sx):
+        res1 = F(Sx, rx1, rx2) @ F(phi2, rx2, ra * ry2)              # rx1, ra, ry2
+        return flat(F(phi1, ry1, rx1 * ra) @ F(flat(res1), rx1 * ra, ry2))
+    return mv
+
+
+def _cols(fn):
+    def apply(X):
+        return np.column_stack([fn(X[:, j]) for j in range(X.shape[1])])
+    return apply
+
+
+def ztt_ksl(d, n, m, ra, crA, crY0, ry, tau, rmax, typ=2, order=8, verb=0):
+    """One KSL time step.  Returns dict(cores, ry, stats)."""
+    n = list(map(int, n)); m = list(map(int, m)); ra = list(map(int, ra))
+    ry = list(map(int, ry))
+    crA = np.asarray(crA, dtype=np.complex128)
+    eps = 1e-8
+    pa = compute_ps(d, ra, [n[i] * m[i] for i in range(d)])
+    Acore = [crA[pa[i]:pa[i + 1]] for i in range(d)]
+    cr = []
+    off = 0
+    for i in range(d):
+        sz = ry[i] * n[i] * ry[i + 1]
+        cr.append(np.array(crY0[off:off + sz], dtype=np.complex128))
+        off += sz
+    phi = [None] * (d + 1)
+    phi[0] = np.ones(1, dtype=np.complex128)
+    phi[d] = np.ones(1, dtype=np.complex128)
+    for i in range(d - 1):
+        rnew = min(ry[i] * n[i], ry[i + 1])
+        q, r = zqr_lapack(ry[i] * n[i], ry[i + 1], cr[i])
+        cr[i] = q
+        cr[i + 1] = flat(F(r, rnew, ry[i + 1]) @ F(cr[i + 1], ry[i + 1], n[i + 1] * ry[i + 2]))
+        ry[i + 1] = rnew
+        phi[i + 1] = phi_left(ry[i], m[i], ry[i + 1], ry[i], n[i], ry[i + 1], ra[i], ra[i + 1],
+                              phi[i], Acore[i], cr[i], cr[i], conj=True)
+    seed = Seed()
+    tau0 = tau / 2 if typ == 2 else tau
+    stats = {"exp_calls": 0, "nmult": 0, "normest": []}
+
+    def kstep(i):
+        r1, r2 = ry[i], ry[i + 1]
+        N = r1 * n[i] * r2
+        args = (r1, n[i], r2, r1, n[i], r2, ra[i], ra[i + 1], phi[i], Acore[i], phi[i + 1])
+        mv = lambda x: bfun3(*args, x)
+        mvT = lambda x: zbfun3_transp(*args, x)
+        anorm = znormest(N, 4, _cols(mv), _cols(mvT), seed)
+        w, st = zexp_mv(N, order, tau0, cr[i], eps, anorm, mv)
+        stats["exp_calls"] += 1
+        stats["nmult"] += st["nmult"]
+        stats["normest"].append(anorm)
+        return w
+
+    def sstep(rx1, rx2, rr, ry1, ry2, p1, p2, R):
+        mv = sfun(rx1, rx2, rr, ry1, ry2, p1, p2)
+        N = rx1 * ry2
+        anorm = znormest(N, 4, _cols(mv), None, seed)
+        w, st = zexp_mv(N, order, -tau0, R, eps, anorm, mv)
+        stats["exp_calls"] += 1
+        stats["nmult"] += st["nmult"]
+        stats["normest"].append(anorm)
+        return w
+
+    i, dir_, swp = d - 1, -1, 0
+    while swp < 1:
+        curcr = kstep(i)
+        if dir_ < 0:
+            if i > 0:
+                ct = dtransp(ry[i], n[i] * ry[i + 1], curcr)          # (n r2) x r1
+                rnew = min(n[i] * ry[i + 1], ry[i])
+                q, r = zqr_lapack(n[i] * ry[i + 1], ry[i], ct)
+                core = dtransp(n[i] * ry[i + 1], rnew, q)             # rnew x (n r2)
+                cr[i] = core
+                R = dtransp(rnew, ry[i], r)                           # r1 x rnew
+                phitmp = phi_right(rnew, n[i], ry[i + 1], rnew, n[i], ry[i + 1], ra[i], ra[i + 1],
+                                   phi[i + 1], Acore[i], core, core, conj=True)
+                if rnew != ry[i]:
+                    raise ValueError("KSL S-step needs a rank-preserving QR")
+                Stmp = sstep(ry[i], ry[i], ra[i], rnew, rnew, phi[i], phitmp, R)
+                cr[i - 1] = flat(F(cr[i - 1], ry[i - 1] * n[i - 1], ry[i]) @ F(Stmp, ry[i], rnew))
+                ry[i] = rnew
+                phi[i] = phitmp
+            else:
+                cr[i] = curcr
+        else:
+            if i < d - 1:
+                q, r = zqr_lapack(ry[i] * n[i], ry[i + 1], curcr)
+                rnew = min(ry[i] * n[i], ry[i + 1])
+                cr[i] = q
+                phitmp = phi_left(ry[i], n[i], rnew, ry[i], n[i], rnew, ra[i], ra[i + 1],
+                                  phi[i], Acore[i], q, q, conj=True)
+                if rnew != ry[i + 1]:
+                    raise ValueError("KSL S-step needs a rank-preserving QR")
+                Stmp = sstep(rnew, rnew, ra[i + 1], ry[i + 1], ry[i + 1], phitmp, phi[i + 1], r)
+                cr[i + 1] = flat(F(Stmp, rnew, ry[i + 1]) @ F(cr[i + 1], ry[i + 1], n[i + 1] * ry[i + 2]))
+                ry[i + 1] = rnew
+                phi[i + 1] = phitmp
+            else:
+                cr[i] = curcr
+        if dir_ > 0 and i == d - 1:
+            dir_, i = -1, d - 1
+            swp += 1
+        elif dir_ < 0 and i == 0:
+            dir_, i = 1, 0
+            if typ == 1:
+                break
+        else:
+            i += dir_
+    cores = np.concatenate([cr[k][:ry[k] * n[k] * ry[k + 1]] for k in range(d)])
+    return {"cores": cores, "ry": ry, "stats": stats}
+
+
+def tt_full(d, n, ry, cores):
+    """Dense vector (earlier modes fastest) of a TT with ry[0] = ry[d] = 1."""
+    off = 0
+    cur = np.ones((1, 1), dtype=np.result_type(cores.dtype, np.float64))
+    for i in range(d):
+        sz = ry[i] * n[i] * ry[i + 1]
+        c = F(cores[off:off + sz], ry[i], n[i] * ry[i + 1])
+        off += sz
+        cur = (cur @ c).reshape(-1, ry[i + 1], order="F")
+    return cur[:, 0]

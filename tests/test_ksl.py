@@ -1,0 +1,98 @@
+"""CPU tests: the KSL oracle (ztt_ksl, Expokit, normest) pinned against the
+reference's closed-form fixture and dense references."""
+import os
+
+import numpy as np
+import scipy.linalg as sla
+
+from conftest import GOLDEN
+from oracle.expokit import zgpadm, zexp_mv
+from oracle.ksl import ztt_ksl, tt_full
+from oracle.normest import znormest, Seed, unit_randoms
+
+
+def load_dat(name):
+    D = dict(np.load(os.path.join(GOLDEN, name)))
+    return (int(D["d"]), [int(v) for v in D["n"]], [int(v) for v in D["m"]],
+            [int(v) for v in D["ra"]], [int(v) for v in D["ry"]], D["crA"], D["crY"],
+            float(D["tau"]))
+
+
+def test_eye_fixture_is_exp_i_tau():
+    """test_eye_ksl.dat: A = i*I, one step must return exp(i tau) y0."""
+    d, n, m, ra, ry, crA, crY, tau = load_dat("test_eye_ksl_dat.npz")
+    out = ztt_ksl(d, n, m, ra, crA, crY, ry, tau, 150)
+    x0 = tt_full(d, n, ry, crY)
+    x1 = tt_full(d, n, out["ry"], out["cores"])
+    assert np.linalg.norm(x1 - np.exp(1j * tau) * x0) <= 1e-12 * np.linalg.norm(x0)
+
+
+def separable(d, nn, seed):
+    rng = np.random.default_rng(seed)
+    a = [rng.standard_normal((nn, nn)) + 1j * rng.standard_normal((nn, nn)) for _ in range(d)]
+    I = np.eye(nn)
+    cores = []
+    for k in range(d):
+        if k == 0:
+            c = np.zeros((1, nn, nn, 2), complex); c[0, :, :, 0] = a[k]; c[0, :, :, 1] = I
+        elif k == d - 1:
+            c = np.zeros((2, nn, nn, 1), complex); c[0, :, :, 0] = I; c[1, :, :, 0] = a[k]
+        else:
+            c = np.zeros((2, nn, nn, 2), complex)
+            c[0, :, :, 0] = I; c[1, :, :, 0] = a[k]; c[1, :, :, 1] = I
+        cores.append(c)
+    crA = np.concatenate([c.ravel(order="F") for c in cores])
+    ra = [1] + [2] * (d - 1) + [1]
+    full = np.zeros((nn ** d, nn ** d), complex)
+    for k in range(d):
+        mats = [I] * d
+        mats[k] = a[k]
+        M = mats[d - 1]
+        for q in range(d - 2, -1, -1):
+            M = np.kron(M, mats[q])
+        full += M
+    y = np.concatenate([rng.standard_normal(nn) + 1j * rng.standard_normal(nn) for _ in range(d)])
+    return crA, ra, full, y
+
+
+def test_separable_rank1_is_exact():
+    """For A = sum_k a_k (Kronecker sum) and a rank-1 start the exact solution
+    stays rank 1, so the projector-splitting step is exact up to Expokit."""
+    d, nn, tau = 5, 3, 0.05
+    crA, ra, full, y = separable(d, nn, 0)
+    out = ztt_ksl(d, [nn] * d, [nn] * d, ra, crA, y, [1] * (d + 1), tau, 10)
+    x0 = tt_full(d, [nn] * d, [1] * (d + 1), y)
+    x1 = tt_full(d, [nn] * d, out["ry"], out["cores"])
+    ref = sla.expm(tau * full) @ x0
+    assert np.linalg.norm(x1 - ref) <= 1e-10 * np.linalg.norm(ref)
+
+
+def test_zgpadm_and_zexp_mv_against_expm():
+    rng = np.random.default_rng(4)
+    for mdim in (3, 7, 10):
+        H = rng.standard_normal((mdim, mdim)) + 1j * rng.standard_normal((mdim, mdim))
+        for t in (0.01, -0.3, 2.0):
+            assert np.allclose(zgpadm(6, mdim, t, H), sla.expm(t * H), rtol=1e-12, atol=1e-12)
+    N = 60
+    A = (rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))) / np.sqrt(N)
+    v = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    w, st = zexp_mv(N, 8, 0.7, v, 1e-10, np.abs(A).sum(axis=0).max(), lambda x: A @ x)
+    ref = sla.expm(0.7 * A) @ v
+    assert np.linalg.norm(w - ref) <= 1e-8 * np.linalg.norm(ref)
+    assert st["nstep"] >= 1
+
+
+def test_normest_is_a_lower_bound_close_to_the_1norm():
+    rng = np.random.default_rng(5)
+    for N in (1, 3, 17, 120):
+        A = rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))
+        est = znormest(N, 4, lambda X: A @ X, lambda X: A.conj().T @ X, Seed())
+        true = np.abs(A).sum(axis=0).max()
+        assert est <= true * (1 + 1e-12)
+        assert est >= 0.3 * true
+
+
+def test_unit_randoms_stream():
+    z = unit_randoms(0, 5)
+    assert np.allclose(np.abs(z), 1.0)
+    assert np.allclose(unit_randoms(2, 3), z[2:5])

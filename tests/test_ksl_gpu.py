@@ -1,0 +1,64 @@
+"""GPU parity of ztt_ksl (KSL time stepping) against the oracle restatement.
+
+Bar: KSL states to 1e-8 relative in the 2-norm (the Expokit tolerance of the
+reference); the closed-form fixture to 1e-12."""
+import numpy as np
+import pytest
+
+from oracle.ksl import ztt_ksl as oracle_ksl, tt_full
+from test_ksl import load_dat, separable
+from ttgpu.operators import ksl_operator, random_tt_complex
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def test_ksl_eye_fixture(ctx):
+    import ttgpu
+    d, n, m, ra, ry, crA, crY, tau = load_dat("test_eye_ksl_dat.npz")
+    cores, ry1 = ttgpu.ztt_ksl(d, n, m, ra, crA, crY, ry, tau, 150, ctx=ctx)
+    x0 = tt_full(d, n, ry, crY)
+    assert _rel(tt_full(d, n, ry1, cores), np.exp(1j * tau) * x0) < 1e-12
+
+
+def test_ksl_reference_fixture_ten_steps(ctx):
+    """test_ksl.f90 calls ztt_ksl ten times on test_ksl.dat."""
+    import ttgpu
+    d, n, m, ra, ry, crA, crY, tau = load_dat("test_ksl_dat.npz")
+    cores, ry1 = ttgpu.ztt_ksl(d, n, m, ra, crA, crY, ry, tau, 150, nsteps=10, ctx=ctx)
+    c, r = crY, list(ry)
+    for _ in range(10):
+        out = oracle_ksl(d, n, m, ra, crA, c, r, tau, 150)
+        c, r = out["cores"], out["ry"]
+    assert ry1 == r
+    assert _rel(tt_full(d, n, ry1, cores), tt_full(d, n, r, c)) < 1e-8
+
+
+def test_ksl_separable_exact(ctx):
+    import ttgpu
+    import scipy.linalg as sla
+    d, nn, tau = 5, 3, 0.05
+    crA, ra, full, y = separable(d, nn, 0)
+    cores, ry1 = ttgpu.ztt_ksl(d, [nn] * d, [nn] * d, ra, crA, y, [1] * (d + 1), tau, 10, ctx=ctx)
+    x0 = tt_full(d, [nn] * d, [1] * (d + 1), y)
+    ref = sla.expm(tau * full) @ x0
+    assert _rel(tt_full(d, [nn] * d, ry1, cores), ref) < 1e-10
+
+
+def test_ksl_laplace_perturbed_small(ctx):
+    """The KSL workload's operator family at a size the oracle finishes fast:
+    -(Laplacian) + random rank-4 TT-matrix, rank-4 start, 3 steps."""
+    import ttgpu
+    d, n, r, tau = 6, 8, 4, 1e-3
+    nn, mm, ra, crA = ksl_operator(d=d, n=n, rank=4, std=0.1, seed=1)
+    _, ry, y = random_tt_complex(d, n, r, seed=2)
+    cores, ry1 = ttgpu.ztt_ksl(d, nn, mm, ra, crA, y, ry, tau, 64, nsteps=3, ctx=ctx)
+    c, rr = y, list(ry)
+    for _ in range(3):
+        out = oracle_ksl(d, nn, mm, ra, crA, c, rr, tau, 64)
+        c, rr = out["cores"], out["ry"]
+    assert ry1 == rr
+    assert _rel(tt_full(d, nn, ry1, cores), tt_full(d, nn, rr, c)) < 1e-8

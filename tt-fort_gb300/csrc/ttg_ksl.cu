@@ -1,0 +1,321 @@
+// KSL (projector-splitting) time stepper ztt_ksl (tt_ksl.f90:431-668) on the
+// GPU.  One call performs nsteps consecutive time steps, each exactly the
+// reference's single call (QR sweep, backward half sweep with K- and S-steps,
+// forward half sweep); the cores stay in HBM between steps.
+//
+//   K-step  exp(+tau0 A_loc) core_i   A_loc x = zbfun3 (Phi_L A_i Phi_R x)
+//   S-step  exp(-tau0 S) R            S x = Phi1 (x Phi2)   (sfun_ksl,
+//                                     tt_ksl.f90:142-152)
+// with tau0 = tau/2 for the symmetric scheme (typ = 2), Krylov order 8 and
+// tolerance 1e-8 (tt_ksl.f90:477), anorm from the block 1-norm estimate.
+#include "ttg_expokit.cuh"
+#include <algorithm>
+#include <cmath>
+
+namespace ttg {
+
+namespace {
+
+struct DevBlockZ {
+  char* base = nullptr;
+  size_t top = 0, cap = 0;
+  ~DevBlockZ() { if (base) cudaFree(base); }
+  void alloc(size_t bytes) {
+    if (cudaMalloc(&base, bytes) != cudaSuccess) {
+      base = nullptr;
+      throw Error{TTG_ERR_NOMEM, "ztt_ksl: device allocation failed"};
+    }
+    cap = bytes;
+  }
+  template <class T> T* take(size_t count) {
+    size_t b = (count * sizeof(T) + 255) & ~size_t(255);
+    if (top + b > cap) throw Error{TTG_ERR_NOMEM, "ztt_ksl: device block exhausted"};
+    T* p = (T*)(base + top);
+    top += b;
+    return p;
+  }
+};
+
+inline size_t alz(size_t b) { return (b + 255) & ~size_t(255); }
+
+// S operator (sfun_ksl): Sy (ry1 x ry2) = phi1 (ry1 x rx1*ra) [Sx (rx1 x rx2) phi2 (rx2 x ra*ry2)]
+void sfun_apply(i64 rx1, i64 rx2, i64 ra, i64 ry1, i64 ry2, const double2* phi1,
+                const double2* phi2, const double2* X, double2* Y, int t, double2* res,
+                cudaStream_t s) {
+  {
+    GemmZ g;
+    g.M = (int)rx1; g.N = (int)(ra * ry2); g.K = (int)rx2;
+    g.A = X; g.sAm = 1; g.sAk = rx1;
+    g.B = phi2; g.sBk = 1; g.sBn = rx2;
+    g.C = res; g.sCm = 1; g.sCn = rx1;
+    g.nb2 = t; g.bA2 = rx1 * rx2; g.bC2 = rx1 * ra * ry2;
+    gemm_z(g, s);
+  }
+  {
+    GemmZ g;
+    g.M = (int)ry1; g.N = (int)ry2; g.K = (int)(rx1 * ra);
+    g.A = phi1; g.sAm = 1; g.sAk = ry1;
+    g.B = res; g.sBk = 1; g.sBn = rx1 * ra;
+    g.C = Y; g.sCm = 1; g.sCn = ry1;
+    g.nb2 = t; g.bB2 = rx1 * ra * ry2; g.bC2 = ry1 * ry2;
+    gemm_z(g, s);
+  }
+}
+
+}  // namespace
+
+struct KslParams {
+  int d;
+  std::vector<i64> n, m, ra, ry;
+  const double2* crA;
+  const double2* crY0;
+  double tau;
+  int typ, order, nsteps, verb;
+};
+
+static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>& out_cores,
+                    std::vector<i64>& out_ry, ExpStats& est) {
+  cudaStream_t s = ctx->stream;
+  const int d = P.d;
+  auto& n = P.n;
+  auto& ry = P.ry;
+  TTG_REQUIRE(d >= 1, "ztt_ksl: d must be >= 1");
+  TTG_REQUIRE(ry[0] == 1 && ry[d] == 1 && P.ra[0] == 1 && P.ra[d] == 1, "boundary ranks must be 1");
+  for (int i = 0; i < d; ++i) TTG_REQUIRE(n[i] == P.m[i], "ztt_ksl needs square cores (n == m)");
+  TTG_REQUIRE(P.order >= 2 && P.order + 2 <= 16, "Krylov order must be in [2, 14]");
+  const double eps = 1e-8;
+  std::vector<i64> pa(d + 1, 0);
+  for (int i = 0; i < d; ++i) pa[i + 1] = pa[i] + P.ra[i] * n[i] * P.m[i] * P.ra[i + 1];
+  // capacities: ranks never grow in ztt_ksl
+  std::vector<i64> Rc(ry);
+  i64 capmax = 1, Nmax = 1, phimax = 1, scr = 1, rmx = 1;
+  for (int i = 0; i < d; ++i) {
+    const i64 c = Rc[i] * n[i] * Rc[i + 1];
+    capmax = std::max(capmax, c);
+    Nmax = std::max(Nmax, c);
+    LocalDims L{Rc[i], n[i], Rc[i + 1], Rc[i], n[i], Rc[i + 1], P.ra[i], P.ra[i + 1]};
+    scr = std::max<i64>(scr, (i64)(phi_f64_scratch(L) / sizeof(double)) + 1);
+    scr = std::max<i64>(scr, (L.t1size() + L.t2size()) * 4 + 16);
+    scr = std::max<i64>(scr, (Rc[i] * P.ra[i] * n[i] * Rc[i + 1] + Rc[i] * n[i] * P.ra[i + 1] * Rc[i + 1]) * 4 + 16);
+    rmx = std::max(rmx, Rc[i]);
+  }
+  for (int i = 0; i <= d; ++i) phimax = std::max(phimax, Rc[i] * Rc[i] * P.ra[i]);
+  Nmax = std::max(Nmax, rmx * rmx);
+  i64 ramax = *std::max_element(P.ra.begin(), P.ra.end());
+  scr = std::max<i64>(scr, rmx * ramax * rmx * 4 + 16);
+  size_t total = alz(sizeof(double2) * pa[d]);
+  for (int i = 0; i < d; ++i) total += alz(sizeof(double2) * Rc[i] * n[i] * Rc[i + 1]);
+  for (int i = 0; i <= d; ++i) total += alz(sizeof(double2) * std::max<i64>(1, Rc[i] * Rc[i] * P.ra[i]));
+  total += 5 * alz(sizeof(double2) * capmax) + alz(sizeof(double2) * phimax) +
+           2 * alz(sizeof(double2) * rmx * rmx) + alz(sizeof(double2) * rmx * 2) +
+           alz(sizeof(double2) * scr) + alz(ExpWork::bytes(Nmax, P.order)) + (1 << 16);
+  DevBlockZ mem;
+  mem.alloc(total);
+  double2* dA = mem.take<double2>(pa[d]);
+  std::vector<double2*> cr(d), phi(d + 1);
+  for (int i = 0; i < d; ++i) cr[i] = mem.take<double2>(Rc[i] * n[i] * Rc[i + 1]);
+  for (int i = 0; i <= d; ++i) phi[i] = mem.take<double2>(std::max<i64>(1, Rc[i] * Rc[i] * P.ra[i]));
+  double2* curcr = mem.take<double2>(capmax);
+  double2* t1 = mem.take<double2>(capmax);
+  double2* t2 = mem.take<double2>(capmax);
+  double2* t3 = mem.take<double2>(capmax);
+  double2* Sout = mem.take<double2>(capmax);
+  double2* phitmp = mem.take<double2>(phimax);
+  double2* R = mem.take<double2>(rmx * rmx);
+  double2* Rt = mem.take<double2>(rmx * rmx);
+  double2* tau_ws = mem.take<double2>(rmx * 2);
+  double2* scratch = mem.take<double2>(scr);
+  void* expmem = mem.take<char>(ExpWork::bytes(Nmax, P.order));
+  double* pinned = nullptr;
+  TTG_CUDA(cudaMallocHost(&pinned, 4096 * sizeof(double)));
+  struct PinGuard { double* p; ~PinGuard() { if (p) cudaFreeHost(p); } } pg{pinned};
+  ExpWork w;
+  w.bind(expmem, Nmax, P.order, pinned);
+
+  TTG_CUDA(cudaMemcpyAsync(dA, P.crA, sizeof(double2) * pa[d], cudaMemcpyHostToDevice, s));
+  {
+    i64 off = 0;
+    for (int i = 0; i < d; ++i) {
+      const i64 sz = ry[i] * n[i] * ry[i + 1];
+      TTG_CUDA(cudaMemcpyAsync(cr[i], P.crY0 + off, sizeof(double2) * sz, cudaMemcpyHostToDevice, s));
+      off += sz;
+    }
+  }
+  const double2 one = make_double2(1.0, 0.0);
+  TTG_CUDA(cudaMemcpyAsync(phi[0], &one, sizeof(double2), cudaMemcpyHostToDevice, s));
+  TTG_CUDA(cudaMemcpyAsync(phi[d], &one, sizeof(double2), cudaMemcpyHostToDevice, s));
+  auto A_of = [&](int i) { return dA + pa[i]; };
+  auto Ld = [&](int i) {
+    return LocalDims{ry[i], n[i], ry[i + 1], ry[i], n[i], ry[i + 1], P.ra[i], P.ra[i + 1]};
+  };
+  const double tau0 = P.typ == 2 ? P.tau / 2 : P.tau;
+
+  for (int step = 0; step < P.nsteps; ++step) {
+    // QR sweep, tt_ksl.f90:528-550
+    for (int i = 0; i + 1 < d; ++i) {
+      const i64 rows = ry[i] * n[i];
+      const i64 rnew = std::min(rows, ry[i + 1]);
+      qr_householder_z((int)rows, (int)ry[i + 1], cr[i], R, tau_ws, s);
+      GemmZ g;
+      g.M = (int)rnew; g.N = (int)(n[i + 1] * ry[i + 2]); g.K = (int)ry[i + 1];
+      g.A = R; g.sAm = 1; g.sAk = rnew;
+      g.B = cr[i + 1]; g.sBk = 1; g.sBn = ry[i + 1];
+      g.C = t1; g.sCm = 1; g.sCn = rnew;
+      gemm_z(g, s);
+      TTG_CUDA(cudaMemcpyAsync(cr[i + 1], t1, sizeof(double2) * rnew * n[i + 1] * ry[i + 2],
+                               cudaMemcpyDeviceToDevice, s));
+      ry[i + 1] = rnew;
+      phi_left_z(Ld(i), phi[i], A_of(i), cr[i], cr[i], phi[i + 1], scratch, s);
+    }
+    unsigned long long counter = 0;   // init_seed() at every call, tt_ksl.f90:556
+    auto kstep = [&](int i) {
+      const LocalDims L = Ld(i);
+      const i64 N = L.xsize();
+      const double2 *p1 = phi[i], *p2 = phi[i + 1], *Ai = A_of(i);
+      ZMatvecFn mv = [=](const double2* X, double2* Y, int t) { bfun3_z(L, p1, Ai, p2, X, Y, t, scratch, s); };
+      ZMatvecFn mvT = [=](const double2* X, double2* Y, int t) {
+        bfun3_transp_z(L, p1, Ai, p2, X, Y, t, scratch, s);
+      };
+      const double anorm = znormest_dev(w, N, 4, mv, &mvT, counter, s, &est);
+      zexp_mv_dev(w, N, P.order, tau0, cr[i], curcr, eps, anorm, mv, s, &est);
+    };
+    auto sstep = [&](i64 rx1, i64 rx2, i64 ra, i64 ry1, i64 ry2, const double2* ph1,
+                     const double2* ph2, const double2* Rin) {
+      const i64 N = rx1 * ry2;
+      ZMatvecFn mv = [=](const double2* X, double2* Y, int t) {
+        sfun_apply(rx1, rx2, ra, ry1, ry2, ph1, ph2, X, Y, t, scratch, s);
+      };
+      const double anorm = znormest_dev(w, N, 4, mv, nullptr, counter, s, &est);
+      zexp_mv_dev(w, N, P.order, -tau0, Rin, Sout, eps, anorm, mv, s, &est);
+    };
+    int i = d - 1, dir = -1, swp = 0;
+    while (swp < 1) {
+      kstep(i);
+      if (dir < 0) {
+        if (i > 0) {
+          const i64 cols = n[i] * ry[i + 1];
+          const i64 rnew = std::min(cols, ry[i]);
+          TTG_REQUIRE(rnew == ry[i], "ztt_ksl: the S-step needs a rank-preserving QR");
+          transpose_z(ry[i], cols, curcr, t1, s);                    // cols x ry_i
+          qr_householder_z((int)cols, (int)ry[i], t1, R, tau_ws, s); // Q: cols x rnew
+          transpose_z(cols, rnew, t1, cr[i], s);                     // rnew x cols
+          transpose_z(rnew, ry[i], R, Rt, s);                        // ry_i x rnew
+          LocalDims Lr{rnew, n[i], ry[i + 1], rnew, n[i], ry[i + 1], P.ra[i], P.ra[i + 1]};
+          phi_right_z(Lr, phi[i + 1], A_of(i), cr[i], cr[i], phitmp, scratch, s);
+          sstep(ry[i], ry[i], P.ra[i], rnew, rnew, phi[i], phitmp, Rt);
+          GemmZ g;   // core_{i-1} = core_{i-1} * Stmp (ry_i x rnew)
+          g.M = (int)(ry[i - 1] * n[i - 1]); g.N = (int)rnew; g.K = (int)ry[i];
+          g.A = cr[i - 1]; g.sAm = 1; g.sAk = ry[i - 1] * n[i - 1];
+          g.B = Sout; g.sBk = 1; g.sBn = ry[i];
+          g.C = t2; g.sCm = 1; g.sCn = ry[i - 1] * n[i - 1];
+          gemm_z(g, s);
+          TTG_CUDA(cudaMemcpyAsync(cr[i - 1], t2, sizeof(double2) * ry[i - 1] * n[i - 1] * rnew,
+                                   cudaMemcpyDeviceToDevice, s));
+          ry[i] = rnew;
+          TTG_CUDA(cudaMemcpyAsync(phi[i], phitmp, sizeof(double2) * rnew * P.ra[i] * rnew,
+                                   cudaMemcpyDeviceToDevice, s));
+        } else {
+          TTG_CUDA(cudaMemcpyAsync(cr[i], curcr, sizeof(double2) * Ld(i).xsize(),
+                                   cudaMemcpyDeviceToDevice, s));
+        }
+      } else {
+        if (i < d - 1) {
+          const i64 rows = ry[i] * n[i];
+          const i64 rnew = std::min(rows, ry[i + 1]);
+          TTG_REQUIRE(rnew == ry[i + 1], "ztt_ksl: the S-step needs a rank-preserving QR");
+          qr_householder_z((int)rows, (int)ry[i + 1], curcr, R, tau_ws, s);
+          TTG_CUDA(cudaMemcpyAsync(cr[i], curcr, sizeof(double2) * rows * rnew,
+                                   cudaMemcpyDeviceToDevice, s));
+          LocalDims Ll{ry[i], n[i], rnew, ry[i], n[i], rnew, P.ra[i], P.ra[i + 1]};
+          phi_left_z(Ll, phi[i], A_of(i), cr[i], cr[i], phitmp, scratch, s);
+          sstep(rnew, rnew, P.ra[i + 1], ry[i + 1], ry[i + 1], phitmp, phi[i + 1], R);
+          GemmZ g;   // core_{i+1} = Stmp (rnew x ry_{i+1}) * core_{i+1}
+          g.M = (int)rnew; g.N = (int)(n[i + 1] * ry[i + 2]); g.K = (int)ry[i + 1];
+          g.A = Sout; g.sAm = 1; g.sAk = rnew;
+          g.B = cr[i + 1]; g.sBk = 1; g.sBn = ry[i + 1];
+          g.C = t2; g.sCm = 1; g.sCn = rnew;
+          gemm_z(g, s);
+          TTG_CUDA(cudaMemcpyAsync(cr[i + 1], t2, sizeof(double2) * rnew * n[i + 1] * ry[i + 2],
+                                   cudaMemcpyDeviceToDevice, s));
+          ry[i + 1] = rnew;
+          TTG_CUDA(cudaMemcpyAsync(phi[i + 1], phitmp, sizeof(double2) * rnew * rnew * P.ra[i + 1],
+                                   cudaMemcpyDeviceToDevice, s));
+        } else {
+          TTG_CUDA(cudaMemcpyAsync(cr[i], curcr, sizeof(double2) * Ld(i).xsize(),
+                                   cudaMemcpyDeviceToDevice, s));
+        }
+      }
+      if (dir > 0 && i == d - 1) {
+        dir = -1;
+        i = d - 1;
+        swp++;
+      } else if (dir < 0 && i == 0) {
+        dir = 1;
+        i = 0;
+        if (P.typ == 1) break;
+      } else {
+        i += dir;
+      }
+    }
+    if (P.verb > 0) fprintf(stderr, "ztt_ksl: step %d done\n", step + 1);
+  }
+  (void)t3;
+  TTG_CUDA(cudaStreamSynchronize(s));
+  i64 tot = 0;
+  for (int k = 0; k < d; ++k) tot += ry[k] * n[k] * ry[k + 1];
+  out_cores.resize(tot);
+  i64 off = 0;
+  for (int k = 0; k < d; ++k) {
+    const i64 sz = ry[k] * n[k] * ry[k + 1];
+    TTG_CUDA(cudaMemcpyAsync(out_cores.data() + off, cr[k], sizeof(double2) * sz,
+                             cudaMemcpyDeviceToHost, s));
+    off += sz;
+  }
+  TTG_CUDA(cudaStreamSynchronize(s));
+  out_ry = ry;
+}
+
+}  // namespace ttg
+
+using namespace ttg;
+
+extern "C" int ttg_ksl_z(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
+                         const ttg_int* ra, const double* crA, const double* crY0, ttg_int* ry,
+                         double tau, ttg_int rmax, int verb, int typ, int order, int method,
+                         ttg_int nsteps) {
+  if (!ctx) return TTG_ERR_ARG;
+  try {
+    TTG_CUDA(cudaSetDevice(ctx->device));
+    TTG_REQUIRE(d > 0 && n && m && ra && crA && crY0 && ry, "null argument");
+    TTG_REQUIRE(method == TTG_METHOD_PLAIN, "ztt_ksl: only the FP64 method is built");
+    TTG_REQUIRE(typ == 1 || typ == 2, "typ must be 1 (KSL) or 2 (symmetric KSL)");
+    (void)rmax;   // read but unused by the reference as well (tt_ksl.f90:446)
+    KslParams P;
+    P.d = (int)d;
+    P.n.assign(n, n + d);
+    P.m.assign(m, m + d);
+    P.ra.assign(ra, ra + d + 1);
+    P.ry.assign(ry, ry + d + 1);
+    P.crA = (const double2*)crA;
+    P.crY0 = (const double2*)crY0;
+    P.tau = tau;
+    P.typ = typ;
+    P.order = order > 0 ? order : 8;
+    P.nsteps = nsteps > 0 ? (int)nsteps : 1;
+    P.verb = verb;
+    long long l0 = g_launches;
+    ExpStats est;
+    std::vector<i64> ry_out;
+    run_ksl(ctx, P, ctx->zresult_core, ry_out, est);
+    for (int k = 0; k <= d; ++k) ry[k] = ry_out[k];
+    ctx->result_core.clear();
+    ctx->stat_matvecs = est.nmult;
+    ctx->stat_sweeps = P.nsteps;
+    ctx->stat_res = 0.0;
+    ctx->stat_launches = g_launches - l0;
+  } catch (const ttg::Error& e) {
+    ctx->last_error = e.msg;
+    return e.code;
+  }
+  return TTG_OK;
+}

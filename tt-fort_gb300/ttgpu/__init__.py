@@ -178,15 +178,16 @@ def tt_eigb(d, n, m, ra, crA, crY0, ry, eps, rmax, B, kickrank=None, nswp=20,
 
 
 def ztt_ksl(d, n, m, ra, crA, crY0, ry, tau, rmax, kickrank=None, nswp=None, verb=0, typ=2,
-            order=8, method="plain", ctx=None):
-    """One KSL time step (ztt_ksl, tt_ksl.f90:431).  Returns (cores, ry)."""
+            order=8, method="plain", nsteps=1, ctx=None):
+    """KSL time stepping (ztt_ksl, tt_ksl.f90:431): ``nsteps`` consecutive
+    steps of size tau on the device.  Returns (cores, ry)."""
     ctx = ctx or default_context()
     n_, m_, ra_ = _iarr(n), _iarr(m), _iarr(ra)
     ry_ = _iarr(ry).copy()
     A_, Y_ = _carr(crA), _carr(crY0)
     rc = lib().ttg_ksl_z(ctx.handle, _i64(d), _p(n_), _p(m_), _p(ra_), _p(A_), _p(Y_), _p(ry_),
                          C.c_double(tau), _i64(rmax), C.c_int(verb), C.c_int(typ),
-                         C.c_int(order), C.c_int(METHOD[method]))
+                         C.c_int(order), C.c_int(METHOD[method]), _i64(nsteps))
     ctx.check(rc)
     return _result(ctx, real=False), [int(v) for v in ry_]
 
