@@ -9,10 +9,3 @@ extern "C" int ttg_dmaxvol(ttg_ctx* c, ttg_int, ttg_int, const double*, ttg_int*
   return TTG_ERR_UNSUPPORTED;
 }
 
-extern "C" int ttg_amen_solve(ttg_ctx* c, ttg_int, const ttg_int*, const ttg_int*, const ttg_int*,
-                              const ttg_int*, const double*, const double*, const double*,
-                              ttg_int*, double, ttg_int, ttg_int, ttg_int, int, int) {
-  if (!c) return TTG_ERR_ARG;
-  c->last_error = "amen: not built yet";
-  return TTG_ERR_UNSUPPORTED;
-}
