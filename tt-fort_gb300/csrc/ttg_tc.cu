@@ -6,9 +6,12 @@
 //   GEMM1  T1[(b1,j,v), (a2,c2)] = sum_b2 X_v[(b1,j), b2] Phi2[b2, (a2,c2)]
 //          M = rx1*m*nvec (all vectors of the block stacked), N = ra2*ry2, K = rx2
 //   CORE   T2[(i,c2,v), (b1,a1)] = sum_(j,a2) A[(a1,i),(j,a2)] T1[(b1,j,v),(a2,c2)]
-//   GEMM3  Y^T[(i,c2,v), c1]     = sum_(b1,a1) T2[(i,c2,v),(b1,a1)] Phi1[c1,(b1,a1)]
-//          M = n*ry2*nvec, N = ry1, K = rx1*ra1
+//   GEMM3  Y[c1, (i,c2,v)]       = sum_(b1,a1) Phi1[c1,(b1,a1)] T2[(i,c2,v),(b1,a1)]
+//          M = ry1, N = n*ry2*nvec, K = rx1*ra1
 //
+// Both GEMMs put the index that is contiguous in their output (b1 in T1, c1
+// in y) on the MMA M side, i.e. on TMEM lanes, so the epilogue stores of a
+// warp are coalesced.
 // Every FP64 operand a is split as a_hi = bf16(a), a_lo = bf16(a - a_hi) and a
 // product is accumulated as a_hi b_hi + a_hi b_lo + a_lo b_hi in FP32 in
 // tensor memory (the dropped a_lo b_lo term is ~2^-16 relative).  Operands
@@ -173,31 +176,40 @@ __device__ __forceinline__ void split2(double v, bf16& hi, bf16& lo) {
 
 // split an FP64 matrix into tiled hi/lo planes; element (r, k) is read at
 // src[(r / rv) * vs + (r % rv) * sr + k * sk]; padding is written as zero.
+// One thread per (row, 8-wide K group): rows vary fastest across a warp
+// (coalesced reads when sr == 1) and each thread stores one 16-byte core
+// matrix row per plane.
 __global__ void split_kernel(const double* __restrict__ src, i64 rv, i64 vs, i64 sr, i64 sk,
                              int rows, int cols, int R, int rtiles, int ktiles,
                              bf16* __restrict__ hi, bf16* __restrict__ lo) {
-  const i64 tr = (i64)rtiles * R, tk = (i64)ktiles * TK;
-  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tr * tk;
+  const i64 tr = (i64)rtiles * R, tk8 = (i64)ktiles * (TK / 8);
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tr * tk8;
        e += (i64)gridDim.x * blockDim.x) {
-    int r = (int)(e % tr), k = (int)(e / tr);
-    double v = 0.0;
-    if (r < rows && k < cols) v = src[(r / rv) * vs + (r % rv) * sr + (i64)k * sk];
-    bf16 h, l;
-    split2(v, h, l);
-    size_t idx = tiled_index(r, k, R, ktiles);
-    hi[idx] = h;
-    lo[idx] = l;
+    const int r = (int)(e % tr), k0 = (int)(e / tr) * 8;
+    const double* row = src + (r / rv) * vs + (r % rv) * sr;
+    __align__(16) bf16 h[8], l[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      double v = 0.0;
+      if (r < rows && k0 + q < cols) v = row[(i64)(k0 + q) * sk];
+      split2(v, h[q], l[q]);
+    }
+    const size_t idx = tiled_index(r, k0, R, ktiles);
+    *reinterpret_cast<uint4*>(hi + idx) = *reinterpret_cast<const uint4*>(h);
+    *reinterpret_cast<uint4*>(lo + idx) = *reinterpret_cast<const uint4*>(l);
   }
 }
 
 // C[m, n] (m < M, n < N) = sum_k A[m, k] B[n, k], split-3 on tcgen05.
-// Output row m goes to out + (m / rpv) * vstride + (m % rpv) * rstride + n.
+// C[m, n] goes to out[(m / rpv) * vstride + (m % rpv) * rstride + n * cstride].
+// The accumulator row m sits in TMEM lane m % 128, so with rstride == 1 the
+// 32 lanes of a warp store 32 consecutive elements (coalesced).
 template <int BN, int STAGES, class OutT>
 __global__ void __launch_bounds__(NTHREADS, 1)
     split_gemm_kernel(const bf16* __restrict__ Ahi, const bf16* __restrict__ Alo,
                       const bf16* __restrict__ Bhi, const bf16* __restrict__ Blo, int M, int N,
                       int ktiles, OutT* __restrict__ out, i64 rpv, i64 vstride, i64 rstride,
-                      int* __restrict__ err) {
+                      i64 cstride, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   constexpr uint32_t A_BYTES = TM * TK * 2;
   constexpr uint32_t B_BYTES = BN * TK * 2;
@@ -304,7 +316,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
           const int n = n0 + c0 + q;
-          if (n < N) orow[n] = (OutT)__uint_as_float(r[q]);
+          if (n < N) orow[(i64)n * cstride] = (OutT)__uint_as_float(r[q]);
         }
       }
     }
@@ -315,51 +327,213 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 }
 
 // CORE: T2[(i,c2,v),(b1,a1)] = sum_(j,a2) A[(a1,i),(j,a2)] T1[(b1,j,v),(a2,c2)]
-// one thread per (b1, c2, v); writes the split tiled A-operand of GEMM3.
-__global__ void core_kernel(const float* __restrict__ T1, int ldT1, const double* __restrict__ A,
-                            int rx1, int m, int n, int ra1, int ra2, int ry2, int nvec,
-                            int R3, int ktiles3, bf16* __restrict__ hi, bf16* __restrict__ lo) {
-  extern __shared__ float As[];
-  const int asz = ra1 * n * m * ra2;
-  const bool in_smem = asz <= 12288;
-  if (in_smem)
-    for (int e = threadIdx.x; e < asz; e += blockDim.x) As[e] = (float)A[e];
-  __syncthreads();
-  const i64 total = (i64)rx1 * ry2 * nvec;
+// T1 is column-major with leading dimension ld1 over the rows (b1,j,v), so
+// b1 is contiguous; the result is written split and tiled as the B operand of
+// GEMM3 (rows (i,c2,v), K (b1,a1), tile rows 1 << lgR3).
+
+__device__ __forceinline__ size_t tiled_index_pow2(int r, int k, int lgR, int ktiles) {
+  const size_t tile = (size_t)(r >> lgR) * ktiles + (k >> 6);
+  return (tile << (lgR + 6)) + (tile_offset(r & ((1 << lgR) - 1), k & (TK - 1), 1 << lgR) >> 1);
+}
+__device__ __forceinline__ void split2f(float v, bf16& hi, bf16& lo) {
+  hi = __float2bfloat16_rn(v);
+  lo = __float2bfloat16_rn(v - __bfloat162float(hi));   // v - hi is exact in FP32
+}
+
+// the TT-matrix core as a kernel parameter: a[q * NA + p] = A(a1,i,j,a2) with
+// q = j + m*a2 and p = a1 + ra1*i, so every FMA reads it from the constant bank
+template <int JA, int NA>
+struct CoreCoef {
+  float a[JA * NA];
+};
+
+// small cores (m*ra2 <= JA, n*ra1 <= NA): one thread per (B1 consecutive b1,
+// c2, v); with B1 == 8 a thread loads 2 float4 per input and stores one
+// 16-byte core-matrix row per output and plane.
+template <int JA, int NA, int B1>
+__global__ void __launch_bounds__(128)
+    core_small_kernel(const float* __restrict__ T1, i64 ld1, const CoreCoef<JA, NA> A, int rx1,
+                      int m, int ra2, int n, int ra1, int ry2, int nvec, int lgR3, int ktiles3,
+                      bf16* __restrict__ hi, bf16* __restrict__ lo) {
+  const int ja = m * ra2, na = n * ra1;
+  const int nb = rx1 / B1;
+  const i64 total = (i64)nb * ry2 * nvec;
   for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total;
        e += (i64)gridDim.x * blockDim.x) {
-    const int b1 = (int)(e % rx1);
-    const int c2 = (int)((e / rx1) % ry2);
-    const int v = (int)(e / ((i64)rx1 * ry2));
-    for (int a1 = 0; a1 < ra1; ++a1) {
-      for (int i = 0; i < n; ++i) {
-        float acc = 0.f;
-        for (int a2 = 0; a2 < ra2; ++a2) {
-          for (int j = 0; j < m; ++j) {
-            const i64 row = (i64)b1 + (i64)rx1 * j + (i64)rx1 * m * v;
-            const float t = T1[row * ldT1 + a2 + (i64)ra2 * c2];
-            const int ai = a1 + ra1 * (i + n * (j + m * a2));
-            const float a = in_smem ? As[ai] : (float)__ldg(A + ai);
-            acc = fmaf(a, t, acc);
+    const int b1 = (int)(e % nb) * B1;
+    const int c2 = (int)((e / nb) % ry2);
+    const int v = (int)(e / ((i64)nb * ry2));
+    const float* tb = T1 + b1 + (i64)rx1 * m * v + ld1 * ((i64)ra2 * c2);
+    float t[JA][B1];
+    {
+      int j = 0, a2 = 0;
+#pragma unroll
+      for (int q = 0; q < JA; ++q) {
+        if (q < ja) {
+          const float* src = tb + (i64)rx1 * j + ld1 * a2;
+          if (B1 == 8) {
+            const float4 u = *reinterpret_cast<const float4*>(src);
+            const float4 w = *reinterpret_cast<const float4*>(src + 4);
+            t[q][0] = u.x; t[q][1 % B1] = u.y; t[q][2 % B1] = u.z; t[q][3 % B1] = u.w;
+            t[q][4 % B1] = w.x; t[q][5 % B1] = w.y; t[q][6 % B1] = w.z; t[q][7 % B1] = w.w;
+          } else {
+#pragma unroll
+            for (int b = 0; b < B1; ++b) t[q][b] = src[b];
+          }
+          if (++j == m) { j = 0; ++a2; }
+        }
+      }
+    }
+    int a1 = 0, i = 0;
+#pragma unroll
+    for (int p = 0; p < NA; ++p) {
+      if (p < na) {
+        float acc[B1];
+#pragma unroll
+        for (int b = 0; b < B1; ++b) acc[b] = 0.f;
+#pragma unroll
+        for (int q = 0; q < JA; ++q) {
+          if (q < ja) {
+            const float a = A.a[q * NA + p];
+#pragma unroll
+            for (int b = 0; b < B1; ++b) acc[b] = fmaf(a, t[q][b], acc[b]);
           }
         }
-        const int r = i + n * c2 + n * ry2 * v;
+        const int r = i + n * (c2 + ry2 * v);
         const int k = b1 + rx1 * a1;
-        bf16 h, l;
-        split2((double)acc, h, l);
-        const size_t idx = tiled_index(r, k, R3, ktiles3);
-        hi[idx] = h;
-        lo[idx] = l;
+        const size_t idx = tiled_index_pow2(r, k, lgR3, ktiles3);
+        if (B1 == 8) {
+          __align__(16) bf16 h[8], l[8];
+#pragma unroll
+          for (int b = 0; b < 8; ++b) split2f(acc[b % B1], h[b], l[b]);
+          *reinterpret_cast<uint4*>(hi + idx) = *reinterpret_cast<const uint4*>(h);
+          *reinterpret_cast<uint4*>(lo + idx) = *reinterpret_cast<const uint4*>(l);
+        } else {
+#pragma unroll
+          for (int b = 0; b < B1; ++b) {
+            bf16 h, l;
+            split2f(acc[b], h, l);
+            const size_t ib = tiled_index_pow2(r, k + b, lgR3, ktiles3);
+            hi[ib] = h;
+            lo[ib] = l;
+          }
+        }
+        if (++a1 == ra1) { a1 = 0; ++i; }
       }
     }
   }
 }
 
-static int pick_bn(int N) {
-  int best = 64, waste = 1 << 30;
+// large cores (KSL/AMEn mode sizes n = 32..64): a tiled FP32 product over the
+// flattened rows e = b1 + rx1*(c2 + ry2*v) (64 per block) and the outputs
+// p = (a1, i) (64 per block), K = (j, a2) in chunks of 32; 256 threads with
+// 4 x 4 results each.  A(a1,i,j,a2) sits at A[p + n*ra1*q].
+constexpr int CT_R = 64, CT_P = 64, CT_Q = 32;
+__global__ void __launch_bounds__(256)
+    core_tiled_kernel(const float* __restrict__ T1, i64 ld1, const double* __restrict__ A,
+                      int rx1, int m, int ra2, int n, int ra1, int ry2, int nvec, int lgR3,
+                      int ktiles3, bf16* __restrict__ hi, bf16* __restrict__ lo) {
+  __shared__ float Ts[CT_Q][CT_R + 4];
+  __shared__ float As[CT_Q][CT_P + 4];
+  __shared__ i64 rbase[CT_R];
+  const int ja = m * ra2, na = n * ra1;
+  const i64 rows = (i64)rx1 * ry2 * nvec;
+  const i64 row0 = (i64)blockIdx.x * CT_R;
+  const int p0 = blockIdx.y * CT_P;
+  const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+  if (tid < CT_R) {
+    const i64 row = row0 + tid;
+    i64 base = -1;
+    if (row < rows) {
+      const int b1 = (int)(row % rx1);
+      const i64 cv = row / rx1;
+      const int c2 = (int)(cv % ry2), v = (int)(cv / ry2);
+      base = b1 + (i64)rx1 * m * v + ld1 * ((i64)ra2 * c2);
+    }
+    rbase[tid] = base;
+  }
+  float acc[4][4];
+#pragma unroll
+  for (int x = 0; x < 4; ++x)
+#pragma unroll
+    for (int y = 0; y < 4; ++y) acc[x][y] = 0.f;
+  for (int q0 = 0; q0 < ja; q0 += CT_Q) {
+    __syncthreads();
+    for (int l = tid; l < CT_R * CT_Q; l += 256) {
+      const int rr = l % CT_R, qq = l / CT_R, q = q0 + qq;
+      const i64 base = rbase[rr];
+      float val = 0.f;
+      if (base >= 0 && q < ja) val = T1[base + (i64)rx1 * (q % m) + ld1 * (q / m)];
+      Ts[qq][rr] = val;
+    }
+    for (int l = tid; l < CT_P * CT_Q; l += 256) {
+      const int pp = l % CT_P, qq = l / CT_P, p = p0 + pp, q = q0 + qq;
+      As[qq][pp] = (p < na && q < ja) ? (float)A[p + (i64)na * q] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int qq = 0; qq < CT_Q; ++qq) {
+      const float4 t4 = *reinterpret_cast<const float4*>(&Ts[qq][ty * 4]);
+      const float4 a4 = *reinterpret_cast<const float4*>(&As[qq][tx * 4]);
+      const float tv[4] = {t4.x, t4.y, t4.z, t4.w}, av[4] = {a4.x, a4.y, a4.z, a4.w};
+#pragma unroll
+      for (int x = 0; x < 4; ++x)
+#pragma unroll
+        for (int y = 0; y < 4; ++y) acc[x][y] = fmaf(tv[x], av[y], acc[x][y]);
+    }
+  }
+#pragma unroll
+  for (int x = 0; x < 4; ++x) {
+    const i64 row = row0 + ty * 4 + x;
+    if (row >= rows) continue;
+    const int b1 = (int)(row % rx1);
+    const i64 cv = row / rx1;
+#pragma unroll
+    for (int y = 0; y < 4; ++y) {
+      const int p = p0 + tx * 4 + y;
+      if (p >= na) continue;
+      const int a1 = p % ra1, i = p / ra1;
+      const int r = (int)(i + (i64)n * cv);
+      const int k = b1 + rx1 * a1;
+      bf16 h, l;
+      split2f(acc[x][y], h, l);
+      const size_t idx = tiled_index_pow2(r, k, lgR3, ktiles3);
+      hi[idx] = h;
+      lo[idx] = l;
+    }
+  }
+}
+
+static int num_sms() {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0)
+      nsm = 148;
+  }
+  return nsm;
+}
+
+constexpr int stages_for(int bn) { return bn == 256 ? 2 : (bn == 128 ? 3 : 2); }
+constexpr size_t smem_for(int bn) {
+  return (size_t)stages_for(bn) * ((size_t)2 * TM * TK * 2 + (size_t)2 * bn * TK * 2) + 1024;
+}
+
+// B-operand tile rows for an M x N x K product: the estimated time is the
+// number of waves (CTAs over SMs x resident CTAs) times the per-tile cost
+// (K loop of MMAs and bulk copies plus the epilogue), so small products pick
+// narrow tiles that spread over more SMs and large ones pick wide tiles.
+static int pick_bn(int M, int N, int K) {
+  const int mt = ceil_div(M, TM), kt = ceil_div(K, TK), nsm = num_sms();
+  int best = 64;
+  double best_cost = 1e300;
   for (int bn : {256, 128, 64}) {
-    int w = ceil_div(N, bn) * bn - N;
-    if (w < waste) { waste = w; best = bn; }
+    const int per_sm = (int)std::max<size_t>(1, 228 * 1024 / (smem_for(bn) + 1024));
+    const long long ctas = (long long)mt * ceil_div(N, bn);
+    const long long waves = (ctas + (long long)nsm * per_sm - 1) / ((long long)nsm * per_sm);
+    const double cost = (double)waves * (kt * (bn / 64.0 + 1.0) + bn / 64.0 + 2.0);
+    if (cost < best_cost - 1e-9) { best_cost = cost; best = bn; }
   }
   return best;
 }
@@ -381,7 +555,7 @@ static size_t tiled_bytes(int rows, int cols, int R) {
 
 static void split_into(const double* src, i64 rv, i64 vs, i64 sr, i64 sk, const Tiled& t,
                        cudaStream_t s) {
-  i64 total = (i64)t.rtiles * t.R * t.ktiles * TK;
+  i64 total = (i64)t.rtiles * t.R * t.ktiles * (TK / 8);
   int blocks = (int)std::min<i64>(8192, (total + 255) / 256);
   split_kernel<<<blocks, 256, 0, s>>>(src, rv, vs, sr, sk, t.rows, t.cols, t.R, t.rtiles,
                                       t.ktiles, t.hi, t.lo);
@@ -390,10 +564,9 @@ static void split_into(const double* src, i64 rv, i64 vs, i64 sr, i64 sk, const 
 
 template <int BN, class OutT>
 static void gemm_launch_bn(const Tiled& A, const Tiled& B, int M, int N, OutT* out, i64 rpv,
-                           i64 vstride, i64 rstride, int* err, cudaStream_t s) {
-  constexpr int STAGES = BN == 256 ? 2 : (BN == 128 ? 3 : 4);
-  constexpr size_t stage = (size_t)2 * TM * TK * 2 + (size_t)2 * BN * TK * 2;
-  constexpr size_t smem = STAGES * stage + 1024 + SMEM_PAD;
+                           i64 vstride, i64 rstride, i64 cstride, int* err, cudaStream_t s) {
+  constexpr int STAGES = stages_for(BN);
+  constexpr size_t smem = smem_for(BN) + SMEM_PAD;
   auto kern = split_gemm_kernel<BN, STAGES, OutT>;
   static bool attr = false;
   if (!attr) {
@@ -402,42 +575,49 @@ static void gemm_launch_bn(const Tiled& A, const Tiled& B, int M, int N, OutT* o
   }
   dim3 grid(A.rtiles, B.rtiles);
   kern<<<grid, NTHREADS, smem, s>>>(A.hi, A.lo, B.hi, B.lo, M, N, A.ktiles, out, rpv, vstride,
-                                    rstride, err);
+                                    rstride, cstride, err);
   TTG_CHECK_LAUNCH();
 }
 
 template <class OutT>
 static void gemm_launch(const Tiled& A, const Tiled& B, int M, int N, OutT* out, i64 rpv,
-                        i64 vstride, i64 rstride, int* err, cudaStream_t s) {
+                        i64 vstride, i64 rstride, i64 cstride, int* err, cudaStream_t s) {
   TTG_REQUIRE(A.ktiles == B.ktiles, "split gemm: K tiles differ");
-  if (B.R == 256) gemm_launch_bn<256>(A, B, M, N, out, rpv, vstride, rstride, err, s);
-  else if (B.R == 128) gemm_launch_bn<128>(A, B, M, N, out, rpv, vstride, rstride, err, s);
-  else gemm_launch_bn<64>(A, B, M, N, out, rpv, vstride, rstride, err, s);
+  TTG_REQUIRE(A.R == TM, "split gemm: A tiles must have 128 rows");
+  if (B.R == 256) gemm_launch_bn<256>(A, B, M, N, out, rpv, vstride, rstride, cstride, err, s);
+  else if (B.R == 128) gemm_launch_bn<128>(A, B, M, N, out, rpv, vstride, rstride, cstride, err, s);
+  else gemm_launch_bn<64>(A, B, M, N, out, rpv, vstride, rstride, cstride, err, s);
 }
 
 }  // namespace tc
 
 // prepared split operator of one local problem
+//   GEMM1: A = X (rows (b1,j,v), K b2), B = Phi2 (rows (a2,c2), K b2),
+//          T1 column-major (rows (b1,j,v), ld1 = rx1*m*nvec_max)
+//   CORE : T1 -> T2 (GEMM3 B operand: rows (i,c2,v), K (b1,a1))
+//   GEMM3: A = Phi1 (rows c1, K (b1,a1)), B = T2, y[c1 + ry1*(i,c2,v)]
 struct SplitOp {
   LocalDims L;
   int nvec_max;
   int bn1, bn3;
-  tc::Tiled X, P2, T2, P1;     // GEMM1 A/B, GEMM3 A/B
+  tc::Tiled X, P2, P1, T2;
   float* T1;
-  int ldT1;
+  i64 ld1;
   const double* A;
   int* err;
+  int coef_kind;        // 0: tiled CORE kernel; 1..4: small CORE with (JA, NA) bound
+  float coef[256];      // A as FP32 in its own column-major order (small CORE)
 };
 
 static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* base) {
   const int M1 = (int)(L.rx1 * L.m * nvec_max), N1 = (int)(L.ra2 * L.ry2), K1 = (int)L.rx2;
-  const int M3 = (int)(L.n * L.ry2 * nvec_max), N3 = (int)L.ry1, K3 = (int)(L.rx1 * L.ra1);
-  const int bn1 = tc::pick_bn(N1), bn3 = tc::pick_bn(N3);
+  const int M3 = (int)L.ry1, N3 = (int)(L.n * L.ry2 * nvec_max), K3 = (int)(L.rx1 * L.ra1);
+  const int bn1 = tc::pick_bn(M1, N1, K1), bn3 = tc::pick_bn(M3, N3, K3);
   size_t tot = 0;
   tot += tc::tiled_bytes(M1, K1, tc::TM) + tc::tiled_bytes(N1, K1, bn1);
   tot += tc::tiled_bytes(M3, K3, tc::TM) + tc::tiled_bytes(N3, K3, bn3);
-  const int ldT1 = ceil_div(N1, 4) * 4;
-  size_t t1 = ((size_t)ceil_div(M1, tc::TM) * tc::TM * ldT1 * sizeof(float) + 1023) & ~size_t(1023);
+  const i64 ld1 = (i64)ceil_div(M1, 4) * 4;
+  size_t t1 = ((size_t)ld1 * ceil_div(N1, 4) * 4 * sizeof(float) + 1023) & ~size_t(1023);
   tot += t1 + 1024 + sizeof(SplitOp) + 1024;
   if (op && base) {
     char* p = base;
@@ -446,10 +626,10 @@ static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* 
     op->bn1 = bn1; op->bn3 = bn3;
     op->X = tc::make_tiled(M1, K1, tc::TM, p);
     op->P2 = tc::make_tiled(N1, K1, bn1, p);
-    op->T2 = tc::make_tiled(M3, K3, tc::TM, p);
-    op->P1 = tc::make_tiled(N3, K3, bn3, p);
+    op->P1 = tc::make_tiled(M3, K3, tc::TM, p);
+    op->T2 = tc::make_tiled(N3, K3, bn3, p);
     op->T1 = (float*)p; p += t1;
-    op->ldT1 = ldT1;
+    op->ld1 = ld1;
     op->err = (int*)p; p += 1024;
   }
   return tot;
@@ -458,56 +638,100 @@ static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* 
 size_t split_op_bytes(const LocalDims& L, int nvec_max) { return split_layout(L, nvec_max, nullptr, nullptr); }
 
 bool split_op_supported(const LocalDims& L) {
-  return L.rx1 * L.m * 32 < (1ll << 31) && L.n * L.ry2 * 32 < (1ll << 31);
+  return L.rx1 * L.m * 64 < (1ll << 31) && L.n * L.ry2 * 64 < (1ll << 31) &&
+         L.rx1 * L.m * 64 * L.ra2 * L.ry2 < (1ll << 40);
 }
 
-// prepare: split Phi2 (GEMM1 B: rows (a2,c2), K b2) and Phi1^T (GEMM3 B: rows
+// prepare: split Phi2 (GEMM1 B: rows (a2,c2), K b2) and Phi1 (GEMM3 A: rows
 // c1, K (b1,a1)) once per local problem.  The SplitOp header lives in host
 // memory owned by the caller; mem holds the device buffers.
 void split_op_prepare(SplitOp* op, const LocalDims& L, int nvec_max, const double* phi1,
                       const double* A, const double* phi2, void* mem, cudaStream_t s) {
   split_layout(L, nvec_max, op, (char*)mem);
   op->A = A;
+  // small TT-matrix cores travel as a kernel parameter of the CORE kernel
+  const int ja = (int)(L.m * L.ra2), na = (int)(L.n * L.ra1);
+  op->coef_kind = 0;
+  if (ja <= 4 && na <= 4) op->coef_kind = 1;
+  else if (ja <= 8 && na <= 8) op->coef_kind = 2;
+  else if (ja <= 10 && na <= 10) op->coef_kind = 3;
+  else if (ja <= 16 && na <= 16) op->coef_kind = 4;
+  if (op->coef_kind) {
+    double ah[256];
+    TTG_CUDA(cudaMemcpyAsync(ah, A, (size_t)ja * na * sizeof(double), cudaMemcpyDeviceToHost, s));
+    TTG_CUDA(cudaStreamSynchronize(s));
+    for (int e = 0; e < ja * na; ++e) op->coef[e] = (float)ah[e];
+  }
   // Phi2 element (n=(a2,c2), k=b2) at phi2[b2 + rx2*n]
   tc::split_into(phi2, 1ll << 40, 0, L.rx2, 1, op->P2, s);
-  // Phi1^T element (n=c1, k=(b1,a1)) at phi1[c1 + ry1*k]
+  // Phi1 element (c1, k=(b1,a1)) at phi1[c1 + ry1*k]
   tc::split_into(phi1, 1ll << 40, 0, 1, L.ry1, op->P1, s);
-  // T2 padding (rows and K columns the CORE kernel never writes) must be zero:
-  // padded K columns meet zero columns of Phi1, and 0 * garbage could be NaN
+  // T2 padding (K columns the CORE kernel never writes) must be zero: padded
+  // K columns meet zero columns of Phi1, and 0 * garbage could be NaN
   TTG_CUDA(cudaMemsetAsync(op->T2.hi, 0, op->T2.elems() * sizeof(tc::bf16), s));
   TTG_CUDA(cudaMemsetAsync(op->T2.lo, 0, op->T2.elems() * sizeof(tc::bf16), s));
   TTG_CUDA(cudaMemsetAsync(op->err, 0, sizeof(int), s));
+}
+
+static void core_apply(SplitOp* op, int nvec, cudaStream_t s) {
+  const LocalDims& L = op->L;
+  const tc::Tiled& T2 = op->T2;
+  const int lgR3 = T2.R == 256 ? 8 : (T2.R == 128 ? 7 : 6);
+  const int ja = (int)(L.m * L.ra2), na = (int)(L.n * L.ra1);
+  if (op->coef_kind > 0) {
+    const bool wide = L.rx1 % 8 == 0 && (L.rx1 / 8) * L.ry2 * nvec >= 32768;
+    const i64 total = (wide ? L.rx1 / 8 : L.rx1) * L.ry2 * nvec;
+    const int blocks = (int)std::min<i64>(8192, (total + 127) / 128);
+#define TTG_CORE_SMALL(JA, NA)                                                                  \
+  do {                                                                                          \
+    tc::CoreCoef<JA, NA> cc;                                                                    \
+    for (int q = 0; q < JA; ++q)                                                                \
+      for (int p = 0; p < NA; ++p)                                                              \
+        cc.a[q * NA + p] = (q < ja && p < na) ? op->coef[(size_t)q * na + p] : 0.f;            \
+    if (wide)                                                                                   \
+      tc::core_small_kernel<JA, NA, 8><<<blocks, 128, 0, s>>>(                                 \
+          op->T1, op->ld1, cc, (int)L.rx1, (int)L.m, (int)L.ra2, (int)L.n, (int)L.ra1,         \
+          (int)L.ry2, nvec, lgR3, T2.ktiles, T2.hi, T2.lo);                                    \
+    else                                                                                        \
+      tc::core_small_kernel<JA, NA, 1><<<blocks, 128, 0, s>>>(                                 \
+          op->T1, op->ld1, cc, (int)L.rx1, (int)L.m, (int)L.ra2, (int)L.n, (int)L.ra1,         \
+          (int)L.ry2, nvec, lgR3, T2.ktiles, T2.hi, T2.lo);                                    \
+  } while (0)
+    switch (op->coef_kind) {
+      case 1: TTG_CORE_SMALL(4, 4); break;
+      case 2: TTG_CORE_SMALL(8, 8); break;
+      case 3: TTG_CORE_SMALL(10, 10); break;
+      default: TTG_CORE_SMALL(16, 16); break;
+    }
+#undef TTG_CORE_SMALL
+  } else {
+    const i64 rows = L.rx1 * L.ry2 * nvec;
+    dim3 grid((unsigned)ceil_div(rows, (i64)tc::CT_R), (unsigned)ceil_div(na, tc::CT_P));
+    tc::core_tiled_kernel<<<grid, 256, 0, s>>>(op->T1, op->ld1, op->A, (int)L.rx1, (int)L.m,
+                                              (int)L.ra2, (int)L.n, (int)L.ra1, (int)L.ry2, nvec,
+                                              lgR3, T2.ktiles, T2.hi, T2.lo);
+  }
+  TTG_CHECK_LAUNCH();
 }
 
 void split_op_apply(SplitOp* op, const double* x, double* y, int nvec, cudaStream_t s) {
   const LocalDims& L = op->L;
   TTG_REQUIRE(nvec >= 1 && nvec <= op->nvec_max, "split matvec: nvec out of range");
   const int M1 = (int)(L.rx1 * L.m * nvec), N1 = (int)(L.ra2 * L.ry2);
-  const int M3 = (int)(L.n * L.ry2 * nvec), N3 = (int)L.ry1;
+  const int M3 = (int)L.ry1, N3 = (int)(L.n * L.ry2 * nvec);
   // X_v element (row (b1,j), k=b2) at x[v*xsize + row + rx1*m*b2]
   tc::Tiled X = op->X;
   X.rows = M1;
+  X.rtiles = ceil_div(M1, tc::TM);
   tc::split_into(x, L.rx1 * L.m, L.xsize(), 1, L.rx1 * L.m, X, s);
-  // GEMM1 -> T1 (fp32 row-major, ld ldT1); only the M tiles in use
-  tc::Tiled Xa = X;
-  Xa.rtiles = ceil_div(M1, tc::TM);
-  tc::gemm_launch<float>(Xa, op->P2, M1, N1, op->T1, 1ll << 40, 0, op->ldT1, op->err, s);
+  // GEMM1 -> T1 column-major: T1[row + ld1 * col]
+  tc::gemm_launch<float>(X, op->P2, M1, N1, op->T1, 1ll << 40, 0, 1, op->ld1, op->err, s);
   // CORE -> T2 tiled
-  {
-    tc::Tiled T2 = op->T2;
-    i64 total = L.rx1 * L.ry2 * nvec;
-    int blocks = (int)std::min<i64>(4096, (total + 127) / 128);
-    const int asz = (int)(L.ra1 * L.n * L.m * L.ra2);
-    size_t sm = asz <= 12288 ? (size_t)asz * sizeof(float) : 0;
-    tc::core_kernel<<<blocks, 128, sm, s>>>(op->T1, op->ldT1, op->A, (int)L.rx1, (int)L.m,
-                                            (int)L.n, (int)L.ra1, (int)L.ra2, (int)L.ry2, nvec,
-                                            tc::TM, T2.ktiles, T2.hi, T2.lo);
-    TTG_CHECK_LAUNCH();
-  }
-  // GEMM3 -> y: row (i,c2,v) of Y^T goes to y[v*ysize + ry1*(i + n*c2) + c1]
-  tc::Tiled T2a = op->T2;
-  T2a.rtiles = ceil_div(M3, tc::TM);
-  tc::gemm_launch<double>(T2a, op->P1, M3, N3, y, L.n * L.ry2, L.ysize(), L.ry1, op->err, s);
+  core_apply(op, nvec, s);
+  // GEMM3 -> y: C[c1, col] with col = (i,c2,v) goes to y[c1 + ry1 * col]
+  tc::Tiled T2b = op->T2;
+  T2b.rtiles = ceil_div(N3, T2b.R);
+  tc::gemm_launch<double>(op->P1, T2b, M3, N3, y, 1ll << 40, 0, 1, L.ry1, op->err, s);
 }
 
 // Davidson matvec factory for the chosen method (host-side SplitOp header is
