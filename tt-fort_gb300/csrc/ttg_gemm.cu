@@ -210,15 +210,20 @@ void launch(Args<T> a, int nbatch, cudaStream_t s) {
     return;
   }
   if (a.splitk < 1) a.splitk = 1;
-  if (a.splitk == 1 && a.K >= 512) {
-    // FP64 runs at a few GFLOP/s per SM on GB300: when the output tiles do not
-    // cover the SMs, split K so that about two CTAs per SM are busy
-    int bm = a.N <= 16 ? 128 : (a.M <= 16 ? 16 : (sizeof(T) == 8 ? 64 : 32));
-    int bn = a.N <= 16 ? 16 : (a.M <= 16 ? 128 : (sizeof(T) == 8 ? 64 : 32));
+  // FP64 runs at about two FMAs per clock per SM on GB300, so a product is
+  // only fast when its CTAs cover every SM: real products whose 64 x 64 tiles
+  // give fewer than two CTAs per SM use 32 x 32 tiles, and products that still
+  // leave SMs idle split K (atomic accumulation) until about two CTAs per SM
+  // are busy.
+  const bool small_tiles = sizeof(T) == 8 && a.N > 16 && a.M > 16 &&
+                           (i64)ceil_div(a.M, 64) * ceil_div(a.N, 64) * nbatch < 2 * 152;
+  if (a.splitk == 1 && a.K >= 128) {
+    int bm = a.N <= 16 ? 128 : (a.M <= 16 ? 16 : ((sizeof(T) == 8 && !small_tiles) ? 64 : 32));
+    int bn = a.N <= 16 ? 16 : (a.M <= 16 ? 128 : ((sizeof(T) == 8 && !small_tiles) ? 64 : 32));
     i64 ctas = (i64)ceil_div(a.M, bm) * ceil_div(a.N, bn) * nbatch;
     if (ctas < 152) {
       i64 want = (304 + ctas - 1) / ctas;
-      a.splitk = (int)std::max<i64>(1, std::min<i64>(want, a.K / 256));
+      a.splitk = (int)std::max<i64>(1, std::min<i64>(want, a.K / 64));
     }
   }
   a.kchunk = ceil_div(ceil_div(a.K, a.splitk), BK) * BK;
@@ -242,6 +247,14 @@ void launch(Args<T> a, int nbatch, cudaStream_t s) {
     gemm_kernel<T, BM, BN, 2, 4><<<grid, NT, 0, s>>>(a);
   } else {
     if constexpr (sizeof(T) == 8) {
+      if (small_tiles) {
+        constexpr int BM = 32, BN = 32;
+        dim3 grid(ceil_div(a.M, BM), ceil_div(a.N, BN), nbatch * a.splitk);
+        TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
+        gemm_kernel<T, BM, BN, 2, 2><<<grid, NT, 0, s>>>(a);
+        TTG_CHECK_LAUNCH();
+        return;
+      }
       constexpr int BM = 64, BN = 64;
       dim3 grid(ceil_div(a.M, BM), ceil_div(a.N, BN), nbatch * a.splitk);
       TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
