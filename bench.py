@@ -120,6 +120,14 @@ def fp64_peak_tflops(torch):
     return 2 * 4096 ** 3 / best / 1e12
 
 
+# DRAM bytes (read + write) of one split block matvec at r=64, n=2, ra=5, 5
+# vectors: the sum over its four launches (split X, GEMM1, CORE, GEMM3) in one
+# ncu capture (profiles/split_matvec_r64_b5_traffic.md), cold L2 per launch
+SPLIT_MV_TRAFFIC = 339200 + 270592 + 843008 + 1008640
+SPLIT_MV_TRAFFIC_NOTE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum summed over the four "
+                         "launches of one apply, cold L2 (profiles/split_matvec_r64_b5_traffic.md)")
+
+
 def matvec_roofline(torch, ctx, split=False, r=RMAX, nvec=B):
     """Local matvec through a prepared operator (the form the solver calls)
     at the workload's largest local problem (r=64, n=2, ra=5, block of B
@@ -288,7 +296,9 @@ def main():
             "roofline": {"kernel": f"local matvec bfun3 ({'BF16x3 tcgen05' if split else 'FP64'}, "
                                    f"r=64, n=2, ra=5, block 5)",
                          "bound": bound, "achieved": ach, "peak": peak, "unit": unit,
-                         "frac": ach / peak, "traffic": None, "peak_source": peak_note,
+                         "frac": ach / peak, "traffic": SPLIT_MV_TRAFFIC if split else None,
+                         "traffic_source": (SPLIT_MV_TRAFFIC_NOTE if split else None),
+                         "peak_source": peak_note,
                          "launch_us": dt * 1e6, "flops_per_launch": fl, "large_local": big},
             "clocks": clk.summary(), "cpu_baseline": cpu, "plain": plain,
             "solve": {"lambda": lam.tolist(), "matvecs": st["matvecs"], "sweeps": st["sweeps"],
