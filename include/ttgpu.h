@@ -159,6 +159,38 @@ ttg_int ttg_my_chop3(ttg_int n, const double* s, double eps);
 int ttg_dmaxvol(ttg_ctx* ctx, ttg_int n, ttg_int r, const double* A, ttg_int* p, double* Z,
                 double tol, ttg_int maxiters);
 
+/* ------------------------------------------- learned preconditioner (new) */
+/* No counterpart in the reference: PRIMME's applyPreconditioner hook is left
+ * unset by tt_eigb (primme/primme.h:144-145, tt_eigb.f90:252-283).  A ReLU MLP
+ * (3 features -> depth x width -> 1, FP32) corrects the classical diagonal
+ * Davidson preconditioner of the plain method's local solves; it is trained
+ * on local problems that the sweeps record.  Parameters are one flat float
+ * array, layer by layer: W_l (in x out, row-major) then b_l. */
+typedef struct ttg_mlp ttg_mlp;
+int ttg_mlp_create(ttg_ctx* ctx, ttg_int width, ttg_int depth, ttg_int seed, ttg_mlp** out);
+int ttg_mlp_destroy(ttg_mlp* mlp);
+ttg_int ttg_mlp_nparams(const ttg_mlp* mlp);
+int ttg_mlp_get_params(ttg_mlp* mlp, float* host, ttg_int n);
+int ttg_mlp_set_params(ttg_mlp* mlp, const float* host, ttg_int n);
+int ttg_mlp_get_grads(ttg_mlp* mlp, float* host, ttg_int n);
+/* h (P, device) = network(F (P x 3 row-major, device)) */
+int ttg_mlp_forward(ttg_mlp* mlp, ttg_int P, const float* F, float* h);
+/* loss and parameter gradient (kept in the network) of one recorded local
+ * problem, all device arrays: D (N) operator diagonal, theta (B), X (N x B)
+ * start Ritz block, R (N x B) its residuals, V (N x B) ideal corrections */
+int ttg_mlp_loss_grad(ttg_mlp* mlp, ttg_int N, ttg_int B, const double* D, const double* theta,
+                      const double* X, const double* R, const double* V, double* loss);
+int ttg_mlp_adam_step(ttg_mlp* mlp, double lr);
+/* mode bit 0: precondition the plain method's Davidson expansions with mlp;
+ * bit 1: record every iterative local problem of the plain method */
+int ttg_set_learned(ttg_ctx* ctx, ttg_mlp* mlp, int mode);
+int ttg_record_count(const ttg_ctx* ctx, ttg_int* nprob, ttg_int* npoints);
+int ttg_record_clear(ttg_ctx* ctx);
+/* Adam over the problems recorded in rec; mean loss before and after (the
+ * parameters before training are kept when the loss did not decrease) */
+int ttg_mlp_train_recorded(ttg_mlp* mlp, const ttg_ctx* rec, ttg_int steps, double lr,
+                           ttg_int seed, double* loss_first, double* loss_last);
+
 /* ---------------------------------------------------------- drivers (host) */
 /* Block eigensolver, tt_eigb tt_eigb.f90:110-436.  ry (d+1) is updated in
  * place, ry[d] = B on input and output; lambda receives B eigenvalues; the

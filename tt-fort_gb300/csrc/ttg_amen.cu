@@ -180,7 +180,7 @@ static inline double sm_uniform(unsigned long long k) {
   z = z ^ (z >> 31);
   return ((double)(z >> 11) + 1.0) * 0x1.0p-53;
 }
-static void sm_normals(unsigned long long seed, i64 count, double* out) {
+void sm_normals(unsigned long long seed, i64 count, double* out) {
   for (i64 i = 0; i < count; ++i) {
     const double u1 = sm_uniform(seed * 1000003ull + 2 * (unsigned long long)i + 1);
     const double u2 = sm_uniform(seed * 1000003ull + 2 * (unsigned long long)i + 2);

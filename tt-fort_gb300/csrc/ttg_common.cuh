@@ -69,6 +69,20 @@ struct Workspace {
 
 }  // namespace ttg
 
+struct ttg_mlp;   // learned preconditioner network (ttg_learned.cu)
+
+namespace ttg {
+// one local problem recorded for training the learned preconditioner: the
+// start Ritz block X (N x B) with values theta and residuals R, the diagonal
+// D of the local operator, and V = the converged block rotated onto X,
+// minus X, projected off span(X)
+struct LearnedRecord {
+  i64 N = 0;
+  int B = 0;
+  std::vector<double> D, theta, X, R, V;
+};
+}  // namespace ttg
+
 // The opaque context handed across the C-ABI.  One context per host thread;
 // it replaces the reference's module-level globals (tt_eigb.f90:1-50,
 // tt_ksl.f90:1-166) and module result arrays (result_core, zresult_core).
@@ -88,6 +102,11 @@ struct ttg_ctx {
   long long stat_sweeps = 0;
   long long stat_launches = 0;
   double stat_res = 0.0;
+  // learned preconditioner: mode bit 0 = precondition the plain Davidson
+  // expansions, bit 1 = record training problems from the sweeps
+  ttg_mlp* learned = nullptr;
+  int learned_mode = 0;
+  std::vector<ttg::LearnedRecord> records;
 };
 
 namespace ttg {
@@ -110,6 +129,22 @@ struct GemmF64 {
   int splitk = 1;   // > 1: K split over CTAs, C accumulated with FP64 atomics
 };
 void gemm_f64(const GemmF64& g, cudaStream_t s);
+
+// standard normals from the splitmix64/Box-Muller stream shared with the oracle
+void sm_normals(unsigned long long seed, i64 count, double* out);
+
+// FP32 variant (learned preconditioner network)
+struct GemmF32 {
+  int M = 0, N = 0, K = 0;
+  const float* A = nullptr; i64 sAm = 0, sAk = 0;
+  const float* B = nullptr; i64 sBk = 0, sBn = 0;
+  float* C = nullptr;       i64 sCm = 0, sCn = 0;
+  float alpha = 1.f, beta = 0.f;
+  int nb1 = 1, nb2 = 1;
+  i64 bA1 = 0, bA2 = 0, bB1 = 0, bB2 = 0, bC1 = 0, bC2 = 0;
+  int splitk = 1;
+};
+void gemm_f32(const GemmF32& g, cudaStream_t s);
 
 // complex128 variant (KSL path); same strides in units of complex elements.
 struct GemmZ {

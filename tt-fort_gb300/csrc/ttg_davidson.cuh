@@ -72,4 +72,13 @@ void residual_cols(i64 N, int nb, const double* AX, const double* X, const doubl
 void gather_cols(i64 N, int t, const int* idx, const double* src, double* dst, cudaStream_t s);
 int splitk_for(i64 K);
 
+// learned preconditioner (ttg_learned.cu): the Davidson expansion hook of one
+// local problem (D receives the operator's diagonal, N doubles), and the
+// recorder of training problems
+PrecFn make_learned_prec(ttg_mlp* M, const LocalDims& L, const double* phi1, const double* A,
+                         const double* phi2, double* D, cudaStream_t s);
+void learned_record(ttg_ctx* ctx, const LocalDims& L, const double* phi1, const double* A,
+                    const double* phi2, const double* X0, const double* Xs, int B,
+                    const MatvecFn& mv, cudaStream_t s);
+
 }  // namespace ttg

@@ -173,6 +173,9 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
   total += 2 * al(sizeof(double) * dense_max * dense_max) + al(sizeof(double) * 512) + al(256);
   total += al(Davidson::bytes(Nmax, B, maxb_cap));
   if (P.method == TTG_METHOD_SPLIT) total += al(chosen_bytes(Nmax, B));
+  const bool learned_prec = P.method == TTG_METHOD_PLAIN && ctx->learned && (ctx->learned_mode & 1);
+  const bool record = P.method == TTG_METHOD_PLAIN && (ctx->learned_mode & 2);
+  if (learned_prec) total += al(sizeof(double) * Nmax);
   total += 1 << 16;
   DevBlock mem;
   mem.alloc(total);
@@ -196,6 +199,7 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
   int* dst = mem.take<int>(64);
   void* dav_mem = mem.take<char>(Davidson::bytes(Nmax, B, maxb_cap));
   void* jd_mem = P.method == TTG_METHOD_SPLIT ? (void*)mem.take<char>(chosen_bytes(Nmax, B)) : nullptr;
+  double* ldiag = learned_prec ? mem.take<double>(Nmax) : nullptr;
   PinnedBuf hb(4096 + rmaxsvd * 2);
   double* hbuf = hb.p;
 
@@ -291,8 +295,12 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
         const int keep = std::min(B + std::max(1, B / 2), std::max(maxb - B, 1));
         Davidson dav(N, B, maxb, keep, dav_mem, hbuf, s);
         if (pt.on) { pt.dav.s = s; dav.timer = &pt.dav; }
+        // learned preconditioner (no reference counterpart): the Davidson
+        // expansions use it; the FP64 residual test still judges convergence
+        if (learned_prec) dav.prec = make_learned_prec(ctx->learned, L, p1, Ai, p2, ldiag, s);
         st = dav.solve(mv, cr[i], eps2 / resid_damp, max_matvecs, curcr, lam.data());
         fp64_mv += st.matvecs;
+        if (record) learned_record(ctx, L, p1, Ai, p2, cr[i], curcr, B, mv, s);
       }
       nmv = st.matvecs;
       res = st.res;

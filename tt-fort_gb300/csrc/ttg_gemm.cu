@@ -17,6 +17,15 @@ namespace ttg {
 namespace {
 
 template <class T> struct Ops;
+template <> struct Ops<float> {
+  static __device__ __forceinline__ float zero() { return 0.f; }
+  static __device__ __forceinline__ float fma(float a, float b, float c) { return fmaf(a, b, c); }
+  static __device__ __forceinline__ float conj(float a) { return a; }
+  static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+  static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+  static __device__ __forceinline__ bool is_zero(float a) { return a == 0.f; }
+  static __device__ __forceinline__ void atomic_add(float* p, float v) { atomicAdd(p, v); }
+};
 template <> struct Ops<double> {
   static __device__ __forceinline__ double zero() { return 0.0; }
   static __device__ __forceinline__ double fma(double a, double b, double c) { return ::fma(a, b, c); }
@@ -215,11 +224,11 @@ void launch(Args<T> a, int nbatch, cudaStream_t s) {
   // give fewer than two CTAs per SM use 32 x 32 tiles, and products that still
   // leave SMs idle split K (atomic accumulation) until about two CTAs per SM
   // are busy.
-  const bool small_tiles = sizeof(T) == 8 && a.N > 16 && a.M > 16 &&
+  const bool small_tiles = sizeof(T) <= 8 && a.N > 16 && a.M > 16 &&
                            (i64)ceil_div(a.M, 64) * ceil_div(a.N, 64) * nbatch < 2 * 152;
   if (a.splitk == 1 && a.K >= 128) {
-    int bm = a.N <= 16 ? 128 : (a.M <= 16 ? 16 : ((sizeof(T) == 8 && !small_tiles) ? 64 : 32));
-    int bn = a.N <= 16 ? 16 : (a.M <= 16 ? 128 : ((sizeof(T) == 8 && !small_tiles) ? 64 : 32));
+    int bm = a.N <= 16 ? 128 : (a.M <= 16 ? 16 : ((sizeof(T) <= 8 && !small_tiles) ? 64 : 32));
+    int bn = a.N <= 16 ? 16 : (a.M <= 16 ? 128 : ((sizeof(T) <= 8 && !small_tiles) ? 64 : 32));
     i64 ctas = (i64)ceil_div(a.M, bm) * ceil_div(a.N, bn) * nbatch;
     if (ctas < 152) {
       i64 want = (304 + ctas - 1) / ctas;
@@ -246,7 +255,7 @@ void launch(Args<T> a, int nbatch, cudaStream_t s) {
     TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
     gemm_kernel<T, BM, BN, 2, 4><<<grid, NT, 0, s>>>(a);
   } else {
-    if constexpr (sizeof(T) == 8) {
+    if constexpr (sizeof(T) <= 8) {
       if (small_tiles) {
         constexpr int BM = 32, BN = 32;
         dim3 grid(ceil_div(a.M, BM), ceil_div(a.N, BN), nbatch * a.splitk);
@@ -277,6 +286,13 @@ void gemm_f64(const GemmF64& g, cudaStream_t s) {
                  g.alpha, g.beta, g.nb1, g.bA1, g.bA2, g.bB1, g.bB2, g.bC1, g.bC2,
                  g.splitk, 0, false, false};
   launch<double>(a, g.nb1 * g.nb2, s);
+}
+
+void gemm_f32(const GemmF32& g, cudaStream_t s) {
+  Args<float> a{g.M, g.N, g.K, g.A, g.sAm, g.sAk, g.B, g.sBk, g.sBn, g.C, g.sCm, g.sCn,
+                g.alpha, g.beta, g.nb1, g.bA1, g.bA2, g.bB1, g.bB2, g.bC1, g.bC2,
+                g.splitk, 0, false, false};
+  launch<float>(a, g.nb1 * g.nb2, s);
 }
 
 void gemm_z(const GemmZ& g, cudaStream_t s) {

@@ -53,6 +53,8 @@ def lib():
         L.ttg_my_chop3.restype = _i64
         L.ttg_my_chop3.argtypes = [_i64, C.c_void_p, C.c_double]
         L.ttg_launch_count.restype = _i64
+        L.ttg_mlp_nparams.restype = _i64
+        L.ttg_mlp_nparams.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -66,6 +68,10 @@ EXPORTED = [
     "ttg_my_chop3", "ttg_dmaxvol", "ttg_eigb", "ttg_ksl_z", "ttg_amen_solve",
     "ttg_result_size", "ttg_result_copy", "ttg_zresult_copy", "ttg_free_result", "ttg_stats",
     "ttg_launch_count", "ttg_localop_create", "ttg_localop_apply", "ttg_localop_destroy",
+    "ttg_mlp_create", "ttg_mlp_destroy", "ttg_mlp_nparams", "ttg_mlp_get_params",
+    "ttg_mlp_set_params", "ttg_mlp_get_grads", "ttg_mlp_forward", "ttg_mlp_loss_grad",
+    "ttg_mlp_adam_step", "ttg_set_learned", "ttg_record_count", "ttg_record_clear",
+    "ttg_mlp_train_recorded",
 ]
 
 
@@ -341,3 +347,84 @@ class LocalOp:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------------- learned preconditioner
+class LearnedPrec:
+    """The learned preconditioner network of the plain local eigensolver (no
+    counterpart in the reference, whose PRIMME preconditioner hook is unset,
+    tt_eigb.f90:252-283).  ``widths`` = [3] + [width] * depth + [1]."""
+
+    def __init__(self, width=512, depth=3, seed=0, ctx=None):
+        self.ctx = ctx or default_context()
+        self.width, self.depth = width, depth
+        self._h = C.c_void_p()
+        self.ctx.check(lib().ttg_mlp_create(self.ctx.handle, _i64(width), _i64(depth), _i64(seed),
+                                            C.byref(self._h)))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def nparams(self):
+        return int(lib().ttg_mlp_nparams(self._h))
+
+    def get_params(self):
+        out = np.empty(self.nparams(), dtype=np.float32)
+        self.ctx.check(lib().ttg_mlp_get_params(self._h, _p(out), _i64(len(out))))
+        return out
+
+    def set_params(self, flat):
+        flat = np.ascontiguousarray(flat, dtype=np.float32)
+        self.ctx.check(lib().ttg_mlp_set_params(self._h, _p(flat), _i64(len(flat))))
+
+    def get_grads(self):
+        out = np.empty(self.nparams(), dtype=np.float32)
+        self.ctx.check(lib().ttg_mlp_get_grads(self._h, _p(out), _i64(len(out))))
+        return out
+
+    def forward(self, P, F, h):
+        self.ctx.bind_torch_stream()
+        self.ctx.check(lib().ttg_mlp_forward(self._h, _i64(P), _dev(F), _dev(h)))
+
+    def loss_grad(self, N, B, D, theta, X, R, V):
+        self.ctx.bind_torch_stream()
+        loss = C.c_double()
+        self.ctx.check(lib().ttg_mlp_loss_grad(self._h, _i64(N), _i64(B), _dev(D), _dev(theta),
+                                               _dev(X), _dev(R), _dev(V), C.byref(loss)))
+        return loss.value
+
+    def adam_step(self, lr):
+        self.ctx.check(lib().ttg_mlp_adam_step(self._h, C.c_double(lr)))
+
+    def train_recorded(self, rec_ctx, steps, lr=1e-4, seed=0):
+        l0, l1 = C.c_double(), C.c_double()
+        self.ctx.check(lib().ttg_mlp_train_recorded(self._h, rec_ctx.handle, _i64(steps),
+                                                    C.c_double(lr), _i64(seed), C.byref(l0),
+                                                    C.byref(l1)))
+        return l0.value, l1.value
+
+    def close(self):
+        if self._h:
+            lib().ttg_mlp_destroy(self._h)
+            self._h = C.c_void_p()
+
+
+def set_learned(mlp, mode, ctx=None):
+    """mode bit 0: precondition the plain method's Davidson expansions with
+    ``mlp``; bit 1: record the plain method's iterative local problems."""
+    ctx = ctx or default_context()
+    ctx.check(lib().ttg_set_learned(ctx.handle, mlp.handle if mlp is not None else C.c_void_p(),
+                                    C.c_int(mode)))
+
+
+def record_count(ctx=None):
+    ctx = ctx or default_context()
+    a, b = _i64(), _i64()
+    ctx.check(lib().ttg_record_count(ctx.handle, C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
+def record_clear(ctx=None):
+    ctx = ctx or default_context()
+    ctx.check(lib().ttg_record_clear(ctx.handle))
