@@ -209,11 +209,23 @@ int ttg_ksl_z(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m, const
               const double* crA, const double* crY0, ttg_int* ry, double tau, ttg_int rmax,
               int verb, int typ, int order, int method, ttg_int nsteps);
 /* AMEn linear solve A x = y, tt_amen_solve tt_adapt_als.f90:513-1132
- * (argument order follows it; rx updated in place). */
+ * (argument order follows it; rx updated in place).  kickrank 4, nswp 20,
+ * prec 'n', nrestart 40, niters 2 are the reference's defaults (pass them,
+ * or values <= 0 / 0 for the defaults of nswp, nrestart, niters); only the
+ * 'n' preconditioner is built (others return TTG_ERR_UNSUPPORTED).  rmax
+ * caps the kept ranks (<= 0: no cap, as in the reference). */
 int ttg_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
                    const ttg_int* ry, const ttg_int* ra, const double* crA, const double* crY,
-                   const double* crX0, ttg_int* rx, double eps, ttg_int rmax, ttg_int kickrank,
-                   ttg_int nswp, int verb, int method);
+                   const double* crX0, ttg_int* rx, double eps, ttg_int kickrank, ttg_int nswp,
+                   int verb, char prec, ttg_int nrestart, ttg_int niters, ttg_int rmax,
+                   int method);
+/* AMEn of ttamen.f90 (dtt_amen_solve, ttamen.f90:29-252) with the packed
+ * cores of the arguments above in place of the dtt type; rmax caps the
+ * ranks (<= 0: no cap). */
+int ttg_dtt_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
+                       const ttg_int* ry, const ttg_int* ra, const double* crA,
+                       const double* crY, const double* crX0, ttg_int* rx, double eps,
+                       ttg_int rmax, ttg_int kickrank, ttg_int nswp, int verb, int method);
 /* Results of the last driver call. */
 int ttg_result_size(const ttg_ctx* ctx, ttg_int* nelem);
 int ttg_result_copy(const ttg_ctx* ctx, double* out, ttg_int nelem);   /* real */

@@ -37,7 +37,7 @@ def test_amen_dense_check(ctx, d, n, ryr, rxr):
     nn, mm, ra, crA = amen_operator(d=d, n=n)
     _, ry, y = random_tt(d, n, ryr, seed=3)
     _, rx, x0 = random_tt(d, n, rxr, seed=7)
-    cores, rx1 = ttgpu.tt_amen_solve(d, nn, mm, ry, ra, crA, y, x0, rx, tol, ctx=ctx)
+    cores, rx1 = ttgpu.dtt_amen_solve(d, nn, mm, ry, ra, crA, y, x0, rx, tol, ctx=ctx)
     A = tt_matrix_full(d, nn, ra, crA)
     yf = tt_full(d, nn, ry, y)
     xf = tt_full(d, nn, rx1, cores)
@@ -57,7 +57,7 @@ def test_amen_workload_family(ctx):
     nn, mm, ra, crA = amen_operator(d=d, n=n)
     _, ry, y = random_tt(d, n, 4, seed=3)
     _, rx, x0 = random_tt(d, n, 2, seed=5)
-    cores, rx1 = ttgpu.tt_amen_solve(d, nn, mm, ry, ra, crA, y, x0, rx, tol, nswp=nswp, ctx=ctx)
+    cores, rx1 = ttgpu.dtt_amen_solve(d, nn, mm, ry, ra, crA, y, x0, rx, tol, nswp=nswp, ctx=ctx)
     st = ctx.stats()
     ref = oracle_amen(d, nn, ra, crA, ry, y, rx, x0, tol, nswp=nswp)
     assert rx1 == ref["rx"]

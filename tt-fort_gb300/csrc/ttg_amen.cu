@@ -222,6 +222,95 @@ struct Arena {
 
 inline size_t al8(size_t count) { return (count * sizeof(double) + 255) & ~size_t(255); }
 
+// device buffers of one GMRES: V (N x (nr+1)), w (N), gm (4096 doubles:
+// Hessenberg columns, rotations, rhs, Ritz coefficients, R), red (64), h
+// (pinned host, >= 4 doubles)
+struct GmresBufs {
+  double *V, *w, *gm, *red, *h;
+};
+
+// GMRES(nr) x iters for L x = b (x0 = 0) with Arnoldi by classical
+// Gram-Schmidt applied twice; stops when |residual| / |b| < tol (the
+// Householder GMRES of the reference minimises the same residual over the
+// same Krylov space, ttlocsolve.f90:509-682, tt_linalg.f90:651-845).
+template <class MV>
+void gmres_cgs2(const MV& mv, i64 N, const double* b, double* x, double tol, int nr, int iters,
+                const GmresBufs& G, cudaStream_t s) {
+  double* H = G.gm;                    // Hessenberg column (first pass)
+  double* H2 = G.gm + 64;              // second Gram-Schmidt pass
+  double* cs = G.gm + 128;
+  double* sn = G.gm + 192;
+  double* g = G.gm + 256;
+  double* y = G.gm + 320;
+  double* hres = G.gm + 384;
+  double* Rm = G.gm + 448;             // (nr+1) x nr, nr <= 60
+  const int ldr = nr + 1;
+  double* V = G.V;
+  double* red = G.red;
+  double* h = G.h;
+  auto sync = [&]() { TTG_CUDA(cudaStreamSynchronize(s)); };
+  TTG_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * N, s));
+  double nrmb = -1.0, curres = 1.0;
+  for (int it = 0; it < iters; ++it) {
+    // w = b - L x
+    mv(x, G.w, 1);
+    sub_kernel<<<eb(N), 256, 0, s>>>(N, b, G.w, G.w);
+    TTG_CHECK_LAUNCH();
+    TTG_CUDA(cudaMemsetAsync(red, 0, sizeof(double), s));
+    {
+      int bx = (int)std::max<i64>(1, std::min<i64>(256, (N + 2047) / 2048));
+      sqnorm_cols_kernel<<<dim3(bx, 1), 256, 0, s>>>(N, G.w, N, red);
+      TTG_CHECK_LAUNCH();
+    }
+    TTG_CUDA(cudaMemcpyAsync(h, red, sizeof(double), cudaMemcpyDeviceToHost, s));
+    sync();
+    const double beta = std::sqrt(h[0]);
+    if (it == 0) nrmb = beta;
+    if (beta == 0.0) break;
+    TTG_CUDA(cudaMemcpyAsync(V, G.w, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+    h[1] = 1.0 / beta;
+    TTG_CUDA(cudaMemcpyAsync(red + 8, h + 1, sizeof(double), cudaMemcpyHostToDevice, s));
+    scal_kernel<<<eb(N), 256, 0, s>>>(N, red + 8, 0, V);
+    TTG_CHECK_LAUNCH();
+    TTG_CUDA(cudaMemsetAsync(g, 0, sizeof(double) * 64, s));
+    h[2] = beta;
+    TTG_CUDA(cudaMemcpyAsync(g, h + 2, sizeof(double), cudaMemcpyHostToDevice, s));
+    int jdone = 0;
+    for (int j = 0; j < nr; ++j) {
+      double* vj = V + N * j;
+      double* wv = V + N * (j + 1);
+      mv(vj, wv, 1);
+      // CGS2 against V[:, 0..j]
+      gemm_tn_small(j + 1, 1, N, V, N, wv, N, H, j + 2, 1.0, 0.0, s);
+      gemm_nn_small(N, 1, j + 1, V, N, H, j + 2, wv, N, -1.0, 1.0, s);
+      gemm_tn_small(j + 1, 1, N, V, N, wv, N, H2, j + 2, 1.0, 0.0, s);
+      gemm_nn_small(N, 1, j + 1, V, N, H2, j + 2, wv, N, -1.0, 1.0, s);
+      axpy_kernel<<<1, 64, 0, s>>>(j + 1, 1.0, H2, H);
+      TTG_CHECK_LAUNCH();
+      TTG_CUDA(cudaMemsetAsync(red, 0, sizeof(double), s));
+      int bx = (int)std::max<i64>(1, std::min<i64>(256, (N + 2047) / 2048));
+      sqnorm_cols_kernel<<<dim3(bx, 1), 256, 0, s>>>(N, wv, N, red);
+      TTG_CHECK_LAUNCH();
+      sqrt_kernel<<<1, 32, 0, s>>>(1, red);
+      TTG_CHECK_LAUNCH();
+      TTG_CUDA(cudaMemcpyAsync(H + j + 1, red, sizeof(double), cudaMemcpyDeviceToDevice, s));
+      scal_kernel<<<eb(N), 256, 0, s>>>(N, red, 1, wv);
+      TTG_CHECK_LAUNCH();
+      givens_kernel<<<1, 1, 0, s>>>(j, H, cs, sn, g, Rm, ldr, hres);
+      TTG_CHECK_LAUNCH();
+      TTG_CUDA(cudaMemcpyAsync(h, hres, sizeof(double), cudaMemcpyDeviceToHost, s));
+      sync();
+      jdone = j + 1;
+      curres = h[0] / nrmb;
+      if (curres < tol) break;
+    }
+    trsv_kernel<<<1, 1, 0, s>>>(jdone, Rm, ldr, g, y);
+    TTG_CHECK_LAUNCH();
+    gemm_nn_small(N, 1, jdone, V, N, y, jdone, x, N, 1.0, 1.0, s);
+    if (curres < tol) break;
+  }
+}
+
 }  // namespace
 
 struct AmenParams {
@@ -356,74 +445,15 @@ void AmenSolver::project_y(const double* pl, const double* pr, i64 rl, i64 rr, i
 }
 
 
-// GMRES(local_restart) x local_iters for L x = b (x0 = 0), Arnoldi with
-// classical Gram-Schmidt twice, relative tolerance against ||b||.
+// GMRES(local_restart) x local_iters for L x = b (x0 = 0), relative tolerance
+// against ||b||.
 void AmenSolver::gmres(const LocalDims& L, int k, const double* b, double* x, double tol) {
   const i64 N = L.xsize();
   const int nr = (int)std::min<i64>(std::min<i64>(N, P_.local_restart), 60);
   const double* p1 = pxax_[k];
   const double* p2 = pxax_[k + 1];
-  double* H = gm_;                     // Hessenberg column (first pass)
-  double* H2 = gm_ + 64;               // second Gram-Schmidt pass
-  double* cs = gm_ + 128;
-  double* sn = gm_ + 192;
-  double* g = gm_ + 256;
-  double* y = gm_ + 320;
-  double* hres = gm_ + 384;
-  double* Rm = gm_ + 448;              // (nr+1) x nr, nr <= 60
-  const int ldr = nr + 1;
-  TTG_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * N, s_));
-  double nrmb = -1.0, curres = 1.0;
-  for (int it = 0; it < P_.local_iters; ++it) {
-    // w = b - L x
-    local_mv(L, p1, p2, k, x, w_, 1);
-    sub_kernel<<<eb(N), 256, 0, s_>>>(N, b, w_, w_);
-    TTG_CHECK_LAUNCH();
-    const double beta = norm2(w_, N);
-    if (it == 0) nrmb = beta;
-    if (beta == 0.0) break;
-    TTG_CUDA(cudaMemcpyAsync(V_, w_, sizeof(double) * N, cudaMemcpyDeviceToDevice, s_));
-    h_[1] = 1.0 / beta;
-    TTG_CUDA(cudaMemcpyAsync(red_ + 8, h_ + 1, sizeof(double), cudaMemcpyHostToDevice, s_));
-    scal_kernel<<<eb(N), 256, 0, s_>>>(N, red_ + 8, 0, V_);
-    TTG_CHECK_LAUNCH();
-    TTG_CUDA(cudaMemsetAsync(g, 0, sizeof(double) * 64, s_));
-    h_[2] = beta;
-    TTG_CUDA(cudaMemcpyAsync(g, h_ + 2, sizeof(double), cudaMemcpyHostToDevice, s_));
-    int jdone = 0;
-    for (int j = 0; j < nr; ++j) {
-      double* vj = V_ + N * j;
-      double* wv = V_ + N * (j + 1);
-      local_mv(L, p1, p2, k, vj, wv, 1);
-      // CGS2 against V[:, 0..j]
-      gemm_tn_small(j + 1, 1, N, V_, N, wv, N, H, j + 2, 1.0, 0.0, s_);
-      gemm_nn_small(N, 1, j + 1, V_, N, H, j + 2, wv, N, -1.0, 1.0, s_);
-      gemm_tn_small(j + 1, 1, N, V_, N, wv, N, H2, j + 2, 1.0, 0.0, s_);
-      gemm_nn_small(N, 1, j + 1, V_, N, H2, j + 2, wv, N, -1.0, 1.0, s_);
-      axpy_kernel<<<1, 64, 0, s_>>>(j + 1, 1.0, H2, H);
-      TTG_CHECK_LAUNCH();
-      TTG_CUDA(cudaMemsetAsync(red_, 0, sizeof(double), s_));
-      int bx = (int)std::max<i64>(1, std::min<i64>(256, (N + 2047) / 2048));
-      sqnorm_cols_kernel<<<dim3(bx, 1), 256, 0, s_>>>(N, wv, N, red_);
-      TTG_CHECK_LAUNCH();
-      sqrt_kernel<<<1, 32, 0, s_>>>(1, red_);
-      TTG_CHECK_LAUNCH();
-      TTG_CUDA(cudaMemcpyAsync(H + j + 1, red_, sizeof(double), cudaMemcpyDeviceToDevice, s_));
-      scal_kernel<<<eb(N), 256, 0, s_>>>(N, red_, 1, wv);
-      TTG_CHECK_LAUNCH();
-      givens_kernel<<<1, 1, 0, s_>>>(j, H, cs, sn, g, Rm, ldr, hres);
-      TTG_CHECK_LAUNCH();
-      TTG_CUDA(cudaMemcpyAsync(h_, hres, sizeof(double), cudaMemcpyDeviceToHost, s_));
-      sync();
-      jdone = j + 1;
-      curres = h_[0] / nrmb;
-      if (curres < tol) break;
-    }
-    trsv_kernel<<<1, 1, 0, s_>>>(jdone, Rm, ldr, g, y);
-    TTG_CHECK_LAUNCH();
-    gemm_nn_small(N, 1, jdone, V_, N, y, jdone, x, N, 1.0, 1.0, s_);
-    if (curres < tol) break;
-  }
+  auto mv = [&](const double* in, double* out, int nv) { local_mv(L, p1, p2, k, in, out, nv); };
+  gmres_cgs2(mv, N, b, x, tol, nr, P_.local_iters, GmresBufs{V_, w_, gm_, red_, h_}, s_);
 }
 
 // dtt_trunc dir=+1 with the residual criterion (ttnodeop.f90:227-302)
@@ -705,14 +735,575 @@ void AmenSolver::run(AmenOut& out) {
   out.matvecs = nmv_;
 }
 
+
+// ---------------------------------------------------------------------------
+// tt_amen_solve of tt_adapt_als.f90 (alternating half sweeps, Householder
+// GMRES correction, residual-based truncation from the top, kick by an
+// incremental Cholesky of [Y-projection, A-projection])
+// ---------------------------------------------------------------------------
+namespace {
+
+// B(n1, n3, n2, n4) = A(n1, n2, n3, n4)   (dperm1324, tt_linalg.f90:101-120)
+__global__ void perm1324_kernel(i64 n1, i64 n2, i64 n3, i64 n4, const double* __restrict__ A,
+                                double* __restrict__ B) {
+  const i64 tot = n1 * n2 * n3 * n4;
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x) {
+    const i64 i1 = e % n1, i2 = (e / n1) % n2, i3 = (e / (n1 * n2)) % n3, i4 = e / (n1 * n2 * n3);
+    B[i1 + n1 * (i3 + n3 * (i2 + n2 * i4))] = A[e];
+  }
+}
+// out ((m1 + m2) x nc) = [A (m1 x nc); B (m2 x nc)]   (drow_add, tt_linalg.f90:54-69)
+__global__ void concat_rows_kernel(i64 m1, i64 m2, i64 nc, const double* __restrict__ A,
+                                   const double* __restrict__ B, double* __restrict__ out) {
+  const i64 M = m1 + m2;
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < M * nc; e += (i64)gridDim.x * blockDim.x) {
+    const i64 r = e % M, c = e / M;
+    out[e] = r < m1 ? A[r + m1 * c] : B[(r - m1) + m2 * c];
+  }
+}
+// incremental Cholesky (duchol_fort) pieces; A(i, k) = dA[i * si + k * sk],
+// i < n rows, k < m columns
+__global__ void uchol_diag_kernel(i64 n, i64 m, const double* __restrict__ dA, i64 si, i64 sk,
+                                  double* __restrict__ dd) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (i64 k = 0; k < m; ++k) { const double v = dA[i * si + k * sk]; acc = fma(v, v, acc); }
+    dd[i] = acc;
+  }
+}
+// first index of the largest |dd| (idamax), one block
+__global__ void argmax_abs_kernel(i64 n, const double* __restrict__ dd, int* __restrict__ out) {
+  __shared__ double sv[32];
+  __shared__ int si[32];
+  double v = -1.0;
+  int idx = 0x7fffffff;
+  for (i64 i = threadIdx.x; i < n; i += blockDim.x) {
+    const double a = fabs(dd[i]);
+    if (a > v || (a == v && (int)i < idx)) { v = a; idx = (int)i; }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+    const int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+    if (v2 > v || (v2 == v && i2 < idx)) { v = v2; idx = i2; }
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { sv[w] = v; si[w] = idx; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double bv = -1.0;
+    int bi = 0x7fffffff;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q)
+      if (sv[q] > bv || (sv[q] == bv && si[q] < bi)) { bv = sv[q]; bi = si[q]; }
+    *out = bi;
+  }
+}
+// du[:, c] = A A(maxi, :)^T - sum_{j < c} lam_j du(maxi, j) du[:, j]
+__global__ void uchol_col_kernel(i64 n, i64 m, const double* __restrict__ dA, i64 si, i64 sk,
+                                 const int* __restrict__ maxi_p, int c, const double* __restrict__ lam,
+                                 double* __restrict__ du) {
+  const i64 mi = *maxi_p;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (i64 k = 0; k < m; ++k) acc = fma(dA[i * si + k * sk], dA[mi * si + k * sk], acc);
+    for (int j = 0; j < c; ++j) acc -= lam[j] * du[mi + n * j] * du[i + n * j];
+    du[i + n * c] = acc;
+  }
+}
+__global__ void uchol_pick_kernel(i64 n, const int* __restrict__ maxi_p, int c,
+                                  const double* __restrict__ du, double* __restrict__ out) {
+  *out = du[*maxi_p + n * c];
+}
+// du[:, c] /= sqrt(|piv|); dd -= du[:, c]^2
+__global__ void uchol_scale_kernel(i64 n, int c, const double* __restrict__ piv, double* __restrict__ du,
+                                   double* __restrict__ dd) {
+  const double inv = 1.0 / sqrt(fabs(*piv));
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+    const double v = du[i + n * c] * inv;
+    du[i + n * c] = v;
+    dd[i] -= v * v;
+  }
+}
+// dv (k x k) = dx dx^T + diag(lam), dx = R(:, k-1) (R k x k)
+__global__ void uchol_dv_kernel(int k, const double* __restrict__ R, const double* __restrict__ lam,
+                                double* __restrict__ dv) {
+  for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+    const int i = e % k, j = e / k;
+    dv[e] = R[i + k * (k - 1)] * R[j + k * (k - 1)] + (i == j ? lam[i] : 0.0);
+  }
+}
+
+}  // namespace
+
+struct AlsParams {
+  int d;
+  std::vector<i64> n, ra, ry, rx;
+  const double *crA, *crY, *crX0;
+  double eps;
+  i64 rmax;
+  int kick, nswp, nrestart, niters, verb;
+};
+
+class AlsSolver {
+ public:
+  AlsSolver(ttg_ctx* ctx, const AlsParams& P) : P_(P), s_(ctx->stream) {}
+  void run(AmenOut& out);
+
+ private:
+  AlsParams P_;
+  cudaStream_t s_;
+  Arena mem_;
+  std::vector<i64> n_, rx_, cap_;
+  std::vector<double*> x_, A_, Y_, phiA_, phiy_;
+  double *rhs_, *r0_, *sol_, *w_, *V_, *gm_, *red_, *kickY_, *kickB_, *tA_, *tB_, *tC_, *U_, *S_,
+      *Vt_, *svScr_, *cand_, *candY_, *Um_, *Rm_, *Rq_, *tau_, *tmp_, *scr_, *du_, *dd_, *small_;
+  int* ired_;
+  double* h_ = nullptr;
+  long long nmv_ = 0;
+  static constexpr int kBatch = 8;
+
+  void sync() { TTG_CUDA(cudaStreamSynchronize(s_)); }
+  LocalDims dims(int k) const {
+    return LocalDims{rx_[k], n_[k], rx_[k + 1], rx_[k], n_[k], rx_[k + 1], P_.ra[k], P_.ra[k + 1]};
+  }
+  void gemm(int M, int N, int K, const double* A, i64 sAm, i64 sAk, const double* B, i64 sBk,
+            i64 sBn, double* C, i64 sCm, i64 sCn, double alpha = 1.0, double beta = 0.0) {
+    GemmF64 g;
+    g.M = M; g.N = N; g.K = K;
+    g.A = A; g.sAm = sAm; g.sAk = sAk;
+    g.B = B; g.sBk = sBk; g.sBn = sBn;
+    g.C = C; g.sCm = sCm; g.sCn = sCn;
+    g.alpha = alpha; g.beta = beta;
+    gemm_f64(g, s_);
+  }
+  double norm2(const double* v, i64 n) {
+    TTG_CUDA(cudaMemsetAsync(red_, 0, sizeof(double), s_));
+    int bx = (int)std::max<i64>(1, std::min<i64>(256, (n + 2047) / 2048));
+    sqnorm_cols_kernel<<<dim3(bx, 1), 256, 0, s_>>>(n, v, n, red_);
+    TTG_CHECK_LAUNCH();
+    TTG_CUDA(cudaMemcpyAsync(h_, red_, sizeof(double), cudaMemcpyDeviceToHost, s_));
+    sync();
+    return std::sqrt(h_[0]);
+  }
+  void mv(int k, const double* x, double* y, int nv) {
+    bfun3_f64(dims(k), phiA_[k], A_[k], phiA_[k + 1], x, y, nv, scr_, s_);
+    nmv_ += nv;
+  }
+  void qr(i64 m, i64 c, double* A, double* R) { qr_householder((int)m, (int)c, A, R, tau_, s_); }
+  void upd_left(int i);
+  void upd_right(int i);
+  int scan(int i, int rmin, const double* L, i64 ldl, const double* Rr, i64 ldr, i64 rows, i64 cols,
+           const double* rhs, double nrhs, double res_new, double eps2);
+  int uchol(bool trans, i64 m, i64 n, const double* dA, int numvec, double* du);
+  void bfun3_left(int i, const double* x, double* y);
+  void bfun3_right(int i, const double* x, double* y);
+};
+
+void AlsSolver::upd_left(int i) {
+  phi_left_f64(dims(i), phiA_[i], A_[i], x_[i], x_[i], phiA_[i + 1], scr_, s_);
+  phi2_left_f64(P_.ry[i], P_.ry[i + 1], rx_[i], n_[i], rx_[i + 1], phiy_[i], Y_[i], x_[i],
+                phiy_[i + 1], scr_, s_);
+}
+
+void AlsSolver::upd_right(int i) {
+  phi_right_f64(dims(i), phiA_[i + 1], A_[i], x_[i], x_[i], phiA_[i], scr_, s_);
+  phi2_right_f64(P_.ry[i], P_.ry[i + 1], rx_[i], n_[i], rx_[i + 1], phiy_[i + 1], Y_[i], x_[i],
+                 phiy_[i], scr_, s_);
+}
+
+// Residual-based rank scan from the top (tt_adapt_als.f90:812-829, 917-934):
+// candidate rank c gives the core L[:, :c] R[:c, :] (rows x cols); the kept
+// rank is one more than the first c (counting down from rmin-1) whose
+// residual exceeds both 2 res_new and eps2, or 1 when none does.  Candidates
+// are evaluated kBatch at a time with one block matvec.
+int AlsSolver::scan(int i, int rmin, const double* L, i64 ldl, const double* Rr, i64 ldr, i64 rows,
+                    i64 cols, const double* rhs, double nrhs, double res_new, double eps2) {
+  const i64 N = rows * cols;
+  int c0 = rmin - 1;
+  while (c0 >= 1) {
+    const int cnt = std::min(kBatch, c0);
+    for (int q = 0; q < cnt; ++q)
+      gemm((int)rows, (int)cols, c0 - q, L, 1, ldl, Rr, 1, ldr, cand_ + N * q, 1, rows);
+    mv(i, cand_, candY_, cnt);
+    sub_cols_kernel<<<eb(N * cnt), 256, 0, s_>>>(N, cnt, candY_, rhs, candY_);
+    TTG_CHECK_LAUNCH();
+    TTG_CUDA(cudaMemsetAsync(red_, 0, sizeof(double) * cnt, s_));
+    int bx = (int)std::max<i64>(1, std::min<i64>(128, (N + 2047) / 2048));
+    sqnorm_cols_kernel<<<dim3(bx, cnt), 256, 0, s_>>>(N, candY_, N, red_);
+    TTG_CHECK_LAUNCH();
+    TTG_CUDA(cudaMemcpyAsync(h_, red_, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s_));
+    sync();
+    for (int q = 0; q < cnt; ++q) {
+      const double e = std::sqrt(h_[q]) / nrhs;
+      if (e > res_new * 2.0 && e > eps2) return c0 - q + 1;
+    }
+    c0 -= cnt;
+  }
+  return 1;
+}
+
+// duchol_fort (tt_linalg.f90:540-642).  trans: dA is n x m, else m x n.
+// Writes du (n x real) and returns real (the Fortran loop index: numvec, or
+// the failing step when the pivot vanishes).
+int AlsSolver::uchol(bool trans, i64 m, i64 n, const double* dA, int numvec, double* du) {
+  const i64 si = trans ? 1 : m, sk = trans ? n : 1;
+  double* lam = small_;          // numvec <= 16
+  double* Rk = small_ + 16;      // k x k
+  double* dv = small_ + 272;     // k x k
+  double* V = small_ + 528;      // k x k
+  double* piv = small_ + 784;
+  TTG_CUDA(cudaMemsetAsync(lam, 0, sizeof(double) * 16, s_));
+  TTG_CUDA(cudaMemsetAsync(du, 0, sizeof(double) * n * numvec, s_));
+  uchol_diag_kernel<<<eb(n), 256, 0, s_>>>(n, m, dA, si, sk, dd_);
+  TTG_CHECK_LAUNCH();
+  int cnt = 0;
+  bool broke = false;
+  while (cnt < numvec) {
+    argmax_abs_kernel<<<1, 256, 0, s_>>>(n, dd_, ired_);
+    TTG_CHECK_LAUNCH();
+    uchol_col_kernel<<<eb(n), 256, 0, s_>>>(n, m, dA, si, sk, ired_, cnt, lam, du);
+    TTG_CHECK_LAUNCH();
+    uchol_pick_kernel<<<1, 1, 0, s_>>>(n, ired_, cnt, du, piv);
+    TTG_CHECK_LAUNCH();
+    TTG_CUDA(cudaMemcpyAsync(h_, piv, sizeof(double), cudaMemcpyDeviceToHost, s_));
+    sync();
+    if (std::sqrt(std::fabs(h_[0])) < 1e-300) { broke = true; break; }
+    uchol_scale_kernel<<<eb(n), 256, 0, s_>>>(n, cnt, piv, du, dd_);
+    TTG_CHECK_LAUNCH();
+    const int k = cnt + 1;
+    qr(n, k, du, Rk);                                     // du[:, :k] = Q, Rk = R
+    uchol_dv_kernel<<<1, 256, 0, s_>>>(k, Rk, lam, dv);
+    TTG_CHECK_LAUNCH();
+    syev_jacobi(k, dv, k, lam, V, k, ired_ + 8, s_);      // ascending, as dsyev
+    gemm((int)n, k, k, du, 1, n, V, 1, k, tmp_, 1, n);
+    TTG_CUDA(cudaMemcpyAsync(du, tmp_, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, s_));
+    ++cnt;
+  }
+  return broke ? cnt + 1 : numvec;
+}
+
+// dbfun3_left as the reference writes it (tt_linalg.f90:242-253): Phi1's
+// (ry1, rx1, ra1) memory is multiplied as an (ra1*ry1) x rx1 matrix.
+// y: (ry1 n) x (rx2 ra2), ry1 = rx1 = rx_[i].
+void AlsSolver::bfun3_left(int i, const double* x, double* y) {
+  const i64 rx1 = rx_[i], m = n_[i], rx2 = rx_[i + 1], ry1 = rx1, n = m;
+  const i64 ra1 = P_.ra[i], ra2 = P_.ra[i + 1];
+  gemm((int)(ra1 * ry1), (int)(m * rx2), (int)rx1, phiA_[i], 1, ra1 * ry1, x, 1, rx1, tA_, 1,
+       ra1 * ry1);                                                         // (a1,c1),(j,b2)
+  perm1324_kernel<<<eb(ra1 * ry1 * m * rx2), 256, 0, s_>>>(ra1, ry1, m, rx2, tA_, tB_);  // a1,j,c1,b2
+  TTG_CHECK_LAUNCH();
+  perm1324_kernel<<<eb(ra1 * n * m * ra2), 256, 0, s_>>>(ra1, n, m, ra2, A_[i], tC_);   // a1,j,i,a2
+  TTG_CHECK_LAUNCH();
+  gemm((int)(ry1 * rx2), (int)(n * ra2), (int)(ra1 * m), tB_, ra1 * m, 1, tC_, 1, ra1 * m, tA_, 1,
+       ry1 * rx2);                                                         // (c1,b2),(i,a2)
+  perm1324_kernel<<<eb(ry1 * rx2 * n * ra2), 256, 0, s_>>>(ry1, rx2, n, ra2, tA_, y);   // c1,i,b2,a2
+  TTG_CHECK_LAUNCH();
+}
+
+// dbfun3_right (tt_linalg.f90:210-240): y (rx1 ra1) x (n ry2), ry2 = rx2
+void AlsSolver::bfun3_right(int i, const double* x, double* y) {
+  const i64 rx1 = rx_[i], m = n_[i], rx2 = rx_[i + 1], ry2 = rx2, n = m;
+  const i64 ra1 = P_.ra[i], ra2 = P_.ra[i + 1];
+  gemm((int)(rx1 * m), (int)(ra2 * ry2), (int)rx2, x, 1, rx1 * m, phiA_[i + 1], 1, rx2, tA_, 1,
+       rx1 * m);                                                           // b1,j,a2,c2
+  transpose_f64(rx1, m * ra2 * ry2, tA_, tB_, s_);                          // j,a2,c2,b1
+  gemm((int)(ra1 * n), (int)(ry2 * rx1), (int)(m * ra2), A_[i], 1, ra1 * n, tB_, 1, m * ra2, tA_,
+       1, ra1 * n);                                                        // a1,i,c2,b1
+  transpose_f64(ra1 * n * ry2, rx1, tA_, y, s_);                            // b1,a1,i,c2
+}
+
+void AlsSolver::run(AmenOut& out) {
+  const int d = P_.d;
+  n_ = P_.n;
+  rx_ = P_.rx;
+  const auto& ry = P_.ry;
+  const auto& ra = P_.ra;
+  TTG_REQUIRE(d >= 2, "amen: d must be >= 2");
+  TTG_REQUIRE(rx_[0] == 1 && rx_[d] == 1 && ry[0] == 1 && ry[d] == 1 && ra[0] == 1 && ra[d] == 1,
+              "boundary ranks must be 1");
+  const double eps2 = P_.eps / std::sqrt((double)d);
+  const int kick0 = P_.kick;
+  const int kpad = std::max(kick0, 0);
+  // rank capacities: the kept rank is at most min(rmax, both sides of the
+  // bond), and the kick adds at most kickrank
+  std::vector<i64> left(d + 1, 1), right(d + 1, 1);
+  for (int k = 1; k <= d; ++k) left[k] = std::min<i64>(left[k - 1] * n_[k - 1], 1ll << 40);
+  for (int k = d - 1; k >= 0; --k) right[k] = std::min<i64>(right[k + 1] * n_[k], 1ll << 40);
+  cap_.assign(d + 1, 1);
+  for (int k = 1; k < d; ++k)
+    cap_[k] = std::max(rx_[k], std::min(P_.rmax, std::min(left[k], right[k])) + kpad);
+  i64 Nmax = 1, ramax = 1, rymax = 1, T = 1, KB = 1, Mmax = 1, SVD = 1, PHS = 1, Cmax = 1;
+  size_t scr = 0, svs = 0;
+  for (int k = 0; k <= d; ++k) { ramax = std::max(ramax, ra[k]); rymax = std::max(rymax, ry[k]); }
+  for (int k = 0; k < d; ++k) {
+    const i64 c1 = cap_[k], c2 = cap_[k + 1], nk = n_[k];
+    Nmax = std::max(Nmax, c1 * nk * c2);
+    Mmax = std::max(Mmax, std::max(c1 * nk, nk * c2));
+    T = std::max(T, std::max(ra[k], ra[k + 1]) * std::max(c1, c2) * std::max(c1, c2) * nk *
+                        std::max(ra[k], ra[k + 1]) + ra[k] * nk * nk * ra[k + 1]);
+    KB = std::max(KB, c1 * nk * (ry[k + 1] + c2 * ra[k + 1]));
+    KB = std::max(KB, (ry[k] + c1 * ra[k]) * nk * c2);
+    Cmax = std::max(Cmax, std::max(c1 * nk * c2, std::max(ry[k], c1) * nk * std::max(ry[k + 1], c2)));
+    LocalDims L{c1, nk, c2, c1, nk, c2, ra[k], ra[k + 1]};
+    scr = std::max(scr, bfun3_f64_scratch(L, kBatch));
+    scr = std::max(scr, phi_f64_scratch(L));
+    scr = std::max(scr, (size_t)(4 * std::max(ry[k], c1) * nk * std::max(ry[k + 1], c2) * 8));
+    svs = std::max(svs, svd_scratch((int)(c1 * nk), (int)c2));
+    svs = std::max(svs, svd_scratch((int)c1, (int)(nk * c2)));
+    SVD = std::max(SVD, c1 * nk * c2 + std::max(c1 * nk, nk * c2) * std::min(std::max(c1 * nk, nk * c2), std::max(c1, c2)));
+    PHS = std::max(PHS, c1 * c1 * ra[k]);
+  }
+  const int nr = (int)std::min<i64>(std::min<i64>(Nmax, P_.nrestart), 60);
+  i64 at = 0, yt = 0;
+  for (int k = 0; k < d; ++k) {
+    at += ra[k] * n_[k] * n_[k] * ra[k + 1];
+    yt += ry[k] * n_[k] * ry[k + 1];
+  }
+  const i64 M2 = Mmax * std::max<i64>(Mmax, 1);
+  size_t total = al8(at) + al8(yt);
+  for (int k = 0; k < d; ++k) total += al8(cap_[k] * n_[k] * cap_[k + 1]);
+  for (int k = 0; k <= d; ++k) total += al8(cap_[k] * cap_[k] * ra[k]) + al8(cap_[k] * ry[k]);
+  total += 4 * al8(Nmax) + al8(Nmax * (nr + 1)) + al8(4096) + al8(64) + al8(Cmax) + al8(KB) +
+           3 * al8(T) + al8(SVD) + al8(1024) + al8(SVD) + svs + 256 + 2 * al8(Nmax * kBatch) +
+           al8(M2) + 2 * al8(M2) + al8(8192) + al8(M2) + scr + 256 + al8(Mmax * 16) +
+           al8(Mmax) + al8(1024) + al8(64) + (1 << 16);
+  mem_.alloc(total);
+  double* dA = mem_.take(at);
+  double* dY = mem_.take(yt);
+  A_.resize(d); Y_.resize(d); x_.resize(d);
+  {
+    i64 oa = 0, oy = 0;
+    for (int k = 0; k < d; ++k) {
+      A_[k] = dA + oa; oa += ra[k] * n_[k] * n_[k] * ra[k + 1];
+      Y_[k] = dY + oy; oy += ry[k] * n_[k] * ry[k + 1];
+    }
+  }
+  for (int k = 0; k < d; ++k) x_[k] = mem_.take(cap_[k] * n_[k] * cap_[k + 1]);
+  phiA_.resize(d + 1); phiy_.resize(d + 1);
+  for (int k = 0; k <= d; ++k) {
+    phiA_[k] = mem_.take(cap_[k] * cap_[k] * ra[k]);
+    phiy_[k] = mem_.take(cap_[k] * ry[k]);
+  }
+  rhs_ = mem_.take(Nmax); r0_ = mem_.take(Nmax); sol_ = mem_.take(Nmax); w_ = mem_.take(Nmax);
+  V_ = mem_.take(Nmax * (nr + 1));
+  gm_ = mem_.take(4096);
+  red_ = mem_.take(64);
+  kickY_ = mem_.take(Cmax);
+  kickB_ = mem_.take(KB);
+  tA_ = mem_.take(T); tB_ = mem_.take(T); tC_ = mem_.take(T);
+  U_ = mem_.take(SVD); S_ = mem_.take(1024); Vt_ = mem_.take(SVD);
+  svScr_ = (double*)mem_.take(svs / sizeof(double) + 1);
+  cand_ = mem_.take(Nmax * kBatch); candY_ = mem_.take(Nmax * kBatch);
+  Um_ = mem_.take(M2); Rm_ = mem_.take(M2); Rq_ = mem_.take(M2);
+  tau_ = mem_.take(8192);
+  tmp_ = mem_.take(M2);
+  scr_ = (double*)mem_.take(scr / sizeof(double) + 1);
+  du_ = mem_.take(Mmax * 16);
+  dd_ = mem_.take(Mmax);
+  small_ = mem_.take(1024);
+  ired_ = (int*)mem_.take(64);
+  TTG_CUDA(cudaMallocHost(&h_, 4096 * sizeof(double)));
+  struct HG { double* p; ~HG() { if (p) cudaFreeHost(p); } } hg{h_};
+
+  TTG_CUDA(cudaMemcpyAsync(dA, P_.crA, sizeof(double) * at, cudaMemcpyHostToDevice, s_));
+  TTG_CUDA(cudaMemcpyAsync(dY, P_.crY, sizeof(double) * yt, cudaMemcpyHostToDevice, s_));
+  {
+    i64 ox = 0;
+    for (int k = 0; k < d; ++k) {
+      const i64 sz = rx_[k] * n_[k] * rx_[k + 1];
+      TTG_CUDA(cudaMemcpyAsync(x_[k], P_.crX0 + ox, sizeof(double) * sz, cudaMemcpyHostToDevice, s_));
+      ox += sz;
+    }
+  }
+  for (double* ph : {phiA_[0], phiA_[d], phiy_[0], phiy_[d]}) fill_f64(ph, 1, 1.0, s_);
+
+  // initial QR, left to right (tt_adapt_als.f90:618-644)
+  for (int i = 0; i + 1 < d; ++i) {
+    const i64 m_ = rx_[i] * n_[i], rr = rx_[i + 1], p = n_[i + 1] * rx_[i + 2];
+    const i64 rnew = std::min(m_, rr);
+    TTG_CUDA(cudaMemcpyAsync(Um_, x_[i], sizeof(double) * m_ * rr, cudaMemcpyDeviceToDevice, s_));
+    qr(m_, rr, Um_, Rq_);
+    TTG_CUDA(cudaMemcpyAsync(x_[i], Um_, sizeof(double) * m_ * rnew, cudaMemcpyDeviceToDevice, s_));
+    gemm((int)rnew, (int)p, (int)rr, Rq_, 1, rnew, x_[i + 1], 1, rr, tmp_, 1, rnew);
+    TTG_CUDA(cudaMemcpyAsync(x_[i + 1], tmp_, sizeof(double) * rnew * p, cudaMemcpyDeviceToDevice, s_));
+    rx_[i + 1] = rnew;
+    upd_left(i);
+  }
+
+  const GmresBufs G{V_, w_, gm_, red_, h_};
+  double res_max = 0.0, last_res = 0.0, err_max = 0.0;
+  int i = d - 1, dir = -1, swp = 1, kick = kick0;
+  while (swp <= P_.nswp) {
+    const i64 r1 = rx_[i], r2 = rx_[i + 1], nk = n_[i];
+    const i64 N = r1 * nk * r2;
+    // local right-hand side (tt_adapt_als.f90:657-687)
+    if (dir < 0) {
+      gemm((int)(ry[i] * nk), (int)r2, (int)ry[i + 1], Y_[i], 1, ry[i] * nk, phiy_[i + 1], 1,
+           ry[i + 1], kickY_, 1, ry[i] * nk);
+      gemm((int)r1, (int)(nk * r2), (int)ry[i], phiy_[i], 1, r1, kickY_, 1, ry[i], rhs_, 1, r1);
+    } else {
+      gemm((int)r1, (int)(nk * ry[i + 1]), (int)ry[i], phiy_[i], 1, r1, Y_[i], 1, ry[i], kickY_, 1, r1);
+      gemm((int)(r1 * nk), (int)r2, (int)ry[i + 1], kickY_, 1, r1 * nk, phiy_[i + 1], 1, ry[i + 1],
+           rhs_, 1, r1 * nk);
+    }
+    // residual and the GMRES correction (:725-797)
+    mv(i, x_[i], r0_, 1);
+    sub_kernel<<<eb(N), 256, 0, s_>>>(N, r0_, rhs_, r0_);
+    TTG_CHECK_LAUNCH();
+    const double nrhs = norm2(rhs_, N);
+    double err = norm2(r0_, N) / nrhs;
+    res_max = std::max(res_max, err);
+    double res_new = err;
+    const double tau = eps2 / (err * 2.0);
+    if (tau < 1.0) {
+      auto mvf = [&](const double* in, double* o, int nv) { mv(i, in, o, nv); };
+      gmres_cgs2(mvf, N, r0_, sol_, tau, (int)std::min<i64>(std::min<i64>(P_.nrestart, N), 60),
+                 P_.niters, G, s_);
+      sub_kernel<<<eb(N), 256, 0, s_>>>(N, x_[i], sol_, x_[i]);
+      TTG_CHECK_LAUNCH();
+      mv(i, x_[i], r0_, 1);
+      sub_kernel<<<eb(N), 256, 0, s_>>>(N, r0_, rhs_, r0_);
+      TTG_CHECK_LAUNCH();
+      res_new = norm2(r0_, N) / nrhs;
+      err_max = std::max(err_max, norm2(sol_, N) / norm2(x_[i], N));
+    }
+    if (dir > 0 && i < d - 1) {
+      // truncation and kick to the right (:807-897)
+      const i64 m_ = r1 * nk, rr = r2, p = n_[i + 1] * rx_[i + 2];
+      i64 rnew = std::min(rr, m_);
+      if (kick > 0 || kick == -1) {
+        const int rmin = (int)std::min(m_, rr);
+        svd_jacobi((int)m_, (int)rr, x_[i], U_, S_, Vt_, svScr_, ired_ + 16, s_);
+        scale_rows_f64(rmin, rr, Vt_, rmin, S_, s_);                     // W = diag(s) Vt
+        int nn = scan(i, rmin, U_, m_, Vt_, rmin, m_, rr, rhs_, nrhs, res_new, eps2);
+        nn = (int)std::min<i64>(nn, P_.rmax);
+        // Um = U[:, :nn], Rm = W[:nn, :]
+        TTG_CUDA(cudaMemcpyAsync(Um_, U_, sizeof(double) * m_ * nn, cudaMemcpyDeviceToDevice, s_));
+        copy_rows_f64(rmin, nn, rr, Vt_, Rm_, s_);
+        rnew = nn;
+        if (kick > 0) {
+          // kick_block (m_ x (ry2 + rr ra2)) = [Y-projection | dbfun3_left]
+          TTG_CUDA(cudaMemcpyAsync(kickB_, kickY_, sizeof(double) * m_ * ry[i + 1],
+                                   cudaMemcpyDeviceToDevice, s_));
+          bfun3_left(i, x_[i], kickB_ + m_ * ry[i + 1]);
+          const int mm = uchol(true, rr * ra[i + 1] + ry[i + 1], m_, kickB_,
+                               (int)std::min<i64>(kick, m_), du_);
+          TTG_CUDA(cudaMemcpyAsync(Um_ + m_ * nn, du_, sizeof(double) * m_ * mm,
+                                   cudaMemcpyDeviceToDevice, s_));
+          pad_rows_kernel<<<eb((nn + mm) * rr), 256, 0, s_>>>(nn, mm, rr, Rm_, tmp_);
+          TTG_CHECK_LAUNCH();
+          rnew = std::min<i64>(m_, nn + mm);
+          qr(m_, nn + mm, Um_, Rq_);                                      // Rq (rnew x nn+mm)
+          gemm((int)rnew, (int)rr, nn + mm, Rq_, 1, rnew, tmp_, 1, nn + mm, Rm_, 1, rnew);
+        }
+      } else {
+        TTG_CUDA(cudaMemcpyAsync(Um_, x_[i], sizeof(double) * m_ * rr, cudaMemcpyDeviceToDevice, s_));
+        qr(m_, rr, Um_, Rm_);
+      }
+      TTG_REQUIRE(rnew <= cap_[i + 1], "amen: rank capacity exceeded");
+      TTG_CUDA(cudaMemcpyAsync(x_[i], Um_, sizeof(double) * m_ * rnew, cudaMemcpyDeviceToDevice, s_));
+      gemm((int)rnew, (int)p, (int)rr, Rm_, 1, rnew, x_[i + 1], 1, rr, tmp_, 1, rnew);
+      TTG_CUDA(cudaMemcpyAsync(x_[i + 1], tmp_, sizeof(double) * rnew * p, cudaMemcpyDeviceToDevice, s_));
+      rx_[i + 1] = rnew;
+      upd_left(i);
+    }
+    if (dir < 0 && i > 0) {
+      // truncation and kick to the left (:900-1040)
+      const i64 m_ = nk * r2, rl = r1, p = rx_[i - 1] * n_[i - 1];
+      i64 rnew = std::min(m_, rl);
+      if (kick > 0 || kick == -1) {
+        const int rmin = (int)std::min(m_, rl);
+        svd_jacobi((int)rl, (int)m_, x_[i], U_, S_, Vt_, svScr_, ired_ + 16, s_);
+        scale_cols_f64(rl, rmin, U_, rl, S_, s_);                        // L = U diag(s)
+        int nn = scan(i, rmin, U_, rl, Vt_, rmin, rl, m_, rhs_, nrhs, res_new, eps2);
+        nn = (int)std::min<i64>(nn, P_.rmax);
+        // Cm = Vt[:nn, :]^T (m_ x nn), Rm = L[:, :nn]^T (nn x rl)
+        copy_rows_f64(rmin, nn, m_, Vt_, tmp_, s_);
+        transpose_f64(nn, m_, tmp_, Um_, s_);
+        transpose_f64(rl, nn, U_, Rm_, s_);
+        rnew = nn;
+        if (kick > 0) {
+          // kick_block ((ry1 + rl ra1) x m_) = [Y-projection; dbfun3_right]
+          bfun3_right(i, x_[i], tC_);
+          concat_rows_kernel<<<eb((ry[i] + rl * ra[i]) * m_), 256, 0, s_>>>(ry[i], rl * ra[i], m_,
+                                                                          kickY_, tC_, kickB_);
+          TTG_CHECK_LAUNCH();
+          const int mm = uchol(false, rl * ra[i] + ry[i], m_, kickB_, (int)std::min<i64>(kick, m_), du_);
+          TTG_CUDA(cudaMemcpyAsync(Um_ + m_ * nn, du_, sizeof(double) * m_ * mm,
+                                   cudaMemcpyDeviceToDevice, s_));
+          pad_rows_kernel<<<eb((nn + mm) * rl), 256, 0, s_>>>(nn, mm, rl, Rm_, tmp_);
+          TTG_CHECK_LAUNCH();
+          rnew = std::min<i64>(m_, nn + mm);
+          qr(m_, nn + mm, Um_, Rq_);
+          gemm((int)rnew, (int)rl, nn + mm, Rq_, 1, rnew, tmp_, 1, nn + mm, Rm_, 1, rnew);
+        }
+      } else {
+        transpose_f64(rl, m_, x_[i], Um_, s_);                          // m_ x rl
+        qr(m_, rl, Um_, Rm_);
+      }
+      TTG_REQUIRE(rnew <= cap_[i], "amen: rank capacity exceeded");
+      transpose_f64(m_, rnew, Um_, x_[i], s_);                          // rnew x m_
+      // core i-1 (p x rl) * Rm^T (rl x rnew)
+      gemm((int)p, (int)rnew, (int)rl, x_[i - 1], 1, p, Rm_, rnew, 1, tmp_, 1, p);
+      TTG_CUDA(cudaMemcpyAsync(x_[i - 1], tmp_, sizeof(double) * p * rnew, cudaMemcpyDeviceToDevice, s_));
+      rx_[i] = rnew;
+      upd_right(i);
+    }
+    if ((dir > 0 && i == d - 1) || (dir < 0 && i == 0)) {
+      last_res = res_max;
+      if (P_.verb > 0) {
+        i64 mr = *std::max_element(rx_.begin(), rx_.end());
+        fprintf(stderr, "als_fort: iteration:%d(%d) max(ry):%lld err_max:%.3e res_max:%.3e\n", swp,
+                dir, (long long)mr, err_max, res_max);
+      }
+    }
+    if (dir > 0 && i == d - 1) {
+      dir = -1;
+      i += 1;
+      if (kick < 0) break;
+      if (res_max < P_.eps) kick = -1;
+      ++swp;
+      err_max = 0.0;
+      res_max = 0.0;
+    }
+    if (dir < 0 && i == 0) {
+      if (kick < 0) break;
+      if (res_max < P_.eps) kick = -1;
+      dir = 1;
+      i -= 1;
+      err_max = 0.0;
+      res_max = 0.0;
+    }
+    i += dir;
+  }
+  sync();
+  i64 tot = 0;
+  for (int k = 0; k < d; ++k) tot += rx_[k] * n_[k] * rx_[k + 1];
+  out.cores.resize(tot);
+  i64 off = 0;
+  for (int k = 0; k < d; ++k) {
+    const i64 sz = rx_[k] * n_[k] * rx_[k + 1];
+    TTG_CUDA(cudaMemcpyAsync(out.cores.data() + off, x_[k], sizeof(double) * sz,
+                             cudaMemcpyDeviceToHost, s_));
+    off += sz;
+  }
+  sync();
+  out.rx = rx_;
+  out.sweeps = std::min(swp, P_.nswp);
+  out.res_max = last_res;
+  out.matvecs = nmv_;
+}
+
 }  // namespace ttg
 
 using namespace ttg;
 
-extern "C" int ttg_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
-                              const ttg_int* ry, const ttg_int* ra, const double* crA,
-                              const double* crY, const double* crX0, ttg_int* rx, double eps,
-                              ttg_int rmax, ttg_int kickrank, ttg_int nswp, int verb, int method) {
+// dtt_amen_solve (ttamen.f90:29-252) with flat arrays: the dtt type of the
+// reference is not C-interoperable, so this entry point takes the packed cores
+extern "C" int ttg_dtt_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
+                                  const ttg_int* ry, const ttg_int* ra, const double* crA,
+                                  const double* crY, const double* crX0, ttg_int* rx, double eps,
+                                  ttg_int rmax, ttg_int kickrank, ttg_int nswp, int verb,
+                                  int method) {
   if (!ctx) return TTG_ERR_ARG;
   try {
     TTG_CUDA(cudaSetDevice(ctx->device));
@@ -738,6 +1329,53 @@ extern "C" int ttg_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const t
     long long l0 = g_launches;
     AmenOut out;
     AmenSolver solver(ctx, P);
+    solver.run(out);
+    for (int k = 0; k <= d; ++k) rx[k] = out.rx[k];
+    ctx->result_core = std::move(out.cores);
+    ctx->zresult_core.clear();
+    ctx->stat_matvecs = out.matvecs;
+    ctx->stat_sweeps = out.sweeps;
+    ctx->stat_res = out.res_max;
+    ctx->stat_launches = g_launches - l0;
+  } catch (const ttg::Error& e) {
+    ctx->last_error = e.msg;
+    return e.code;
+  }
+  return TTG_OK;
+}
+
+// tt_amen_solve (tt_adapt_als.f90:513-1132)
+extern "C" int ttg_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
+                              const ttg_int* ry, const ttg_int* ra, const double* crA,
+                              const double* crY, const double* crX0, ttg_int* rx, double eps,
+                              ttg_int kickrank, ttg_int nswp, int verb, char prec,
+                              ttg_int nrestart, ttg_int niters, ttg_int rmax, int method) {
+  if (!ctx) return TTG_ERR_ARG;
+  try {
+    TTG_CUDA(cudaSetDevice(ctx->device));
+    TTG_REQUIRE(d > 1 && n && m && ry && ra && crA && crY && crX0 && rx, "null argument");
+    TTG_REQUIRE(method == TTG_METHOD_PLAIN, "amen: only the FP64 method is built");
+    if (prec != 'n' && prec != 'N' && prec != 0)
+      throw Error{TTG_ERR_UNSUPPORTED, "amen: only the 'n' preconditioner is built"};
+    for (int k = 0; k < d; ++k) TTG_REQUIRE(n[k] == m[k], "amen needs square cores (n == m)");
+    TTG_REQUIRE(kickrank <= 16, "amen: kickrank > 16");
+    AlsParams P;
+    P.d = (int)d;
+    P.n.assign(n, n + d);
+    P.ry.assign(ry, ry + d + 1);
+    P.ra.assign(ra, ra + d + 1);
+    P.rx.assign(rx, rx + d + 1);
+    P.crA = crA; P.crY = crY; P.crX0 = crX0;
+    P.eps = eps;
+    P.rmax = rmax > 0 ? rmax : (1ll << 40);
+    P.kick = (int)kickrank;
+    P.nswp = nswp > 0 ? (int)nswp : 20;
+    P.nrestart = nrestart > 0 ? (int)nrestart : 40;
+    P.niters = niters > 0 ? (int)niters : 2;
+    P.verb = verb;
+    long long l0 = g_launches;
+    AmenOut out;
+    AlsSolver solver(ctx, P);
     solver.run(out);
     for (int k = 0; k <= d; ++k) rx[k] = out.rx[k];
     ctx->result_core = std::move(out.cores);

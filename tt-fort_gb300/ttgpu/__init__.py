@@ -65,7 +65,7 @@ EXPORTED = [
     "ttg_version", "ttg_dbfun3", "ttg_dbfun3_split", "ttg_dbfun3_noalloc", "ttg_zbfun3", "ttg_zbfun3_transp",
     "ttg_dphi_left", "ttg_dphi_right", "ttg_zphi_left", "ttg_zphi_right", "ttg_dphi2_left",
     "ttg_dphi2_right", "ttg_d2d_fullmat", "ttg_dqr", "ttg_zqr", "ttg_dsyev", "ttg_dgesvd",
-    "ttg_my_chop3", "ttg_dmaxvol", "ttg_eigb", "ttg_ksl_z", "ttg_amen_solve",
+    "ttg_my_chop3", "ttg_dmaxvol", "ttg_eigb", "ttg_ksl_z", "ttg_amen_solve", "ttg_dtt_amen_solve",
     "ttg_result_size", "ttg_result_copy", "ttg_zresult_copy", "ttg_free_result", "ttg_stats",
     "ttg_launch_count", "ttg_localop_create", "ttg_localop_apply", "ttg_localop_destroy",
     "ttg_mlp_create", "ttg_mlp_destroy", "ttg_mlp_nparams", "ttg_mlp_get_params",
@@ -198,17 +198,33 @@ def ztt_ksl(d, n, m, ra, crA, crY0, ry, tau, rmax, kickrank=None, nswp=None, ver
     return _result(ctx, real=False), [int(v) for v in ry_]
 
 
-def tt_amen_solve(d, n, m, ry, ra, crA, crY, crX0, rx, eps, rmax=1000, kickrank=4, nswp=20,
-                  verb=0, method="plain", ctx=None):
+def tt_amen_solve(d, n, m, ry, ra, crA, crY, crX0, rx, eps, kickrank=4, nswp=20, verb=0,
+                  prec="n", nrestart=40, niters=2, rmax=0, method="plain", ctx=None):
     """AMEn solve A x = y (tt_amen_solve, tt_adapt_als.f90:513).  Returns (cores, rx)."""
     ctx = ctx or default_context()
     n_, m_, ry_, ra_ = _iarr(n), _iarr(m), _iarr(ry), _iarr(ra)
     rx_ = _iarr(rx).copy()
     A_, Y_, X_ = _darr(crA), _darr(crY), _darr(crX0)
     rc = lib().ttg_amen_solve(ctx.handle, _i64(d), _p(n_), _p(m_), _p(ry_), _p(ra_), _p(A_),
-                              _p(Y_), _p(X_), _p(rx_), C.c_double(eps), _i64(rmax),
-                              _i64(kickrank), _i64(nswp), C.c_int(verb),
-                              C.c_int(METHOD[method]))
+                              _p(Y_), _p(X_), _p(rx_), C.c_double(eps), _i64(kickrank),
+                              _i64(nswp), C.c_int(verb), C.c_char(prec.encode()),
+                              _i64(nrestart), _i64(niters), _i64(rmax), C.c_int(METHOD[method]))
+    ctx.check(rc)
+    return _result(ctx, real=True), [int(v) for v in rx_]
+
+
+def dtt_amen_solve(d, n, m, ry, ra, crA, crY, crX0, rx, eps, rmax=1000, kickrank=4, nswp=20,
+                   verb=0, method="plain", ctx=None):
+    """AMEn solve of ttamen.f90 (dtt_amen_solve, ttamen.f90:29) on packed cores.
+    Returns (cores, rx)."""
+    ctx = ctx or default_context()
+    n_, m_, ry_, ra_ = _iarr(n), _iarr(m), _iarr(ry), _iarr(ra)
+    rx_ = _iarr(rx).copy()
+    A_, Y_, X_ = _darr(crA), _darr(crY), _darr(crX0)
+    rc = lib().ttg_dtt_amen_solve(ctx.handle, _i64(d), _p(n_), _p(m_), _p(ry_), _p(ra_), _p(A_),
+                                  _p(Y_), _p(X_), _p(rx_), C.c_double(eps), _i64(rmax),
+                                  _i64(kickrank), _i64(nswp), C.c_int(verb),
+                                  C.c_int(METHOD[method]))
     ctx.check(rc)
     return _result(ctx, real=True), [int(v) for v in rx_]
 
