@@ -226,6 +226,25 @@ int ttg_dtt_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int*
                        const ttg_int* ry, const ttg_int* ra, const double* crA,
                        const double* crY, const double* crX0, ttg_int* rx, double eps,
                        ttg_int rmax, ttg_int kickrank, ttg_int nswp, int verb, int method);
+/* Batched eigen sweeps (no counterpart in the reference, whose tt_eigb
+ * solves one chain per call): chains are queued with their inputs copied,
+ * then ttg_batch_run solves all of them on nworkers host threads, each with
+ * its own non-blocking stream, so the chains' kernels overlap on the GPU
+ * (longest chains first).  Arguments of ttg_batch_add_eigb mean what they
+ * mean for ttg_eigb; ry[d] must equal B. */
+typedef struct ttg_batch ttg_batch;
+int ttg_batch_create(ttg_ctx* ctx, int nworkers, ttg_batch** out);
+int ttg_batch_destroy(ttg_batch* batch);
+int ttg_batch_add_eigb(ttg_batch* batch, ttg_int d, const ttg_int* n, const ttg_int* m,
+                       const ttg_int* ra, const double* crA, const double* crY0,
+                       const ttg_int* ry, double eps, ttg_int rmax, ttg_int B, ttg_int nswp,
+                       ttg_int max_full_size, int method, ttg_int* index);
+int ttg_batch_run(ttg_batch* batch);
+/* per chain: B eigenvalues, d+1 ranks, number of core elements, local
+ * matvecs, wall seconds on its worker, status (0, 1 = not run, < 0 error) */
+int ttg_batch_result(const ttg_batch* batch, ttg_int i, double* lambda, ttg_int* ry,
+                     ttg_int* ncore, ttg_int* matvecs, double* seconds, int* status);
+int ttg_batch_cores(const ttg_batch* batch, ttg_int i, double* out, ttg_int nelem);
 /* Results of the last driver call. */
 int ttg_result_size(const ttg_ctx* ctx, ttg_int* nelem);
 int ttg_result_copy(const ttg_ctx* ctx, double* out, ttg_int nelem);   /* real */

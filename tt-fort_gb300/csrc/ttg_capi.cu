@@ -7,7 +7,7 @@
 
 namespace ttg {
 
-long long g_launches = 0;
+std::atomic<long long> g_launches{0};
 
 void Workspace::reserve(size_t bytes) {
   bytes = (bytes + 255) & ~size_t(255);
@@ -362,6 +362,6 @@ int ttg_stats(const ttg_ctx* c, ttg_int* matvecs, ttg_int* sweeps, double* res,
 }
 
 /* total kernel launches issued by this library in this process */
-ttg_int ttg_launch_count(void) { return (ttg_int)ttg::g_launches; }
+ttg_int ttg_launch_count(void) { return (ttg_int)ttg::g_launches.load(); }
 
 }  // extern "C"

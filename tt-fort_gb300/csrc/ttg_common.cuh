@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 #include <complex>
+#include <atomic>
 
 #include "../../include/ttgpu.h"
 
@@ -40,7 +41,7 @@ struct Error {
 
 // every kernel launch site is followed by TTG_CHECK_LAUNCH(); it also counts
 // the launches (reported as gpu_launches by the benchmark)
-extern long long g_launches;
+extern std::atomic<long long> g_launches;
 #define TTG_CHECK_LAUNCH()                                                      \
   do {                                                                          \
     ++::ttg::g_launches;                                                        \

@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <numeric>
+#include <thread>
 
 namespace ttg {
 
@@ -457,5 +458,174 @@ extern "C" int ttg_eigb(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int
     ctx->last_error = e.msg;
     return e.code;
   }
+  return TTG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched eigen sweeps: many independent chains (no counterpart in the
+// reference, whose tt_eigb solves one chain per call).  A single chain's
+// sweep is sequential, so a batch is spread over worker threads, each with
+// its own context and non-blocking stream; the chains' kernels overlap on
+// the GPU.  Chains are taken longest first (estimated cost d * rmax^3 * B).
+// ---------------------------------------------------------------------------
+struct ttg_batch {
+  ttg_ctx* ctx = nullptr;
+  int nworkers = 1;
+  struct Job {
+    int d = 0;
+    std::vector<i64> n, m, ra, ry;
+    std::vector<double> crA, crY0;
+    double eps = 0.0;
+    i64 rmax = 0;
+    int B = 1, nswp = 20, method = 0;
+    i64 mfs = 2000;
+    // results
+    int status = 1;           // 1: not run
+    std::string msg;
+    EigbOutput out;
+    double seconds = 0.0;
+  };
+  std::vector<Job> jobs;
+};
+
+extern "C" int ttg_batch_create(ttg_ctx* ctx, int nworkers, ttg_batch** out) {
+  if (!ctx || !out || nworkers < 1 || nworkers > 256) return TTG_ERR_ARG;
+  ttg_batch* b = new ttg_batch();
+  b->ctx = ctx;
+  b->nworkers = nworkers;
+  *out = b;
+  return TTG_OK;
+}
+
+extern "C" int ttg_batch_destroy(ttg_batch* b) {
+  if (!b) return TTG_ERR_ARG;
+  delete b;
+  return TTG_OK;
+}
+
+extern "C" int ttg_batch_add_eigb(ttg_batch* b, ttg_int d, const ttg_int* n, const ttg_int* m,
+                                  const ttg_int* ra, const double* crA, const double* crY0,
+                                  const ttg_int* ry, double eps, ttg_int rmax, ttg_int B,
+                                  ttg_int nswp, ttg_int max_full_size, int method, ttg_int* index) {
+  if (!b) return TTG_ERR_ARG;
+  ttg_ctx* c = b->ctx;
+  try {
+    TTG_REQUIRE(d > 0 && n && m && ra && crA && crY0 && ry && B > 0, "batch: null or bad argument");
+    TTG_REQUIRE(method == TTG_METHOD_PLAIN || method == TTG_METHOD_SPLIT, "unknown method");
+    TTG_REQUIRE(ry[d] == B, "batch: ry[d] must equal B");
+    ttg_batch::Job j;
+    j.d = (int)d;
+    j.n.assign(n, n + d);
+    j.m.assign(m, m + d);
+    j.ra.assign(ra, ra + d + 1);
+    j.ry.assign(ry, ry + d + 1);
+    i64 na = 0, ny = 0;
+    for (int k = 0; k < d; ++k) {
+      na += ra[k] * n[k] * m[k] * ra[k + 1];
+      ny += ry[k] * n[k] * ry[k + 1];
+    }
+    j.crA.assign(crA, crA + na);
+    j.crY0.assign(crY0, crY0 + ny);
+    j.eps = eps;
+    j.rmax = rmax;
+    j.B = (int)B;
+    j.nswp = (int)(nswp > 0 ? nswp : 20);
+    j.mfs = max_full_size > 0 ? max_full_size : 2000;
+    j.method = method;
+    b->jobs.push_back(std::move(j));
+    if (index) *index = (ttg_int)b->jobs.size() - 1;
+  } catch (const ttg::Error& e) {
+    c->last_error = e.msg;
+    return e.code;
+  }
+  return TTG_OK;
+}
+
+// Runs every chain that has not run yet.  Returns TTG_OK when all succeeded,
+// else the first failing chain's status (each chain's own status and message
+// are kept: ttg_batch_result).
+extern "C" int ttg_batch_run(ttg_batch* b) {
+  if (!b) return TTG_ERR_ARG;
+  ttg_ctx* c = b->ctx;
+  std::vector<int> order;
+  for (int i = 0; i < (int)b->jobs.size(); ++i)
+    if (b->jobs[i].status == 1) order.push_back(i);
+  auto cost = [&](int i) {
+    const auto& j = b->jobs[i];
+    const double r = (double)std::max<i64>(1, j.rmax);
+    return (double)j.d * r * r * r * j.B;
+  };
+  std::stable_sort(order.begin(), order.end(), [&](int a, int z) { return cost(a) > cost(z); });
+  std::atomic<size_t> next{0};
+  const int nw = std::max(1, std::min<int>(b->nworkers, (int)order.size()));
+  auto worker = [&]() {
+    ttg_ctx* wc = nullptr;
+    const int rc0 = ttg_create(c->device, &wc);
+    while (true) {
+      const size_t q = next.fetch_add(1);
+      if (q >= order.size()) break;
+      auto& j = b->jobs[order[q]];
+      if (rc0 != TTG_OK) {
+        j.status = TTG_ERR_CUDA;
+        j.msg = "batch: worker context creation failed";
+        continue;
+      }
+      try {
+        TTG_CUDA(cudaSetDevice(wc->device));
+        EigbParams P;
+        P.d = j.d;
+        P.n = j.n; P.m = j.m; P.ra = j.ra; P.ry = j.ry;
+        P.crA = j.crA.data();
+        P.crY0 = j.crY0.data();
+        P.eps = j.eps;
+        P.rmax = j.rmax;
+        P.B = j.B;
+        P.nswp = j.nswp;
+        P.max_full_size = j.mfs;
+        P.verb = 0;
+        P.method = j.method;
+        const auto t0 = std::chrono::steady_clock::now();
+        run_eigb(wc, P, j.out);
+        j.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        j.status = TTG_OK;
+      } catch (const ttg::Error& e) {
+        j.status = e.code;
+        j.msg = e.msg;
+      }
+    }
+    if (wc) ttg_destroy(wc);
+  };
+  std::vector<std::thread> th;
+  for (int w = 0; w < nw; ++w) th.emplace_back(worker);
+  for (auto& t : th) t.join();
+  for (int i : order)
+    if (b->jobs[i].status != TTG_OK) {
+      c->last_error = "batch chain " + std::to_string(i) + ": " + b->jobs[i].msg;
+      return b->jobs[i].status;
+    }
+  return TTG_OK;
+}
+
+// lambda (B), ry (d+1), ncore = number of core elements, stats; status of the
+// chain (TTG_OK, 1 = not run, < 0 = its error)
+extern "C" int ttg_batch_result(const ttg_batch* b, ttg_int i, double* lambda, ttg_int* ry,
+                                ttg_int* ncore, ttg_int* matvecs, double* seconds, int* status) {
+  if (!b || i < 0 || i >= (ttg_int)b->jobs.size()) return TTG_ERR_ARG;
+  const auto& j = b->jobs[i];
+  if (status) *status = j.status;
+  if (j.status != TTG_OK) return TTG_OK;
+  if (lambda) for (int k = 0; k < j.B; ++k) lambda[k] = j.out.lambda[k];
+  if (ry) for (int k = 0; k <= j.d; ++k) ry[k] = j.out.ry[k];
+  if (ncore) *ncore = (ttg_int)j.out.cores.size();
+  if (matvecs) *matvecs = j.out.matvecs;
+  if (seconds) *seconds = j.seconds;
+  return TTG_OK;
+}
+
+extern "C" int ttg_batch_cores(const ttg_batch* b, ttg_int i, double* out, ttg_int nelem) {
+  if (!b || !out || i < 0 || i >= (ttg_int)b->jobs.size()) return TTG_ERR_ARG;
+  const auto& j = b->jobs[i];
+  if (j.status != TTG_OK || nelem != (ttg_int)j.out.cores.size()) return TTG_ERR_ARG;
+  std::copy(j.out.cores.begin(), j.out.cores.end(), out);
   return TTG_OK;
 }

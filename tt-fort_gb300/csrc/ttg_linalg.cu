@@ -308,12 +308,10 @@ void syev_jacobi(int k, double* A, int lda, double* w, double* V, int ldv, int* 
   size_t smem = (size_t)(warm ? 3 : 2) * k * k * sizeof(double);
   int mode = smem <= 200 * 1024 ? 1 : 0;
   if (mode) {
-    static bool attr_set = false;
-    if (!attr_set) {
-      TTG_CUDA(cudaFuncSetAttribute(syev_jacobi_kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-      attr_set = true;
-    }
+    // thread-safe one-time set-up (C++ static initialisation)
+    static const cudaError_t attr_rc = cudaFuncSetAttribute(
+        syev_jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    TTG_CUDA(attr_rc);
   } else {
     smem = 0;
   }
@@ -443,14 +441,16 @@ static void svd_tall(int p, int q, double* Mw, double* U, double* sigma, double*
   // Mw (p x q, p >= q) is overwritten
   int npairs = (q + 1) / 2;
   int blocks = std::max(1, npairs);
-  static int max_coop = -1;
-  if (max_coop < 0) {
-    int dev, nsm, per;
-    TTG_CUDA(cudaGetDevice(&dev));
-    TTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    TTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, svd_rotate_kernel, SVD_NT, 0));
-    max_coop = nsm * per;
-  }
+  static const int max_coop = [] {
+    int dev = 0, nsm = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, svd_rotate_kernel, SVD_NT, 0) !=
+            cudaSuccess)
+      return 0;
+    return nsm * per;
+  }();
+  TTG_REQUIRE(max_coop > 0, "svd: occupancy query failed");
   blocks = std::min(blocks, max_coop);
   void* args[] = {&p, &q, &Mw, &V, &counters, &status};
   TTG_CUDA(cudaLaunchCooperativeKernel((void*)svd_rotate_kernel, dim3(blocks), dim3(SVD_NT),

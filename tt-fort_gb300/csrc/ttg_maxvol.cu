@@ -249,15 +249,17 @@ extern "C" int ttg_dmaxvol(ttg_ctx* c, ttg_int m, ttg_int n, const double* A, tt
     const int maxit = maxiters > 0 ? (int)std::min<ttg_int>(maxiters, 1 << 30) : 1024;
     cudaStream_t s = c->stream;
     // cooperative grid for the iterations
-    static int max_coop = -1;
-    if (max_coop < 0) {
-      int dev, nsm, per;
-      TTG_CUDA(cudaGetDevice(&dev));
-      TTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-      TTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, maxvol_iter_kernel, MV_NT,
-                                                             (MV_MAX_ROWS + 4096) * sizeof(double)));
-      max_coop = nsm * std::max(per, 1);
-    }
+    static const int max_coop = [] {
+      int dev = 0, nsm = 0, per = 0;
+      if (cudaGetDevice(&dev) != cudaSuccess ||
+          cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, maxvol_iter_kernel, MV_NT,
+                                                        (MV_MAX_ROWS + 4096) * sizeof(double)) !=
+              cudaSuccess)
+        return 0;
+      return nsm * std::max(per, 1);
+    }();
+    TTG_REQUIRE(max_coop > 0, "maxvol: occupancy query failed");
     int blocks = (int)std::min<i64>(std::min(max_coop, 152), std::max<i64>(1, ceil_div(m, (i64)64)));
     blocks = std::max(blocks, (int)std::min<i64>(max_coop, ceil_div(m, (i64)MV_MAX_ROWS)));
     TTG_REQUIRE(ceil_div(m, (i64)blocks) <= MV_MAX_ROWS, "maxvol: too many rows for one grid");

@@ -505,13 +505,13 @@ __global__ void __launch_bounds__(256)
 }
 
 static int num_sms() {
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
+  static const int nsm = [] {
+    int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0)
-      nsm = 148;
-  }
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+      v = 148;
+    return v;
+  }();
   return nsm;
 }
 
@@ -568,11 +568,9 @@ static void gemm_launch_bn(const Tiled& A, const Tiled& B, int M, int N, OutT* o
   constexpr int STAGES = stages_for(BN);
   constexpr size_t smem = smem_for(BN) + SMEM_PAD;
   auto kern = split_gemm_kernel<BN, STAGES, OutT>;
-  static bool attr = false;
-  if (!attr) {
-    TTG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  static const cudaError_t attr_rc =
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  TTG_CUDA(attr_rc);
   dim3 grid(A.rtiles, B.rtiles);
   kern<<<grid, NTHREADS, smem, s>>>(A.hi, A.lo, B.hi, B.lo, M, N, A.ktiles, out, rpv, vstride,
                                     rstride, cstride, err);

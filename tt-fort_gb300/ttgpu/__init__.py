@@ -71,7 +71,8 @@ EXPORTED = [
     "ttg_mlp_create", "ttg_mlp_destroy", "ttg_mlp_nparams", "ttg_mlp_get_params",
     "ttg_mlp_set_params", "ttg_mlp_get_grads", "ttg_mlp_forward", "ttg_mlp_loss_grad",
     "ttg_mlp_adam_step", "ttg_set_learned", "ttg_record_count", "ttg_record_clear",
-    "ttg_mlp_train_recorded",
+    "ttg_mlp_train_recorded", "ttg_batch_create", "ttg_batch_destroy", "ttg_batch_add_eigb",
+    "ttg_batch_run", "ttg_batch_result", "ttg_batch_cores",
 ]
 
 
@@ -444,3 +445,52 @@ def record_count(ctx=None):
 def record_clear(ctx=None):
     ctx = ctx or default_context()
     ctx.check(lib().ttg_record_clear(ctx.handle))
+
+
+# ---------------------------------------------------------- batched chains
+class EigbBatch:
+    """Many independent tt_eigb chains solved together (no counterpart in
+    the reference): ``add`` queues a chain (inputs are copied), ``run``
+    solves every queued chain on ``nworkers`` host threads with one stream
+    each, ``result(i)`` returns (lambda, cores, ry, stats) like ``tt_eigb``."""
+
+    def __init__(self, nworkers=8, ctx=None):
+        self.ctx = ctx or default_context()
+        self._h = C.c_void_p()
+        self.ctx.check(lib().ttg_batch_create(self.ctx.handle, C.c_int(nworkers), C.byref(self._h)))
+        self._meta = []
+
+    def add(self, d, n, m, ra, crA, crY0, ry, eps, rmax, B, nswp=20, max_full_size=2000,
+            method="plain"):
+        n_, m_, ra_, ry_ = _iarr(n), _iarr(m), _iarr(ra), _iarr(ry)
+        A_, Y_ = _darr(crA), _darr(crY0)
+        idx = _i64()
+        self.ctx.check(lib().ttg_batch_add_eigb(self._h, _i64(d), _p(n_), _p(m_), _p(ra_), _p(A_),
+                                                _p(Y_), _p(ry_), C.c_double(eps), _i64(rmax),
+                                                _i64(B), _i64(nswp), _i64(max_full_size),
+                                                C.c_int(METHOD[method]), C.byref(idx)))
+        self._meta.append((d, B))
+        return idx.value
+
+    def run(self):
+        self.ctx.check(lib().ttg_batch_run(self._h))
+
+    def result(self, i):
+        d, B = self._meta[i]
+        lam = np.zeros(B)
+        ry = np.zeros(d + 1, dtype=np.int64)
+        nc, mv = _i64(), _i64()
+        sec = C.c_double()
+        st = C.c_int()
+        self.ctx.check(lib().ttg_batch_result(self._h, _i64(i), _p(lam), _p(ry), C.byref(nc),
+                                              C.byref(mv), C.byref(sec), C.byref(st)))
+        if st.value != TTG_OK:
+            raise TTGError(st.value, f"batch chain {i} did not succeed")
+        cores = np.zeros(nc.value)
+        self.ctx.check(lib().ttg_batch_cores(self._h, _i64(i), _p(cores), _i64(nc.value)))
+        return lam, cores, [int(v) for v in ry], {"matvecs": mv.value, "seconds": sec.value}
+
+    def close(self):
+        if self._h:
+            lib().ttg_batch_destroy(self._h)
+            self._h = C.c_void_p()
