@@ -207,6 +207,11 @@ def main():
         dist.init_process_group("nccl")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     ctx = ttgpu.Context(torch.cuda.current_device())
+    # a non-blocking stream of our own (the legacy default stream serialises
+    # with every other stream and cannot be captured into CUDA graphs); it is
+    # torch's current stream from here on, so events and flushes use it too
+    bench_stream = torch.cuda.Stream()
+    torch.cuda.set_stream(bench_stream)
     ctx.bind_torch_stream()
     n, m, ra, crA, ry, cr = workload()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")

@@ -131,7 +131,64 @@ struct JdCg {
     gemm_nn_small(N, t, nb, X, N, c, nb, v, N, -1.0, 1.0, s);
   }
 
+  // The fixed-length CG solve issues ~12 launches per step and has no host
+  // synchronisation, so after its first call for a given (block, shift,
+  // Ritz-vector) set of buffers and widths it is captured once into a CUDA
+  // graph and replayed: one launch per correction solve instead of ~150.
+  bool use_graph = true;
+  struct Cached {
+    double* T;
+    const double* X;
+    const double* theta;
+    int t, nb;
+    cudaGraphExec_t exec;
+    long long nlaunch;
+  };
+  std::vector<Cached> graphs;
+  JdCg() = default;
+  JdCg(const JdCg&) = delete;
+  JdCg& operator=(const JdCg&) = delete;
+  ~JdCg() {
+    for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
+  }
+
   void operator()(double* T, int t, const double* X, int nb, const double* theta) {
+    // the legacy default stream cannot be captured
+    if (!use_graph || s == nullptr || s == cudaStreamLegacy) { run(T, t, X, nb, theta); return; }
+    for (auto& g : graphs)
+      if (g.T == T && g.X == X && g.theta == theta && g.t == t && g.nb == nb) {
+        TTG_CUDA(cudaGraphLaunch(g.exec, s));
+        g_launches += g.nlaunch;
+        return;
+      }
+    const long long l0 = g_launches;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      use_graph = false;
+      run(T, t, X, nb, theta);
+      return;
+    }
+    cudaGraph_t graph = nullptr;
+    try {
+      run(T, t, X, nb, theta);
+    } catch (...) {
+      cudaStreamEndCapture(s, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    TTG_CUDA(cudaStreamEndCapture(s, &graph));
+    const long long nl = g_launches - l0;
+    g_launches -= nl;                     // captured, not yet run
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    TTG_CUDA(e);
+    graphs.push_back(Cached{T, X, theta, t, nb, exec, nl});
+    TTG_CUDA(cudaGraphLaunch(exec, s));
+    g_launches += nl;
+  }
+
+  void run(double* T, int t, const double* X, int nb, const double* theta) {
     double* rr = sc;
     double* rr_new = sc + 64;
     double* pq = sc + 2 * 64;
@@ -190,6 +247,7 @@ DavidsonStats chosen_solve(i64 N, int B, void* dav_mem, double* hbuf, void* jd_m
                            cudaStream_t s, DavTimer* timer, int* fp64_matvecs) {
   JdCg jd;
   jd.N = N; jd.Bmax = B; jd.iters = 12; jd.rel_tol = 1e-3; jd.low = mvlow; jd.s = s;
+  jd.use_graph = timer == nullptr;      // the profiler synchronises inside matvecs
   jd.bind(jd_mem);
   const int maxb2 = (int)std::min<i64>(2 * B, N);
   auto jd_prec = [&jd](double* T, int t, const double* Xr, int nb, const double* th) {
