@@ -327,7 +327,8 @@ constexpr int SVD_NT = 32;   // one warp per CTA: FP64 throughput is per SM
 constexpr int SVD_MAX_SWEEPS = 60;
 
 __global__ void __launch_bounds__(SVD_NT) svd_rotate_kernel(int p, int q, double* M, double* V,
-                                                            int* counters, int* status) {
+                                                            int* counters, int* status,
+                                                            int init_v) {
   cg::grid_group grid = cg::this_grid();
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * SVD_NT + threadIdx.x) >> 5;
@@ -335,9 +336,10 @@ __global__ void __launch_bounds__(SVD_NT) svd_rotate_kernel(int p, int q, double
   const int K = (q + 1) & ~1;
   const int npairs = K / 2;
   const double tol = sqrt((double)p) * DBL_EPSILON;
-  // V = I
-  for (i64 e = blockIdx.x * (i64)SVD_NT + threadIdx.x; e < (i64)q * q; e += (i64)gridDim.x * SVD_NT)
-    V[e] = (e % q == e / q) ? 1.0 : 0.0;
+  // V = I, unless the FP32 pre-sweeps already supplied the rotation
+  if (!init_v)
+    for (i64 e = blockIdx.x * (i64)SVD_NT + threadIdx.x; e < (i64)q * q; e += (i64)gridDim.x * SVD_NT)
+      V[e] = (e % q == e / q) ? 1.0 : 0.0;
   if (blockIdx.x == 0 && threadIdx.x == 0) { counters[0] = 0; counters[1] = 0; }
   grid.sync();
   int sweep = 0;
@@ -386,6 +388,85 @@ __global__ void __launch_bounds__(SVD_NT) svd_rotate_kernel(int p, int q, double
   if (blockIdx.x == 0 && threadIdx.x == 0 && status) *status = sweep;
 }
 
+// FP32 pre-sweeps of the one-sided Jacobi SVD, one CTA with M (p x q) and the
+// accumulated rotation V (q x q) in shared memory.  FP32 runs at 64 times
+// the FP64 rate of a GB300 SM, so the sweeps that take the columns from
+// arbitrary to nearly orthogonal are cheap here; the FP64 sweeps that follow
+// (svd_rotate_kernel, started from V) only polish.  V is written as FP64.
+constexpr int SVD32_NT = 1024;
+constexpr int SVD32_MAX_SWEEPS = 20;
+constexpr size_t SVD32_SMEM = 227 * 1024 - 1024;
+
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__global__ void __launch_bounds__(SVD32_NT) svd_pre32_kernel(int p, int q, const double* __restrict__ M,
+                                                             double* __restrict__ Vout, int* status) {
+  extern __shared__ float sm32[];
+  float* A = sm32;                       // p x q
+  float* W = sm32 + (size_t)p * q;       // q x q
+  __shared__ int rot;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = SVD32_NT >> 5;
+  for (int e = tid; e < p * q; e += SVD32_NT) A[e] = (float)M[e];
+  for (int e = tid; e < q * q; e += SVD32_NT) W[e] = (e % q == e / q) ? 1.f : 0.f;
+  const int K = (q + 1) & ~1;
+  const int npairs = K / 2;
+  const float tol = sqrtf((float)p) * FLT_EPSILON;
+  int sweep = 0;
+  for (sweep = 0; sweep < SVD32_MAX_SWEEPS; ++sweep) {
+    if (tid == 0) rot = 0;
+    __syncthreads();
+    for (int r = 0; r < K - 1; ++r) {
+      for (int pi = warp; pi < npairs; pi += nwarp) {
+        int a, b;
+        rr_pair(K, r, pi, a, b);
+        if (a >= q || b >= q) continue;
+        float* ca = A + (size_t)p * a;
+        float* cb = A + (size_t)p * b;
+        float al = 0.f, be = 0.f, ga = 0.f;
+        for (int i = lane; i < p; i += 32) {
+          const float x = ca[i], y = cb[i];
+          al = fmaf(x, x, al); be = fmaf(y, y, be); ga = fmaf(x, y, ga);
+        }
+        al = warp_sumf(al); be = warp_sumf(be); ga = warp_sumf(ga);
+        if (ga == 0.f || !(fabsf(ga) > tol * sqrtf(al * be))) continue;
+        const float zeta = (be - al) / (2.f * ga);
+        const float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+        const float c = 1.f / sqrtf(1.f + t * t);
+        const float sn = c * t;
+        for (int i = lane; i < p; i += 32) {
+          const float x = ca[i], y = cb[i];
+          ca[i] = c * x - sn * y;
+          cb[i] = sn * x + c * y;
+        }
+        float* wa = W + (size_t)q * a;
+        float* wb = W + (size_t)q * b;
+        for (int i = lane; i < q; i += 32) {
+          const float x = wa[i], y = wb[i];
+          wa[i] = c * x - sn * y;
+          wb[i] = sn * x + c * y;
+        }
+        if (lane == 0) atomicAdd(&rot, 1);
+      }
+      __syncthreads();
+    }
+    const int done = rot == 0;
+    __syncthreads();
+    if (done) break;
+  }
+  for (int e = tid; e < q * q; e += SVD32_NT) Vout[e] = (double)W[e];
+  if (tid == 0 && status) *status = sweep;
+}
+
+// Z = 1.5 I - 0.5 Y (one Newton-Schulz step toward the orthogonal factor)
+__global__ void ns_coef_kernel(int q, const double* __restrict__ Y, double* __restrict__ Z) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < q * q; e += gridDim.x * blockDim.x)
+    Z[e] = (e % q == e / q ? 1.5 : 0.0) - 0.5 * Y[e];
+}
+
 // sigma_j = ||M_j||, rank sort descending, write U (normalised), sigma, Vt
 __global__ void svd_finish_kernel(int p, int q, const double* M, const double* V, double* U,
                                   double* sigma, double* Vt, double* nrm, int* rank) {
@@ -430,15 +511,55 @@ __global__ void svd_gather_kernel(int p, int q, const double* M, const double* V
 }
 
 size_t svd_scratch(int p, int q) {
-  // working copy of M (max(p,q) x min(p,q)), V (min^2), norms, ranks, counters, Ut
+  // working copy of M (max(p,q) x min(p,q)), V (min^2), norms, ranks, counters, Ut,
+  // and for the FP32 pre-sweeps two min^2 and one max x min temporaries
   size_t pp = std::max(p, q), qq = std::min(p, q);
-  return (pp * qq + qq * qq + 2 * qq + 64) * sizeof(double) + pp * qq * sizeof(double);
+  return (pp * qq + qq * qq + 2 * qq + 64) * sizeof(double) + pp * qq * sizeof(double) +
+         (2 * qq * qq + pp * qq) * sizeof(double);
 }
 
 static void svd_tall(int p, int q, double* Mw, double* U, double* sigma, double* Vt,
                      double* V, double* nrm, int* rank, int* counters, int* status,
-                     cudaStream_t s) {
-  // Mw (p x q, p >= q) is overwritten
+                     double* tmp, cudaStream_t s) {
+  // Mw (p x q, p >= q) is overwritten.  tmp: 2 q^2 + p q doubles.
+  int init_v = 0;
+  const size_t smem32 = ((size_t)p * q + (size_t)q * q) * sizeof(float);
+  if (q >= 8 && smem32 <= SVD32_SMEM) {
+    static const cudaError_t attr_rc = cudaFuncSetAttribute(
+        svd_pre32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SVD32_SMEM);
+    TTG_CUDA(attr_rc);
+    svd_pre32_kernel<<<1, SVD32_NT, smem32, s>>>(p, q, Mw, V, status);
+    TTG_CHECK_LAUNCH();
+    // make V orthogonal to FP64 precision: V <- V (1.5 I - 0.5 V^T V), twice
+    double* Y = tmp;
+    double* Z = tmp + (size_t)q * q;
+    double* W = tmp + 2 * (size_t)q * q;
+    for (int it = 0; it < 2; ++it) {
+      GemmF64 g;   // Y = V^T V
+      g.M = q; g.N = q; g.K = q;
+      g.A = V; g.sAm = q; g.sAk = 1;
+      g.B = V; g.sBk = 1; g.sBn = q;
+      g.C = Y; g.sCm = 1; g.sCn = q;
+      gemm_f64(g, s);
+      ns_coef_kernel<<<ceil_div((i64)q * q, 256), 256, 0, s>>>(q, Y, Z);
+      TTG_CHECK_LAUNCH();
+      GemmF64 h;   // W = V Z, then V = W
+      h.M = q; h.N = q; h.K = q;
+      h.A = V; h.sAm = 1; h.sAk = q;
+      h.B = Z; h.sBk = 1; h.sBn = q;
+      h.C = W; h.sCm = 1; h.sCn = q;
+      gemm_f64(h, s);
+      TTG_CUDA(cudaMemcpyAsync(V, W, sizeof(double) * q * q, cudaMemcpyDeviceToDevice, s));
+    }
+    GemmF64 m;   // W = Mw V (p x q), then Mw = W
+    m.M = p; m.N = q; m.K = q;
+    m.A = Mw; m.sAm = 1; m.sAk = p;
+    m.B = V; m.sBk = 1; m.sBn = q;
+    m.C = W; m.sCm = 1; m.sCn = p;
+    gemm_f64(m, s);
+    TTG_CUDA(cudaMemcpyAsync(Mw, W, sizeof(double) * p * q, cudaMemcpyDeviceToDevice, s));
+    init_v = 1;
+  }
   int npairs = (q + 1) / 2;
   int blocks = std::max(1, npairs);
   static const int max_coop = [] {
@@ -452,7 +573,7 @@ static void svd_tall(int p, int q, double* Mw, double* U, double* sigma, double*
   }();
   TTG_REQUIRE(max_coop > 0, "svd: occupancy query failed");
   blocks = std::min(blocks, max_coop);
-  void* args[] = {&p, &q, &Mw, &V, &counters, &status};
+  void* args[] = {&p, &q, &Mw, &V, &counters, &status, &init_v};
   TTG_CUDA(cudaLaunchCooperativeKernel((void*)svd_rotate_kernel, dim3(blocks), dim3(SVD_NT),
                                        args, 0, s));
   ++g_launches;
@@ -478,15 +599,16 @@ void svd_jacobi(int p, int q, const double* M, double* U, double* sigma, double*
   int* rank = (int*)(nrm + r);                            // r ints (<= r doubles)
   int* counters = (int*)(nrm + 2 * r);                    // 2 ints
   double* T = nrm + 2 * r + 64;                           // max x min (for p < q)
+  double* tmp = T + (size_t)std::max(p, q) * r;           // 2 min^2 + max x min
   if (p >= q) {
     TTG_CUDA(cudaMemcpyAsync(Mw, M, sizeof(double) * (size_t)p * q, cudaMemcpyDeviceToDevice, s));
-    svd_tall(p, q, Mw, U, sigma, Vt, V, nrm, rank, counters, status, s);
+    svd_tall(p, q, Mw, U, sigma, Vt, V, nrm, rank, counters, status, tmp, s);
   } else {
     // M^T = V S U^T: run on the q x p transpose, then U_M = Vt_T^T, Vt_M = U_T^T
     transpose_f64(p, q, M, Mw, s);                        // Mw: q x p
     double* UT = T;                                       // q x p   (left vectors of M^T)
     double* VtT = U;                                      // p x p   written into U's storage
-    svd_tall(q, p, Mw, UT, sigma, VtT, V, nrm, rank, counters, status, s);
+    svd_tall(q, p, Mw, UT, sigma, VtT, V, nrm, rank, counters, status, tmp, s);
     // U (p x p) = VtT^T ; VtT currently occupies U: transpose through Mw
     TTG_CUDA(cudaMemcpyAsync(Mw, VtT, sizeof(double) * (size_t)p * p, cudaMemcpyDeviceToDevice, s));
     transpose_f64(p, p, Mw, U, s);
