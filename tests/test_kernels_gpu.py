@@ -195,7 +195,8 @@ def test_dsyev_jacobi(torch_cuda, ctx, k):
     assert np.linalg.norm(V.T @ V - np.eye(k)) < 1e-12 * k
 
 
-@pytest.mark.parametrize("pq", [(320, 128), (128, 320), (40, 40), (7, 3), (3, 7), (640, 256)])
+@pytest.mark.parametrize("pq", [(320, 128), (128, 320), (40, 40), (7, 3), (3, 7), (640, 256),
+                                (2048, 512), (300, 900)])
 def test_dgesvd_jacobi(torch_cuda, ctx, pq):
     import ttgpu
     torch = torch_cuda

@@ -323,69 +323,131 @@ void syev_jacobi(int k, double* A, int lda, double* w, double* V, int ldv, int* 
 // ---------------------------------------------------------------------------
 // one-sided Jacobi SVD (cooperative launch, grid barrier between rounds)
 // ---------------------------------------------------------------------------
-constexpr int SVD_NT = 32;   // one warp per CTA: FP64 throughput is per SM
+constexpr int SVD_CT = 128;   // one CTA per column pair: four warps share its rows
 constexpr int SVD_MAX_SWEEPS = 60;
 
-__global__ void __launch_bounds__(SVD_NT) svd_rotate_kernel(int p, int q, double* M, double* V,
-                                                            int* counters, int* status,
-                                                            int init_v) {
+template <class T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// One-sided Jacobi sweeps over the column pairs of M (p x q), rotations
+// accumulated in V (q x q).  Cooperative launch: a round of disjoint pairs
+// (round-robin ordering) per grid barrier, one CTA per pair whose four warps
+// split the rows (so all four FP64 pipes of an SM work on it).  T = float
+// gives the cheap pre-sweeps of large matrices, T = double the polish.
+template <class T>
+__global__ void __launch_bounds__(SVD_CT) svd_sweep_kernel(int p, int q, T* M, T* V,
+                                                           int* counters, int* status, int init_v,
+                                                           T tol, int max_sweeps) {
   cg::grid_group grid = cg::this_grid();
-  const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * SVD_NT + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * SVD_NT) >> 5;
+  __shared__ T red[3][SVD_CT / 32];
+  __shared__ T csn[2];
+  __shared__ int act;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int K = (q + 1) & ~1;
   const int npairs = K / 2;
-  const double tol = sqrt((double)p) * DBL_EPSILON;
-  // V = I, unless the FP32 pre-sweeps already supplied the rotation
+  // V = I, unless the pre-sweeps already supplied the rotation
   if (!init_v)
-    for (i64 e = blockIdx.x * (i64)SVD_NT + threadIdx.x; e < (i64)q * q; e += (i64)gridDim.x * SVD_NT)
-      V[e] = (e % q == e / q) ? 1.0 : 0.0;
-  if (blockIdx.x == 0 && threadIdx.x == 0) { counters[0] = 0; counters[1] = 0; }
+    for (i64 e = blockIdx.x * (i64)SVD_CT + tid; e < (i64)q * q; e += (i64)gridDim.x * SVD_CT)
+      V[e] = (e % q == e / q) ? T(1) : T(0);
+  if (blockIdx.x == 0 && tid == 0) { counters[0] = 0; counters[1] = 0; }
   grid.sync();
   int sweep = 0;
-  for (sweep = 0; sweep < SVD_MAX_SWEEPS; ++sweep) {
+  for (sweep = 0; sweep < max_sweeps; ++sweep) {
     int* cnt = counters + (sweep & 1);
     for (int r = 0; r < K - 1; ++r) {
-      for (int pi = gw; pi < npairs; pi += nw) {
+      for (int pi = blockIdx.x; pi < npairs; pi += gridDim.x) {
         int a, b;
         rr_pair(K, r, pi, a, b);
         if (a >= q || b >= q) continue;
-        double* ca = M + (i64)p * a;
-        double* cb = M + (i64)p * b;
-        double al = 0.0, be = 0.0, ga = 0.0;
-        for (int i = lane; i < p; i += 32) {
-          double x = ca[i], y = cb[i];
+        T* ca = M + (i64)p * a;
+        T* cb = M + (i64)p * b;
+        T al = 0, be = 0, ga = 0;
+        for (int i = tid; i < p; i += SVD_CT) {
+          const T x = ca[i], y = cb[i];
           al = fma(x, x, al); be = fma(y, y, be); ga = fma(x, y, ga);
         }
-        al = warp_sum(al); be = warp_sum(be); ga = warp_sum(ga);
-        if (ga == 0.0 || !(fabs(ga) > tol * sqrt(al * be))) continue;
-        double zeta = (be - al) / (2.0 * ga);
-        double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        double c = 1.0 / sqrt(1.0 + t * t);
-        double s = c * t;
-        for (int i = lane; i < p; i += 32) {
-          double x = ca[i], y = cb[i];
-          ca[i] = c * x - s * y;
-          cb[i] = s * x + c * y;
+        al = warp_sum_t(al); be = warp_sum_t(be); ga = warp_sum_t(ga);
+        if (lane == 0) { red[0][warp] = al; red[1][warp] = be; red[2][warp] = ga; }
+        __syncthreads();
+        if (tid == 0) {
+          T A = 0, Bv = 0, G = 0;
+          for (int w = 0; w < SVD_CT / 32; ++w) { A += red[0][w]; Bv += red[1][w]; G += red[2][w]; }
+          int go = (G != T(0)) && (fabs(G) > tol * sqrt(A * Bv));
+          if (go) {
+            const T zeta = (Bv - A) / (T(2) * G);
+            const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+            const T c = T(1) / sqrt(T(1) + t * t);
+            csn[0] = c;
+            csn[1] = c * t;
+            atomicAdd(cnt, 1);
+          }
+          act = go;
         }
-        double* va = V + (i64)q * a;
-        double* vb = V + (i64)q * b;
-        for (int i = lane; i < q; i += 32) {
-          double x = va[i], y = vb[i];
-          va[i] = c * x - s * y;
-          vb[i] = s * x + c * y;
+        __syncthreads();
+        if (act) {
+          const T c = csn[0], sn = csn[1];
+          for (int i = tid; i < p; i += SVD_CT) {
+            const T x = ca[i], y = cb[i];
+            ca[i] = c * x - sn * y;
+            cb[i] = sn * x + c * y;
+          }
+          T* va = V + (i64)q * a;
+          T* vb = V + (i64)q * b;
+          for (int i = tid; i < q; i += SVD_CT) {
+            const T x = va[i], y = vb[i];
+            va[i] = c * x - sn * y;
+            vb[i] = sn * x + c * y;
+          }
         }
-        if (lane == 0) atomicAdd(cnt, 1);
+        __syncthreads();
       }
       grid.sync();
     }
     int done = (*((volatile int*)cnt) == 0);
     grid.sync();
-    if (blockIdx.x == 0 && threadIdx.x == 0) counters[(sweep + 1) & 1] = 0;
+    if (blockIdx.x == 0 && tid == 0) counters[(sweep + 1) & 1] = 0;
     grid.sync();
     if (done) break;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0 && status) *status = sweep;
+  if (blockIdx.x == 0 && tid == 0 && status) *status = sweep;
+}
+
+__global__ void d2f_kernel(i64 n, const double* __restrict__ a, float* __restrict__ b) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x)
+    b[e] = (float)a[e];
+}
+__global__ void f2d_kernel(i64 n, const float* __restrict__ a, double* __restrict__ b) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x)
+    b[e] = (double)a[e];
+}
+
+template <class T>
+static int svd_coop_blocks() {
+  static const int max_coop = [] {
+    int dev = 0, nsm = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, svd_sweep_kernel<T>, SVD_CT, 0) !=
+            cudaSuccess)
+      return 0;
+    return nsm * per;
+  }();
+  TTG_REQUIRE(max_coop > 0, "svd: occupancy query failed");
+  return max_coop;
+}
+
+template <class T>
+static void svd_sweeps(int p, int q, T* M, T* V, int* counters, int* status, int init_v, T tol,
+                       int max_sweeps, cudaStream_t s) {
+  int blocks = std::max(1, std::min((q + 1) / 2, svd_coop_blocks<T>()));
+  void* args[] = {&p, &q, &M, &V, &counters, &status, &init_v, &tol, &max_sweeps};
+  TTG_CUDA(cudaLaunchCooperativeKernel((void*)svd_sweep_kernel<T>, dim3(blocks), dim3(SVD_CT),
+                                       args, 0, s));
+  ++g_launches;
 }
 
 // FP32 pre-sweeps of the one-sided Jacobi SVD, one CTA with M (p x q) and the
@@ -523,17 +585,29 @@ static void svd_tall(int p, int q, double* Mw, double* U, double* sigma, double*
                      double* tmp, cudaStream_t s) {
   // Mw (p x q, p >= q) is overwritten.  tmp: 2 q^2 + p q doubles.
   int init_v = 0;
+  double* Y = tmp;
+  double* Z = tmp + (size_t)q * q;
+  double* W = tmp + 2 * (size_t)q * q;
   const size_t smem32 = ((size_t)p * q + (size_t)q * q) * sizeof(float);
-  if (q >= 8 && smem32 <= SVD32_SMEM) {
-    static const cudaError_t attr_rc = cudaFuncSetAttribute(
-        svd_pre32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SVD32_SMEM);
-    TTG_CUDA(attr_rc);
-    svd_pre32_kernel<<<1, SVD32_NT, smem32, s>>>(p, q, Mw, V, status);
-    TTG_CHECK_LAUNCH();
+  if (q >= 8) {
+    if (smem32 <= SVD32_SMEM) {
+      // FP32 pre-sweeps in one CTA's shared memory
+      static const cudaError_t attr_rc = cudaFuncSetAttribute(
+          svd_pre32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SVD32_SMEM);
+      TTG_CUDA(attr_rc);
+      svd_pre32_kernel<<<1, SVD32_NT, smem32, s>>>(p, q, Mw, V, status);
+      TTG_CHECK_LAUNCH();
+    } else {
+      // FP32 pre-sweeps over the whole grid: M32 in W's space, V32 in Y's
+      float* M32 = (float*)W;
+      float* V32 = (float*)Y;
+      d2f_kernel<<<(int)std::min<i64>(4096, ((i64)p * q + 255) / 256), 256, 0, s>>>((i64)p * q, Mw, M32);
+      TTG_CHECK_LAUNCH();
+      svd_sweeps<float>(p, q, M32, V32, counters, status, 0, sqrtf((float)p) * FLT_EPSILON, 30, s);
+      f2d_kernel<<<(int)std::min<i64>(4096, ((i64)q * q + 255) / 256), 256, 0, s>>>((i64)q * q, V32, V);
+      TTG_CHECK_LAUNCH();
+    }
     // make V orthogonal to FP64 precision: V <- V (1.5 I - 0.5 V^T V), twice
-    double* Y = tmp;
-    double* Z = tmp + (size_t)q * q;
-    double* W = tmp + 2 * (size_t)q * q;
     for (int it = 0; it < 2; ++it) {
       GemmF64 g;   // Y = V^T V
       g.M = q; g.N = q; g.K = q;
@@ -560,23 +634,8 @@ static void svd_tall(int p, int q, double* Mw, double* U, double* sigma, double*
     TTG_CUDA(cudaMemcpyAsync(Mw, W, sizeof(double) * p * q, cudaMemcpyDeviceToDevice, s));
     init_v = 1;
   }
-  int npairs = (q + 1) / 2;
-  int blocks = std::max(1, npairs);
-  static const int max_coop = [] {
-    int dev = 0, nsm = 0, per = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, svd_rotate_kernel, SVD_NT, 0) !=
-            cudaSuccess)
-      return 0;
-    return nsm * per;
-  }();
-  TTG_REQUIRE(max_coop > 0, "svd: occupancy query failed");
-  blocks = std::min(blocks, max_coop);
-  void* args[] = {&p, &q, &Mw, &V, &counters, &status, &init_v};
-  TTG_CUDA(cudaLaunchCooperativeKernel((void*)svd_rotate_kernel, dim3(blocks), dim3(SVD_NT),
-                                       args, 0, s));
-  ++g_launches;
+  svd_sweeps<double>(p, q, Mw, V, counters, status, init_v, sqrt((double)p) * DBL_EPSILON,
+                     SVD_MAX_SWEEPS, s);
   int nb = std::max(1, std::min(1024, ceil_div((i64)q * 32, 256)));
   svd_finish_kernel<<<nb, 256, 0, s>>>(p, q, Mw, V, U, sigma, Vt, nrm, rank);
   TTG_CHECK_LAUNCH();
