@@ -341,7 +341,7 @@ __device__ __forceinline__ T warp_sum_t(T v) {
 template <class T>
 __global__ void __launch_bounds__(SVD_CT) svd_sweep_kernel(int p, int q, T* M, T* V,
                                                            int* counters, int* status, int init_v,
-                                                           T tol, int max_sweeps) {
+                                                           T tol, T tol_count, int max_sweeps) {
   cg::grid_group grid = cg::this_grid();
   __shared__ T red[3][SVD_CT / 32];
   __shared__ T csn[2];
@@ -376,14 +376,17 @@ __global__ void __launch_bounds__(SVD_CT) svd_sweep_kernel(int p, int q, T* M, T
         if (tid == 0) {
           T A = 0, Bv = 0, G = 0;
           for (int w = 0; w < SVD_CT / 32; ++w) { A += red[0][w]; Bv += red[1][w]; G += red[2][w]; }
-          int go = (G != T(0)) && (fabs(G) > tol * sqrt(A * Bv));
+          const T nab = sqrt(A * Bv);
+          int go = (G != T(0)) && (fabs(G) > tol * nab);
           if (go) {
             const T zeta = (Bv - A) / (T(2) * G);
             const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
             const T c = T(1) / sqrt(T(1) + t * t);
             csn[0] = c;
             csn[1] = c * t;
-            atomicAdd(cnt, 1);
+            // rotations whose cosine is within the rounding noise of a dot
+            // product of length p are applied but do not keep the sweeps going
+            if (fabs(G) > tol_count * nab) atomicAdd(cnt, 1);
           }
           act = go;
         }
@@ -442,9 +445,9 @@ static int svd_coop_blocks() {
 
 template <class T>
 static void svd_sweeps(int p, int q, T* M, T* V, int* counters, int* status, int init_v, T tol,
-                       int max_sweeps, cudaStream_t s) {
+                       T tol_count, int max_sweeps, cudaStream_t s) {
   int blocks = std::max(1, std::min((q + 1) / 2, svd_coop_blocks<T>()));
-  void* args[] = {&p, &q, &M, &V, &counters, &status, &init_v, &tol, &max_sweeps};
+  void* args[] = {&p, &q, &M, &V, &counters, &status, &init_v, &tol, &tol_count, &max_sweeps};
   TTG_CUDA(cudaLaunchCooperativeKernel((void*)svd_sweep_kernel<T>, dim3(blocks), dim3(SVD_CT),
                                        args, 0, s));
   ++g_launches;
@@ -603,7 +606,8 @@ static void svd_tall(int p, int q, double* Mw, double* U, double* sigma, double*
       float* V32 = (float*)Y;
       d2f_kernel<<<(int)std::min<i64>(4096, ((i64)p * q + 255) / 256), 256, 0, s>>>((i64)p * q, Mw, M32);
       TTG_CHECK_LAUNCH();
-      svd_sweeps<float>(p, q, M32, V32, counters, status, 0, sqrtf((float)p) * FLT_EPSILON, 30, s);
+      svd_sweeps<float>(p, q, M32, V32, counters, status, 0, sqrtf((float)p) * FLT_EPSILON,
+                        (float)p * FLT_EPSILON, 30, s);
       f2d_kernel<<<(int)std::min<i64>(4096, ((i64)q * q + 255) / 256), 256, 0, s>>>((i64)q * q, V32, V);
       TTG_CHECK_LAUNCH();
     }
@@ -635,7 +639,7 @@ static void svd_tall(int p, int q, double* Mw, double* U, double* sigma, double*
     init_v = 1;
   }
   svd_sweeps<double>(p, q, Mw, V, counters, status, init_v, sqrt((double)p) * DBL_EPSILON,
-                     SVD_MAX_SWEEPS, s);
+                     (double)p * DBL_EPSILON, SVD_MAX_SWEEPS, s);
   int nb = std::max(1, std::min(1024, ceil_div((i64)q * 32, 256)));
   svd_finish_kernel<<<nb, 256, 0, s>>>(p, q, Mw, V, U, sigma, Vt, nrm, rank);
   TTG_CHECK_LAUNCH();
