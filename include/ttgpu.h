@@ -221,7 +221,9 @@ int ttg_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
                    int method);
 /* AMEn of ttamen.f90 (dtt_amen_solve, ttamen.f90:29-252) with the packed
  * cores of the arguments above in place of the dtt type; rmax caps the
- * ranks (<= 0: no cap). */
+ * ranks (<= 0: no cap).  method TTG_METHOD_SPLIT runs the local GMRES on the
+ * BF16x3 tensor-core operator inside FP64 iterative refinement; the FP64
+ * residual is the stopping test in both methods. */
 int ttg_dtt_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
                        const ttg_int* ry, const ttg_int* ra, const double* crA,
                        const double* crY, const double* crX0, ttg_int* rx, double eps,

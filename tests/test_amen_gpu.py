@@ -47,6 +47,27 @@ def test_amen_dense_check(ctx, d, n, ryr, rxr):
     assert np.linalg.norm(xf - xo) <= 1e-8 * np.linalg.norm(xo)
 
 
+@pytest.mark.parametrize("d,n,ryr,rxr", [(4, 8, 2, 2), (5, 6, 3, 2), (3, 16, 2, 3)])
+def test_amen_chosen_dense_check(ctx, d, n, ryr, rxr):
+    """Chosen form (split-precision GMRES inside FP64 iterative refinement):
+    the FP64 residual against the dense operator meets the same tolerance,
+    and the solution equals the oracle's to 1e-8."""
+    import ttgpu
+    tol = 1e-9
+    nn, mm, ra, crA = amen_operator(d=d, n=n)
+    _, ry, y = random_tt(d, n, ryr, seed=3)
+    _, rx, x0 = random_tt(d, n, rxr, seed=7)
+    cores, rx1 = ttgpu.dtt_amen_solve(d, nn, mm, ry, ra, crA, y, x0, rx, tol, method="split",
+                                      ctx=ctx)
+    A = tt_matrix_full(d, nn, ra, crA)
+    yf = tt_full(d, nn, ry, y)
+    xf = tt_full(d, nn, rx1, cores)
+    assert np.linalg.norm(A @ xf - yf) <= tol * np.linalg.norm(yf)
+    ref = oracle_amen(d, nn, ra, crA, ry, y, rx, x0, tol)
+    xo = tt_full(d, nn, ref["rx"], ref["cores"])
+    assert np.linalg.norm(xf - xo) <= 1e-8 * np.linalg.norm(xo)
+
+
 def test_amen_workload_family(ctx):
     """Laplacian + Gaussian potential (rank 3), rhs rank 4, d=6, n=16: the
     reference's algorithm needs many sweeps here (GMRES(40) x 2 without a

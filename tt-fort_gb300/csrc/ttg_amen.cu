@@ -313,6 +313,11 @@ void gmres_cgs2(const MV& mv, i64 N, const double* b, double* x, double tol, int
 
 }  // namespace
 
+void split_matvec_factory(const LocalDims& L, const double* phi1, const double* A,
+                          const double* phi2, int nvec_max, void* mem, cudaStream_t s,
+                          MatvecFn* out);
+size_t split_matvec_bytes(const LocalDims& L, int nvec_max);
+
 struct AmenParams {
   int d;
   std::vector<i64> n, ra, ry, rx;
@@ -321,6 +326,7 @@ struct AmenParams {
   i64 rmax;
   int kick, nswp, local_iters, local_restart, max_full_size, verb;
   unsigned long long seed;
+  int method = TTG_METHOD_PLAIN;
 };
 
 struct AmenOut {
@@ -384,6 +390,10 @@ class AmenSolver {
     nmv_ += nvec;
   }
   void gmres(const LocalDims& L, int k, const double* b, double* x, double tol);
+  void gmres_split(const LocalDims& L, int k, const double* b, double* x, double tol);
+  void* split_mem_ = nullptr;
+  double *ir_r_ = nullptr, *ir_d_ = nullptr;
+  long long split_mv_ = 0;
   void trunc(int k, double tol, const double* rhs, double rhs_norm);
 };
 
@@ -448,12 +458,43 @@ void AmenSolver::project_y(const double* pl, const double* pr, i64 rl, i64 rr, i
 // GMRES(local_restart) x local_iters for L x = b (x0 = 0), relative tolerance
 // against ||b||.
 void AmenSolver::gmres(const LocalDims& L, int k, const double* b, double* x, double tol) {
+  if (P_.method == TTG_METHOD_SPLIT) { gmres_split(L, k, b, x, tol); return; }
   const i64 N = L.xsize();
   const int nr = (int)std::min<i64>(std::min<i64>(N, P_.local_restart), 60);
   const double* p1 = pxax_[k];
   const double* p2 = pxax_[k + 1];
   auto mv = [&](const double* in, double* out, int nv) { local_mv(L, p1, p2, k, in, out, nv); };
   gmres_cgs2(mv, N, b, x, tol, nr, P_.local_iters, GmresBufs{V_, w_, gm_, red_, h_}, s_);
+}
+
+
+// Chosen form of the local solve: iterative refinement in FP64 around GMRES
+// on the BF16x3 tensor-core operator.  Each pass solves A~ d = r (r the FP64
+// residual) to the relative accuracy the split operator can carry (1e-4, or
+// less when the target is closer), adds d, and recomputes the FP64
+// residual; the target tol is the one the plain GMRES is given, measured in
+// FP64.
+void AmenSolver::gmres_split(const LocalDims& L, int k, const double* b, double* x, double tol) {
+  const i64 N = L.xsize();
+  const int nr = (int)std::min<i64>(std::min<i64>(N, P_.local_restart), 60);
+  MatvecFn mvlow;
+  split_matvec_factory(L, pxax_[k], A_[k], pxax_[k + 1], kBatch, split_mem_, s_, &mvlow);
+  auto mvs = [&](const double* in, double* out, int nv) { mvlow(in, out, nv); split_mv_ += nv; };
+  const GmresBufs G{V_, w_, gm_, red_, h_};
+  const double nb = norm2(b, N);
+  TTG_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * N, s_));
+  TTG_CUDA(cudaMemcpyAsync(ir_r_, b, sizeof(double) * N, cudaMemcpyDeviceToDevice, s_));
+  double nrr = nb;
+  for (int it = 0; it < 8 && nrr > tol * nb; ++it) {
+    const double inner = std::max(tol * nb / nrr, 1e-4);
+    gmres_cgs2(mvs, N, ir_r_, ir_d_, inner, nr, P_.local_iters, G, s_);
+    axpy_kernel<<<eb(N), 256, 0, s_>>>(N, 1.0, ir_d_, x);
+    TTG_CHECK_LAUNCH();
+    local_mv(L, pxax_[k], pxax_[k + 1], k, x, ir_r_, 1);        // FP64 residual b - A x
+    sub_kernel<<<eb(N), 256, 0, s_>>>(N, b, ir_r_, ir_r_);
+    TTG_CHECK_LAUNCH();
+    nrr = norm2(ir_r_, N);
+  }
 }
 
 // dtt_trunc dir=+1 with the residual criterion (ttnodeop.f90:227-302)
@@ -470,16 +511,34 @@ void AmenSolver::trunc(int k, double tol, const double* rhs, double rhs_norm) {
   const i64 N = L.xsize();
   int rnew = rmin - 1;
   int fail = 0;   // largest candidate rank whose residual exceeds tol (0: none)
+  MatvecFn mvlow;
+  if (P_.method == TTG_METHOD_SPLIT)
+    split_matvec_factory(L, pxax_[k], A_[k], pxax_[k + 1], kBatch, split_mem_, s_, &mvlow);
   while (rnew >= 1 && !fail) {
     const int cnt = std::min(kBatch, rnew);
-    // candidates rank rnew, rnew-1, ..., rnew-cnt+1: core_c = U[:, :rc] W[:rc, :]
-    for (int c = 0; c < cnt; ++c) {
-      const int rc = rnew - c;
-      gemm((int)m, (int)rr, rc, svU_, 1, m, svVt_, 1, rmin, cand_ + N * c, 1, m);
+    if (P_.method == TTG_METHOD_SPLIT) {
+      // A x_c - rhs = (A x - rhs) - A (x - x_c): the first term is the FP64
+      // residual of the full core (resid_), the second the discarded part
+      // U[:, rc:] W[rc:, :] through the split operator, whose relative error
+      // is then relative to the candidate's own residual
+      for (int c = 0; c < cnt; ++c) {
+        const int rc = rnew - c;
+        gemm((int)m, (int)rr, rmin - rc, svU_ + m * rc, 1, m, svVt_ + rc, 1, rmin, cand_ + N * c, 1, m);
+      }
+      mvlow(cand_, candY_, cnt);
+      split_mv_ += cnt;
+      sub_cols_kernel<<<eb(N * cnt), 256, 0, s_>>>(N, cnt, candY_, resid_, candY_);
+      TTG_CHECK_LAUNCH();
+    } else {
+      // candidates rank rnew, rnew-1, ..., rnew-cnt+1: core_c = U[:, :rc] W[:rc, :]
+      for (int c = 0; c < cnt; ++c) {
+        const int rc = rnew - c;
+        gemm((int)m, (int)rr, rc, svU_, 1, m, svVt_, 1, rmin, cand_ + N * c, 1, m);
+      }
+      local_mv(L, pxax_[k], pxax_[k + 1], k, cand_, candY_, cnt);
+      sub_cols_kernel<<<eb(N * cnt), 256, 0, s_>>>(N, cnt, candY_, rhs, candY_);
+      TTG_CHECK_LAUNCH();
     }
-    local_mv(L, pxax_[k], pxax_[k + 1], k, cand_, candY_, cnt);
-    sub_cols_kernel<<<eb(N * cnt), 256, 0, s_>>>(N, cnt, candY_, rhs, candY_);
-    TTG_CHECK_LAUNCH();
     TTG_CUDA(cudaMemsetAsync(red_, 0, sizeof(double) * cnt, s_));
     int bx = (int)std::max<i64>(1, std::min<i64>(128, (N + 2047) / 2048));
     sqnorm_cols_kernel<<<dim3(bx, cnt), 256, 0, s_>>>(N, candY_, N, red_);
@@ -560,6 +619,15 @@ void AmenSolver::run(AmenOut& out) {
   total += svds + 256 + 3 * al8(cmax) + al8(8192);
   total += 2 * al8(Nmax * kBatch) + al8(Nmax * (nr + 1)) + al8(Nmax) + al8(4096) +
            al8((size_t)std::min<i64>(P_.max_full_size, 64) * 64) + (1 << 16);
+  size_t splitb = 0;
+  if (P_.method == TTG_METHOD_SPLIT) {
+    for (int k = 0; k < d; ++k) {
+      LocalDims L{x_.cap[k], n[k], x_.cap[k + 1], x_.cap[k], n[k], x_.cap[k + 1], P_.ra[k], P_.ra[k + 1]};
+      TTG_REQUIRE(split_op_supported(L), "amen: local problem too large for the split operator");
+      splitb = std::max(splitb, split_matvec_bytes(L, kBatch));
+    }
+    total += splitb + 1024 + 2 * al8(Nmax);
+  }
   mem_.alloc(total);
   double* dA = mem_.take(at);
   A_.resize(d);
@@ -593,6 +661,11 @@ void AmenSolver::run(AmenOut& out) {
   red_ = mem_.take(64);
   gm_ = mem_.take(4096);
   dense_ = mem_.take(64 * 64);
+  if (P_.method == TTG_METHOD_SPLIT) {
+    split_mem_ = (void*)mem_.take(splitb / sizeof(double) + 128);
+    ir_r_ = mem_.take(Nmax);
+    ir_d_ = mem_.take(Nmax);
+  }
   TTG_CUDA(cudaMallocHost(&h_, 4096 * sizeof(double)));
   struct HG { double* p; ~HG() { if (p) cudaFreeHost(p); } } hg{h_};
 
@@ -732,7 +805,7 @@ void AmenSolver::run(AmenOut& out) {
   out.rx = x_.r;
   out.sweeps = swp_done;
   out.res_max = res_max;
-  out.matvecs = nmv_;
+  out.matvecs = nmv_ + split_mv_;
 }
 
 
@@ -1308,9 +1381,10 @@ extern "C" int ttg_dtt_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, con
   try {
     TTG_CUDA(cudaSetDevice(ctx->device));
     TTG_REQUIRE(d > 1 && n && m && ry && ra && crA && crY && crX0 && rx, "null argument");
-    TTG_REQUIRE(method == TTG_METHOD_PLAIN, "amen: only the FP64 method is built");
+    TTG_REQUIRE(method == TTG_METHOD_PLAIN || method == TTG_METHOD_SPLIT, "unknown method");
     for (int k = 0; k < d; ++k) TTG_REQUIRE(n[k] == m[k], "amen needs square cores (n == m)");
     AmenParams P;
+    P.method = method;
     P.d = (int)d;
     P.n.assign(n, n + d);
     P.ry.assign(ry, ry + d + 1);
