@@ -7,7 +7,14 @@ block with ranks 16 (seed 0), ranks capped at 64, eps=1e-8, max_full_size=200,
 swept to convergence.  Metric: wall time of one full solve (lower is better).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--method plain|split]
+                  [--method plain|split] [--workload heisenberg20|xxz100|amen10]
+
+The default workload (heisenberg20) is the metric's.  Two larger workloads
+are measured the same way, one timed run per method after a warm-up solve:
+xxz100 = tt_eigb on the XXZ chain d=100, delta=1, B=8, ranks up to 256 (local
+problems r^2 n = 131k), two sweeps; amen10 = the ttamen AMEn solve of
+(Laplacian + exp(-|i-c|^2/sigma^2)) x = y, d=10, n=64, operator rank 3, rhs
+rank 4, tol 1e-9, ranks up to 128, 20 sweeps.
 
 GPU arm: times K solves through the C-ABI with CUDA events on the library's
 stream (value), the same solves end to end from pinned host buffers (e2e),
@@ -185,6 +192,63 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def bench_extra(args, torch, ttgpu, ctx):
+    """The larger workloads: chosen (split) and plain methods, one timed run
+    each (CUDA events on the library's stream) after a warm-up solve."""
+    from ttgpu.operators import xxz_mpo, random_tt, amen_operator
+    n, m, ra, crA, ry, cr = workload()
+    ttgpu.tt_eigb(D, n, m, ra, crA, cr, ry, EPS, RMAX, B, nswp=20, max_full_size=MFS,
+                  method="split", ctx=ctx)
+    res = {}
+    with ClockSampler() as clk:
+        for meth in ("split", "plain"):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            l0 = ttgpu.launch_count()
+            e0.record()
+            if args.workload == "xxz100":
+                d, Bx = 100, 8
+                n, m, ra, crA = xxz_mpo(d, delta=1.0)
+                _, ry, cr = random_tt(d, 2, 16, last=Bx, seed=5)
+                lam, _, ry_out = ttgpu.tt_eigb(d, n, m, ra, crA, cr, ry, 1e-10, 256, Bx, nswp=2,
+                                               max_full_size=200, method=meth, ctx=ctx)
+                out = {"lambda": np.asarray(lam), "max_rank": max(ry_out[:d])}
+            else:
+                d, nn = 10, 64
+                n_, m_, ra, crA = amen_operator(d=d, n=nn)
+                _, ry, y = random_tt(d, nn, 4, seed=3)
+                _, rx, x0 = random_tt(d, nn, 2, seed=7)
+                _, rx_out = ttgpu.dtt_amen_solve(d, n_, m_, ry, ra, crA, y, x0, rx, 1e-9,
+                                                 rmax=128, nswp=20, method=meth, ctx=ctx)
+                out = {"max_rank": max(rx_out), "res": ctx.stats()["res"]}
+            e1.record()
+            torch.cuda.synchronize()
+            out["time"] = e0.elapsed_time(e1) / 1e3
+            out["launches"] = ttgpu.launch_count() - l0
+            out["matvecs"] = ctx.stats()["matvecs"]
+            res[meth] = out
+    sp, pl = res["split"], res["plain"]
+    if args.workload == "xxz100":
+        metric = "tt_eigb time of 2 sweeps (d=100 XXZ, delta=1, B=8, rmax=256)"
+        cfg = {"workload": "tt_eigb xxz d=100 n=2 ra=5 delta=1 B=8 start_rank=16 rmax=256 "
+                           "eps=1e-10 nswp=2 max_full_size=200"}
+        agree = float(np.max(np.abs(sp["lambda"] - pl["lambda"]) / np.abs(pl["lambda"])))
+        extra = {"lambda_maxrel_vs_plain": agree, "lambda": sp["lambda"].tolist()}
+    else:
+        metric = "ttamen solve time, 20 sweeps (d=10, n=64 Laplacian + potential, tol 1e-9)"
+        cfg = {"workload": "dtt_amen_solve d=10 n=64 ra=3 ry=4 rx0=2 tol=1e-9 rmax=128 nswp=20"}
+        extra = {"res_split": sp["res"], "res_plain": pl["res"]}
+    line = {"metric": metric, "value": sp["time"], "unit": "s", "n_gpus": 1, "steps": 1,
+            "warmup": 1, "higher_is_better": False, "dtype": "bf16x3+f64", "data": "synthetic (seeded)",
+            "method": "split", "config": cfg, "gpu_launches": int(sp["launches"]),
+            "matvecs": sp["matvecs"], "max_rank": int(sp["max_rank"]),
+            "plain": {"value": pl["time"], "gpu_launches": int(pl["launches"]),
+                      "matvecs": pl["matvecs"], "plain_over_chosen": pl["time"] / sp["time"]},
+            "clocks": clk.summary()}
+    line.update(extra)
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -194,6 +258,8 @@ def main():
     ap.add_argument("--method", default="split", choices=["split", "plain"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--workload", default="heisenberg20",
+                    choices=["heisenberg20", "xxz100", "amen10"])
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
@@ -213,6 +279,10 @@ def main():
     bench_stream = torch.cuda.Stream()
     torch.cuda.set_stream(bench_stream)
     ctx.bind_torch_stream()
+    if args.workload != "heisenberg20":
+        if rank == 0:
+            bench_extra(args, torch, ttgpu, ctx)
+        return
     n, m, ra, crA, ry, cr = workload()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 

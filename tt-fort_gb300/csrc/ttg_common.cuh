@@ -232,6 +232,11 @@ void syev_jacobi(int k, double* A, int lda, double* w, double* V, int ldv, int* 
 // One-sided Jacobi SVD of M (p x q, p >= q, ldm = p), in place.  Outputs:
 // sigma (q, descending), U (p x q), Vt (q x q, rows = right singular vectors).
 size_t svd_scratch(int p, int q);
+// lowest k eigenpairs (ascending) of a symmetric N x N matrix H (overwritten)
+// by the Jacobi SVD of H + ||H||_F I; V (N x k), w (k)
+size_t syev_lowest_scratch(int N);
+void syev_lowest_svd(int N, int k, double* H, double* w, double* V, double* scratch, int* status,
+                     cudaStream_t s);
 void svd_jacobi(int p, int q, const double* M, double* U, double* sigma, double* Vt,
                 double* scratch, int* status, cudaStream_t s);
 // Householder QR with LAPACK's convention: A (n x m) -> Q (n x min), R (min x m).

@@ -172,6 +172,7 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
   total += al(svdmax) + al(sizeof(double) * capmax) * 2 + al(sizeof(double) * rmaxsvd * 2);
   total += al(bf_scr) + al(phi_scr) + al(split_bytes);
   total += 2 * al(sizeof(double) * dense_max * dense_max) + al(sizeof(double) * 512) + al(256);
+  total += al(syev_lowest_scratch((int)std::max<i64>(1, dense_max)));
   total += al(Davidson::bytes(Nmax, B, maxb_cap));
   if (P.method == TTG_METHOD_SPLIT) total += al(chosen_bytes(Nmax, B));
   const bool learned_prec = P.method == TTG_METHOD_PLAIN && ctx->learned && (ctx->learned_mode & 1);
@@ -197,6 +198,7 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
   double* dH = mem.take<double>(std::max<i64>(1, dense_max * dense_max));
   double* dV = mem.take<double>(std::max<i64>(1, dense_max * dense_max));
   double* dw = mem.take<double>(512);
+  double* dscr = (double*)mem.take<char>(syev_lowest_scratch((int)std::max<i64>(1, dense_max)));
   int* dst = mem.take<int>(64);
   void* dav_mem = mem.take<char>(Davidson::bytes(Nmax, B, maxb_cap));
   void* jd_mem = P.method == TTG_METHOD_SPLIT ? (void*)mem.take<char>(chosen_bytes(Nmax, B)) : nullptr;
@@ -255,7 +257,7 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
     if (N < P.max_full_size && N <= dense_max) {
       // dense branch: d2d_fullmat + dsyev, tt_eigb.f90:234-249
       fullmat_f64(ry[i], n[i], ry[i + 1], P.ra[i], P.ra[i + 1], phi[i], A_of(i), phi[i + 1], dH, s);
-      syev_jacobi((int)N, dH, (int)N, dw, dV, (int)N, dst, s);
+      syev_lowest_svd((int)N, B, dH, dw, dV, dscr, dst, s);
       TTG_CUDA(cudaMemcpyAsync(curcr, dV, sizeof(double) * N * B, cudaMemcpyDeviceToDevice, s));
       TTG_CUDA(cudaMemcpyAsync(hbuf, dw, sizeof(double) * B, cudaMemcpyDeviceToHost, s));
       TTG_CUDA(cudaStreamSynchronize(s));

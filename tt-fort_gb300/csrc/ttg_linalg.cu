@@ -820,3 +820,63 @@ void qr_householder_z(int n, int m, double2* A, double2* R, double2* tau, cudaSt
 }
 
 }  // namespace ttg
+
+namespace ttg {
+
+// ---------------------------------------------------------------------------
+// Lowest eigenpairs of a dense symmetric matrix through the Jacobi SVD: with
+// c = ||H||_F, H + c I is positive semidefinite, so its singular vectors are
+// its eigenvectors and its singular values are lambda + c.  The one-sided
+// Jacobi SVD above (FP32 pre-sweeps + FP64 polish) is much faster on GB300
+// than the cyclic two-sided FP64 Jacobi; the shift adds an absolute error of
+// order eps ||H||, the backward error of any dense symmetric eigensolver.
+// ---------------------------------------------------------------------------
+namespace {
+__global__ void fro_shift_kernel(int N, double* H, double* cval) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (i64 e = threadIdx.x; e < (i64)N * N; e += blockDim.x) acc = fma(H[e], H[e], acc);
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    red[0] = sqrt(t) > 0.0 ? sqrt(t) : 1.0;
+    *cval = red[0];
+  }
+  __syncthreads();
+  const double c = red[0];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) H[i + (i64)N * i] += c;
+}
+// w[j] = S[N-1-j] - c, V[:, j] = row N-1-j of Vt (j < k)
+__global__ void lowest_pairs_kernel(int N, int k, const double* S, const double* Vt,
+                                    const double* cval, double* w, double* V) {
+  const double c = *cval;
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)N * k; e += (i64)gridDim.x * blockDim.x) {
+    const int r = (int)(e % N), j = (int)(e / N);
+    V[e] = Vt[(N - 1 - j) + (i64)N * r];
+    if (r == 0) w[j] = S[N - 1 - j] - c;
+  }
+}
+}  // namespace
+
+size_t syev_lowest_scratch(int N) {
+  return svd_scratch(N, N) + (2 * (size_t)N * N + N + 64) * sizeof(double);
+}
+
+void syev_lowest_svd(int N, int k, double* H, double* w, double* V, double* scratch, int* status,
+                     cudaStream_t s) {
+  double* U = scratch;
+  double* Sv = U + (size_t)N * N;
+  double* Vt = Sv + N;
+  double* cval = Vt + (size_t)N * N;
+  double* svscr = cval + 64;
+  fro_shift_kernel<<<1, 1024, 0, s>>>(N, H, cval);
+  TTG_CHECK_LAUNCH();
+  svd_jacobi(N, N, H, U, Sv, Vt, svscr, status, s);
+  lowest_pairs_kernel<<<ceil_div((i64)N * k, 256), 256, 0, s>>>(N, k, Sv, Vt, cval, w, V);
+  TTG_CHECK_LAUNCH();
+}
+
+}  // namespace ttg
