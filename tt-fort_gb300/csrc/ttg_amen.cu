@@ -296,13 +296,26 @@ void gmres_cgs2(const MV& mv, i64 N, const double* b, double* x, double tol, int
       TTG_CUDA(cudaMemcpyAsync(H + j + 1, red, sizeof(double), cudaMemcpyDeviceToDevice, s));
       scal_kernel<<<eb(N), 256, 0, s>>>(N, red, 1, wv);
       TTG_CHECK_LAUNCH();
-      givens_kernel<<<1, 1, 0, s>>>(j, H, cs, sn, g, Rm, ldr, hres);
+      givens_kernel<<<1, 1, 0, s>>>(j, H, cs, sn, g, Rm, ldr, hres + j);
       TTG_CHECK_LAUNCH();
-      TTG_CUDA(cudaMemcpyAsync(h, hres, sizeof(double), cudaMemcpyDeviceToHost, s));
-      sync();
       jdone = j + 1;
-      curres = h[0] / nrmb;
-      if (curres < tol) break;
+      // the residual estimates are read back every 4th step (and at the
+      // last): a host synchronisation per step would bound the solve by
+      // latency.  The first step below tol ends the cycle exactly as a
+      // per-step test would: the Givens-reduced R and g of steps 0..j are
+      // final after step j, so the extra steps only cost their matvecs.
+      if (jdone % 4 == 0 || jdone == nr) {
+        const int j0 = ((jdone - 1) / 4) * 4;
+        TTG_CUDA(cudaMemcpyAsync(h, hres + j0, sizeof(double) * (jdone - j0),
+                                 cudaMemcpyDeviceToHost, s));
+        sync();
+        bool conv = false;
+        for (int q = 0; q < jdone - j0; ++q) {
+          curres = h[q] / nrmb;
+          if (curres < tol) { jdone = j0 + q + 1; conv = true; break; }
+        }
+        if (conv) break;
+      }
     }
     trsv_kernel<<<1, 1, 0, s>>>(jdone, Rm, ldr, g, y);
     TTG_CHECK_LAUNCH();
