@@ -7,14 +7,17 @@ block with ranks 16 (seed 0), ranks capped at 64, eps=1e-8, max_full_size=200,
 swept to convergence.  Metric: wall time of one full solve (lower is better).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--method plain|split] [--workload heisenberg20|xxz100|amen10]
+                  [--method plain|split] [--workload heisenberg20|xxz100|amen10|ksl16]
 
 The default workload (heisenberg20) is the metric's.  Two larger workloads
 are measured the same way, one timed run per method after a warm-up solve:
 xxz100 = tt_eigb on the XXZ chain d=100, delta=1, B=8, ranks up to 256 (local
 problems r^2 n = 131k), two sweeps; amen10 = the ttamen AMEn solve of
 (Laplacian + exp(-|i-c|^2/sigma^2)) x = y, d=10, n=64, operator rank 3, rhs
-rank 4, tol 1e-9, ranks up to 128, 20 sweeps.
+rank 4, tol 1e-9, ranks up to 128, 20 sweeps; ksl16 = ztt_ksl, 200 steps of
+tau=1e-3 of dx/dt = A x, A = -(Dirichlet Laplacian, d=16, n=32) + a random
+rank-4 TT-matrix with N(0, 0.01^2) entries, x0 a random rank-8 TT vector of
+norm 1, with the split state's relative error against the FP64 state.
 
 GPU arm: times K solves through the C-ABI with CUDA events on the library's
 stream (value), the same solves end to end from pinned host buffers (e2e),
@@ -195,10 +198,16 @@ def run_reference(args):
 def bench_extra(args, torch, ttgpu, ctx):
     """The larger workloads: chosen (split) and plain methods, one timed run
     each (CUDA events on the library's stream) after a warm-up solve."""
-    from ttgpu.operators import xxz_mpo, random_tt, amen_operator
+    from ttgpu.operators import (xxz_mpo, random_tt, amen_operator, ksl_operator,
+                                 random_tt_complex, tt_dot, tt_rel_diff)
     n, m, ra, crA, ry, cr = workload()
     ttgpu.tt_eigb(D, n, m, ra, crA, cr, ry, EPS, RMAX, B, nswp=20, max_full_size=MFS,
                   method="split", ctx=ctx)
+    if args.workload == "ksl16":
+        n_, m_, ra_, crA_ = ksl_operator(d=16, n=32, rank=4, std=0.01, seed=1)
+        _, ry_, y_ = random_tt_complex(16, 32, 8, seed=2)
+        for meth in ("split", "plain"):
+            ttgpu.ztt_ksl(16, n_, m_, ra_, crA_, y_, ry_, 1e-3, 64, nsteps=2, method=meth, ctx=ctx)
     res = {}
     with ClockSampler() as clk:
         for meth in ("split", "plain"):
@@ -213,6 +222,15 @@ def bench_extra(args, torch, ttgpu, ctx):
                 lam, _, ry_out = ttgpu.tt_eigb(d, n, m, ra, crA, cr, ry, 1e-10, 256, Bx, nswp=2,
                                                max_full_size=200, method=meth, ctx=ctx)
                 out = {"lambda": np.asarray(lam), "max_rank": max(ry_out[:d])}
+            elif args.workload == "ksl16":
+                d, nn, r = 16, 32, 8
+                n_, m_, ra, crA = ksl_operator(d=d, n=nn, rank=4, std=0.01, seed=1)
+                _, ry, y = random_tt_complex(d, nn, r, seed=2)
+                y = y.copy()
+                y[:ry[1] * nn] /= np.sqrt(tt_dot(d, n_, ry, y, ry, y).real)
+                cores, ry_out = ttgpu.ztt_ksl(d, n_, m_, ra, crA, y, ry, 1e-3, 64, nsteps=200,
+                                              method=meth, ctx=ctx)
+                out = {"cores": cores, "ry": ry_out, "n": n_, "max_rank": max(ry_out)}
             else:
                 d, nn = 10, 64
                 n_, m_, ra, crA = amen_operator(d=d, n=nn)
@@ -234,6 +252,14 @@ def bench_extra(args, torch, ttgpu, ctx):
                            "eps=1e-10 nswp=2 max_full_size=200"}
         agree = float(np.max(np.abs(sp["lambda"] - pl["lambda"]) / np.abs(pl["lambda"])))
         extra = {"lambda_maxrel_vs_plain": agree, "lambda": sp["lambda"].tolist()}
+    elif args.workload == "ksl16":
+        metric = "ztt_ksl time of 200 steps (d=16, n=32, -Laplacian + rank-4 N(0,0.01^2), rank 8)"
+        cfg = {"workload": "ztt_ksl d=16 n=32 ra=6 ry=8 tau=1e-3 nsteps=200 typ=2 order=8"}
+        extra = {"err_vs_fp64": tt_rel_diff(16, sp["n"], sp["ry"], sp["cores"], pl["ry"],
+                                            pl["cores"])}
+        for o in (sp, pl):
+            for k in ("cores", "ry", "n"):
+                o.pop(k)
     else:
         metric = "ttamen solve time, 20 sweeps (d=10, n=64 Laplacian + potential, tol 1e-9)"
         cfg = {"workload": "dtt_amen_solve d=10 n=64 ra=3 ry=4 rx0=2 tol=1e-9 rmax=128 nswp=20"}
@@ -259,7 +285,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--workload", default="heisenberg20",
-                    choices=["heisenberg20", "xxz100", "amen10"])
+                    choices=["heisenberg20", "xxz100", "amen10", "ksl16"])
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

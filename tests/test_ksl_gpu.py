@@ -62,3 +62,29 @@ def test_ksl_laplace_perturbed_small(ctx):
         c, rr = out["cores"], out["ry"]
     assert ry1 == rr
     assert _rel(tt_full(d, nn, ry1, cores), tt_full(d, nn, rr, c)) < 1e-8
+
+
+@pytest.mark.parametrize("d,n,r,steps", [(6, 8, 4, 3), (5, 16, 8, 4)])
+def test_ksl_split_against_fp64(ctx, d, n, r, steps):
+    """Chosen form: the K-step products on the BF16x3 tensor-core operator
+    (complex operator realified with doubled ranks); S-steps, QR and the
+    norm estimate's transposed products stay FP64.  Bar: 1e-5 relative to
+    the FP64 state (the split products carry ~1e-6 relative error)."""
+    import ttgpu
+    tau = 1e-3
+    nn, mm, ra, crA = ksl_operator(d=d, n=n, rank=4, std=0.1, seed=3)
+    _, ry, y = random_tt_complex(d, n, r, seed=4)
+    c64, r64 = ttgpu.ztt_ksl(d, nn, mm, ra, crA, y, ry, tau, 64, nsteps=steps, ctx=ctx)
+    csp, rsp = ttgpu.ztt_ksl(d, nn, mm, ra, crA, y, ry, tau, 64, nsteps=steps, method="split",
+                             ctx=ctx)
+    assert rsp == r64
+    err = _rel(tt_full(d, nn, rsp, csp), tt_full(d, nn, r64, c64))
+    assert err < 1e-5, err
+
+
+def test_ksl_split_eye_fixture(ctx):
+    import ttgpu
+    d, n, m, ra, ry, crA, crY, tau = load_dat("test_eye_ksl_dat.npz")
+    cores, ry1 = ttgpu.ztt_ksl(d, n, m, ra, crA, crY, ry, tau, 150, method="split", ctx=ctx)
+    x0 = tt_full(d, n, ry, crY)
+    assert _rel(tt_full(d, n, ry1, cores), np.exp(1j * tau) * x0) < 1e-6

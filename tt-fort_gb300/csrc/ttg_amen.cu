@@ -326,10 +326,6 @@ void gmres_cgs2(const MV& mv, i64 N, const double* b, double* x, double tol, int
 
 }  // namespace
 
-void split_matvec_factory(const LocalDims& L, const double* phi1, const double* A,
-                          const double* phi2, int nvec_max, void* mem, cudaStream_t s,
-                          MatvecFn* out);
-size_t split_matvec_bytes(const LocalDims& L, int nvec_max);
 
 struct AmenParams {
   int d;
@@ -508,6 +504,7 @@ void AmenSolver::gmres_split(const LocalDims& L, int k, const double* b, double*
     TTG_CHECK_LAUNCH();
     nrr = norm2(ir_r_, N);
   }
+  split_matvec_check(s_);
 }
 
 // dtt_trunc dir=+1 with the residual criterion (ttnodeop.f90:227-302)
@@ -566,6 +563,7 @@ void AmenSolver::trunc(int k, double tol, const double* rhs, double rhs_norm) {
     }
     rnew -= cnt;
   }
+  if (P_.method == TTG_METHOD_SPLIT) split_matvec_check(s_);
   int rk = fail + 1;
   if (rk > rmin) rk = rmin;
   rk = (int)std::min<i64>(rk, P_.rmax);

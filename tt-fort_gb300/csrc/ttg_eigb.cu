@@ -17,10 +17,6 @@
 
 namespace ttg {
 
-void split_matvec_factory(const LocalDims& L, const double* phi1, const double* A,
-                          const double* phi2, int nvec_max, void* mem, cudaStream_t s,
-                          MatvecFn* out);
-size_t split_matvec_bytes(const LocalDims& L, int nvec_max);
 size_t chosen_bytes(i64 N, int B);
 DavidsonStats chosen_solve(i64 N, int B, void* dav_mem, double* hbuf, void* jd_mem,
                            const MatvecFn& mv64, const MatvecFn& mvlow, const double* X0,
@@ -293,6 +289,7 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
         st = chosen_solve(N, B, dav_mem, hbuf, jd_mem, mv, mvlow, cr[i], eps2 / resid_damp,
                           max_matvecs, curcr, lam.data(), s, pt.on ? &pt.dav : nullptr, &n64);
         fp64_mv += n64;
+        split_matvec_check(s);
       } else {
         const int maxb = (int)std::min<i64>(std::max(4 * B, 32), N);
         const int keep = std::min(B + std::max(1, B / 2), std::max(maxb - B, 1));

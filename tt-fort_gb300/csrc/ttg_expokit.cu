@@ -16,9 +16,12 @@
 // stream (LAPACK's ZLARNV is not part of the reference; the oracle uses the
 // same stream), the top-t selection breaking ties by the lower index.
 #include "ttg_expokit.cuh"
+#include <cooperative_groups.h>
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+
+namespace cg = cooperative_groups;
 
 namespace ttg {
 
@@ -66,7 +69,8 @@ size_t ExpWork::bytes(i64 nmax, int m) {
   auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
   return al(sizeof(double2) * nmax * (m + 1)) + al(sizeof(double2) * nmax) +
          2 * al(sizeof(double2) * nmax * 4) + al(sizeof(double2) * (m + 2) * (m + 2)) +
-         al(sizeof(double2) * (m + 2)) + al(sizeof(double) * 64) + al(sizeof(int) * 64) + 4096;
+         al(sizeof(double2) * (m + 2)) + al(sizeof(double) * 64) + al(sizeof(int) * 64) +
+         al(sizeof(double2) * 64 * (m + 2)) + 4096;
 }
 
 void ExpWork::bind(void* mem, i64 nmax_, int m_, double* pinned) {
@@ -87,6 +91,7 @@ void ExpWork::bind(void* mem, i64 nmax_, int m_, double* pinned) {
   E = (double2*)take(sizeof(double2) * (m + 2));
   red = (double*)take(sizeof(double) * 64);
   ired = (int*)take(sizeof(int) * 64);
+  part = (double2*)take(sizeof(double2) * 64 * (m + 2));
 }
 
 // ---------------------------------------------------------------------------
@@ -323,138 +328,250 @@ __global__ void mgs_kernel(i64 n, int j, int mh, double2* V, double2* H, int* fl
   for (i64 k = threadIdx.x; k < n; k += blockDim.x) p[k] = cscale(p[k], inv);
 }
 
-// exp(t H[:mx,:mx]) (H with leading dimension mh), degree-6 Pade with scaling
-// and squaring as ZGPADM (expokit.f:767-940); writes the first column to E.
-// One CTA of 256 threads, mx <= 16.  status[0] = 1 if the Pade system is
-// singular (the reference stops there).
-constexpr int PADE_MAX = 16;
-__global__ void zgpadm_kernel(int ideg, int mx, double t, const double2* Hg, int mh, double2* E,
-                              int* status) {
-  __shared__ double2 H[PADE_MAX][PADE_MAX], H2[PADE_MAX][PADE_MAX], P[PADE_MAX][PADE_MAX],
-      Q[PADE_MAX][PADE_MAX], F[PADE_MAX][PADE_MAX];
-  __shared__ double coef[16];
-  __shared__ double s_scale, s_scale2;
-  __shared__ int s_ns;
-  __shared__ int piv[PADE_MAX];
-  const int tid = threadIdx.x;
-  const int mm = mx * mx;
-  for (int e = tid; e < mm; e += blockDim.x) H[e % mx][e / mx] = Hg[(e % mx) + mh * (e / mx)];
-  __syncthreads();
-  if (tid == 0) {
-    double hn = 0.0;
-    for (int i = 0; i < mx; ++i) {
-      double r = 0.0;
-      for (int j = 0; j < mx; ++j) r += hypot(H[i][j].x, H[i][j].y);
-      hn = fmax(hn, r);
+// The same step in one warp, for small vectors (S-step problems): warp
+// shuffles only, no block barriers.
+__global__ void mgs_warp_kernel(i64 n, int j, int mh, double2* V, double2* H, int* flag,
+                                double break_tol) {
+  if (flag[0] != 0) return;
+  double2* p = V + n * (j + 1);
+  const int lane = threadIdx.x;
+  for (int i = 0; i <= j; ++i) {
+    const double2* vi = V + n * i;
+    double ar = 0.0, ai = 0.0;
+    for (i64 k = lane; k < n; k += 32) {
+      const double2 a = vi[k], c = p[k];
+      ar += a.x * c.x + a.y * c.y;
+      ai += a.x * c.y - a.y * c.x;
     }
-    hn = fabs(t * hn);
-    int ns = hn > 0.0 ? max(0, (int)(log(hn) / log(2.0)) + 2) : 0;
-    if (!(hn > 0.0)) status[0] = 2;
-    s_ns = ns;
-    s_scale = t / (double)(1ll << ns);
-    s_scale2 = s_scale * s_scale;
-    coef[0] = 1.0;
+    const double2 hij = make_double2(wsum(ar), wsum(ai));
+    for (i64 k = lane; k < n; k += 32) p[k] = csub(p[k], cmul(hij, vi[k]));
+    if (lane == 0) H[i + (i64)mh * j] = hij;
+    __syncwarp();
+  }
+  double acc = 0.0;
+  for (i64 k = lane; k < n; k += 32) acc += cabs2(p[k]);
+  const double nrm = sqrt(wsum(acc));
+  if (nrm <= break_tol) {
+    if (lane == 0) flag[0] = j + 1;
+    return;
+  }
+  if (lane == 0) H[(j + 1) + (i64)mh * j] = make_double2(nrm, 0.0);
+  const double inv = 1.0 / nrm;
+  for (i64 k = lane; k < n; k += 32) p[k] = cscale(p[k], inv);
+}
+
+// The same modified Gram-Schmidt step spread over the CTAs of a cooperative
+// grid: FP64 runs at two FMAs per clock per SM on GB300, so one CTA would
+// leave the step FP64-bound on a single SM.  Each CTA owns a contiguous slice
+// of the vector; per column the slices' partial dot products go to their own
+// slots of part (round r uses part[r * gridDim.x ...]), and after a grid
+// barrier every CTA sums them in the same order.
+constexpr int MGS_NT = 128;
+__global__ void __launch_bounds__(MGS_NT) mgs_coop_kernel(i64 n, int j, int mh, double2* V,
+                                                          double2* H, int* flag, double break_tol,
+                                                          double2* part) {
+  __shared__ double red[33];
+  __shared__ double2 tot;
+  cg::grid_group grid = cg::this_grid();
+  if (flag[0] != 0) return;   // uniform: flag changes only after the last barrier
+  const int G = gridDim.x, b = blockIdx.x;
+  const i64 chunk = (n + G - 1) / G;
+  const i64 lo = std::min<i64>(n, chunk * b), hi = std::min<i64>(n, lo + chunk);
+  double2* p = V + n * (j + 1);
+  auto reduce_slots = [&](int r) {
+    // every CTA sums the G partials of round r in index order
+    if (threadIdx.x < 32) {
+      double ax = 0.0, ay = 0.0;
+      for (int q = threadIdx.x; q < G; q += 32) {
+        const double2 v = __ldcg(part + (i64)r * G + q);
+        ax += v.x;
+        ay += v.y;
+      }
+      ax = wsum(ax);
+      ay = wsum(ay);
+      if (threadIdx.x == 0) tot = make_double2(ax, ay);
+    }
+    __syncthreads();
+    return tot;
+  };
+  for (int i = 0; i <= j; ++i) {
+    const double2* vi = V + n * i;
+    double ar = 0.0, ai = 0.0;
+    for (i64 k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+      const double2 a = vi[k], c = p[k];
+      ar += a.x * c.x + a.y * c.y;
+      ai += a.x * c.y - a.y * c.x;
+    }
+    ar = bsum(ar, red);
+    ai = bsum(ai, red);
+    if (threadIdx.x == 0) part[(i64)i * G + b] = make_double2(ar, ai);
+    grid.sync();
+    const double2 hij = reduce_slots(i);
+    for (i64 k = lo + threadIdx.x; k < hi; k += blockDim.x) p[k] = csub(p[k], cmul(hij, vi[k]));
+    if (b == 0 && threadIdx.x == 0) H[i + (i64)mh * j] = hij;
+    __syncthreads();
+  }
+  double acc = 0.0;
+  for (i64 k = lo + threadIdx.x; k < hi; k += blockDim.x) acc += cabs2(p[k]);
+  acc = bsum(acc, red);
+  if (threadIdx.x == 0) part[(i64)(j + 1) * G + b] = make_double2(acc, 0.0);
+  grid.sync();
+  const double nrm = sqrt(reduce_slots(j + 1).x);
+  if (nrm <= break_tol) {
+    if (b == 0 && threadIdx.x == 0) flag[0] = j + 1;
+    return;
+  }
+  if (b == 0 && threadIdx.x == 0) H[(j + 1) + (i64)mh * j] = make_double2(nrm, 0.0);
+  const double inv = 1.0 / nrm;
+  for (i64 k = lo + threadIdx.x; k < hi; k += blockDim.x) p[k] = cscale(p[k], inv);
+}
+
+static void mgs_step(ExpWork& w, i64 n, int j, int mh, double break_tol, cudaStream_t s) {
+  static const int G_MAX = [] {
+    int dev = 0, per = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, mgs_coop_kernel, MGS_NT, 0);
+    return std::max(1, std::min(64, per * sms));
+  }();
+  const int G = (int)std::max<i64>(1, std::min<i64>(G_MAX, (n + 2 * MGS_NT - 1) / (2 * MGS_NT)));
+  if (n <= 1024) {
+    mgs_warp_kernel<<<1, 32, 0, s>>>(n, j, mh, w.V, w.H, w.ired, break_tol);
+    TTG_CHECK_LAUNCH();
+    return;
+  }
+  if (G == 1) {
+    mgs_kernel<<<1, 1024, 0, s>>>(n, j, mh, w.V, w.H, w.ired, break_tol);
+    TTG_CHECK_LAUNCH();
+    return;
+  }
+  double2* part = w.part;
+  void* args[] = {&n, &j, &mh, &w.V, &w.H, &w.ired, &break_tol, &part};
+  TTG_CUDA(cudaLaunchCooperativeKernel((const void*)mgs_coop_kernel, dim3(G), dim3(MGS_NT), args, 0, s));
+  g_launches++;
+}
+
+// exp(t H[:mx,:mx]) (H with leading dimension mh), degree-ideg Pade with
+// scaling and squaring as ZGPADM (expokit.f:767-940); writes the first
+// column to E.  Runs on the host: the matrix is at most 16 x 16, its result
+// steers the step control there, and serial FP64 code is what a CPU core
+// does best (one thread on the device pays the full FP64 pipe per warp).
+constexpr int PADE_MAX = 16;
+namespace {
+struct Z {
+  double x, y;
+};
+inline Z zmul(Z a, Z b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+inline Z zadd(Z a, Z b) { return {a.x + b.x, a.y + b.y}; }
+inline Z zsub(Z a, Z b) { return {a.x - b.x, a.y - b.y}; }
+inline Z zsc(Z a, double s) { return {a.x * s, a.y * s}; }
+inline Z zdiv(Z a, Z b) {
+  if (std::fabs(b.x) >= std::fabs(b.y)) {
+    const double r = b.y / b.x, den = b.x + b.y * r;
+    return {(a.x + a.y * r) / den, (a.y - a.x * r) / den};
+  }
+  const double r = b.x / b.y, den = b.x * r + b.y;
+  return {(a.x * r + a.y) / den, (a.y * r - a.x) / den};
+}
+using ZM = Z[PADE_MAX][PADE_MAX];
+inline void zmm(int mx, const ZM& A, const ZM& B, ZM& C, double sc) {
+  for (int i = 0; i < mx; ++i)
+    for (int j = 0; j < mx; ++j) {
+      Z acc{0.0, 0.0};
+      for (int k = 0; k < mx; ++k) acc = zadd(acc, zmul(A[i][k], B[k][j]));
+      C[i][j] = zsc(acc, sc);
+    }
+}
+}  // namespace
+
+static void zgpadm_host(int ideg, int mx, double t, const double* Hh, int mh, double* Eout) {
+  TTG_REQUIRE(mx >= 1 && mx <= PADE_MAX, "zgpadm: matrix too large");
+  static thread_local ZM H, H2, P, Q, F, G;
+  for (int i = 0; i < mx; ++i)
+    for (int j = 0; j < mx; ++j) H[i][j] = {Hh[2 * (i + mh * j)], Hh[2 * (i + mh * j) + 1]};
+  double hn = 0.0;
+  for (int i = 0; i < mx; ++i) {
+    double r = 0.0;
+    for (int j = 0; j < mx; ++j) r += std::hypot(H[i][j].x, H[i][j].y);
+    hn = std::max(hn, r);
+  }
+  hn = std::fabs(t * hn);
+  TTG_REQUIRE(hn > 0.0, "zgpadm: null H in input");
+  const int ns = std::max(0, (int)(std::log(hn) / std::log(2.0)) + 2);
+  const double scale = t / (double)(1ll << ns), scale2 = scale * scale;
+  double coef[PADE_MAX + 1];
+  coef[0] = 1.0;
+  {
     const int i1 = ideg + 1, j1 = 2 * ideg + 1;
     for (int k = 1; k <= ideg; ++k) coef[k] = coef[k - 1] * (double)(i1 - k) / (double)(k * (j1 - k));
   }
-  __syncthreads();
-  auto matmul = [&](double2 (*A)[PADE_MAX], double2 (*B)[PADE_MAX], double2 (*C)[PADE_MAX], double sc) {
-    for (int e = tid; e < mm; e += blockDim.x) {
-      const int i = e % mx, j = e / mx;
-      double2 acc = make_double2(0.0, 0.0);
-      for (int k = 0; k < mx; ++k) acc = cadd(acc, cmul(A[i][k], B[k][j]));
-      C[i][j] = cscale(acc, sc);
+  zmm(mx, H, H, H2, scale2);
+  for (int i = 0; i < mx; ++i)
+    for (int j = 0; j < mx; ++j) {
+      P[i][j] = {i == j ? coef[ideg - 1] : 0.0, 0.0};
+      Q[i][j] = {i == j ? coef[ideg] : 0.0, 0.0};
     }
-    __syncthreads();
-  };
-  matmul(H, H, H2, s_scale2);
-  for (int e = tid; e < mm; e += blockDim.x) {
-    const int i = e % mx, j = e / mx;
-    P[i][j] = make_double2(i == j ? coef[ideg - 1] : 0.0, 0.0);
-    Q[i][j] = make_double2(i == j ? coef[ideg] : 0.0, 0.0);
-  }
-  __syncthreads();
   // Horner: alternately Q <- Q H2 + c I, P <- P H2 + c I
   int iodd = 1;
   for (int k = ideg - 1; k > 0; --k) {
-    double2 (*U)[PADE_MAX] = iodd ? Q : P;
-    matmul(U, H2, F, 1.0);
-    for (int e = tid; e < mm; e += blockDim.x) {
-      const int i = e % mx, j = e / mx;
-      double2 v = F[i][j];
-      if (i == j) v.x += coef[k - 1];
-      U[i][j] = v;
-    }
-    __syncthreads();
+    ZM& U = iodd ? Q : P;
+    zmm(mx, U, H2, F, 1.0);
+    for (int i = 0; i < mx; ++i)
+      for (int j = 0; j < mx; ++j) U[i][j] = i == j ? Z{F[i][j].x + coef[k - 1], F[i][j].y} : F[i][j];
     iodd = 1 - iodd;
   }
   {
-    double2 (*U)[PADE_MAX] = iodd ? Q : P;
-    matmul(U, H, F, s_scale);
-    for (int e = tid; e < mm; e += blockDim.x) U[e % mx][e / mx] = F[e % mx][e / mx];
-    __syncthreads();
+    ZM& U = iodd ? Q : P;
+    zmm(mx, U, H, F, scale);
+    for (int i = 0; i < mx; ++i)
+      for (int j = 0; j < mx; ++j) U[i][j] = F[i][j];
   }
   // Q <- Q - P; solve Q E = P (LU with partial pivoting, |re|+|im| pivots)
-  for (int e = tid; e < mm; e += blockDim.x) {
-    const int i = e % mx, j = e / mx;
-    Q[i][j] = csub(Q[i][j], P[i][j]);
-  }
-  __syncthreads();
-  if (tid == 0) {
-    for (int k = 0; k < mx; ++k) {
-      int p = k;
-      double best = fabs(Q[k][k].x) + fabs(Q[k][k].y);
-      for (int i = k + 1; i < mx; ++i) {
-        double v = fabs(Q[i][k].x) + fabs(Q[i][k].y);
-        if (v > best) { best = v; p = i; }
-      }
-      piv[k] = p;
-      if (best == 0.0) { status[0] = 1; continue; }
-      if (p != k)
-        for (int j = 0; j < mx; ++j) { double2 tq = Q[k][j]; Q[k][j] = Q[p][j]; Q[p][j] = tq; }
-      for (int i = k + 1; i < mx; ++i) {
-        Q[i][k] = cdiv(Q[i][k], Q[k][k]);
-        for (int j = k + 1; j < mx; ++j) Q[i][j] = csub(Q[i][j], cmul(Q[i][k], Q[k][j]));
-      }
+  for (int i = 0; i < mx; ++i)
+    for (int j = 0; j < mx; ++j) Q[i][j] = zsub(Q[i][j], P[i][j]);
+  int piv[PADE_MAX];
+  for (int k = 0; k < mx; ++k) {
+    int p = k;
+    double best = std::fabs(Q[k][k].x) + std::fabs(Q[k][k].y);
+    for (int i = k + 1; i < mx; ++i) {
+      const double v = std::fabs(Q[i][k].x) + std::fabs(Q[i][k].y);
+      if (v > best) { best = v; p = i; }
+    }
+    piv[k] = p;
+    TTG_REQUIRE(best != 0.0, "zgpadm: the Pade denominator is singular");
+    if (p != k)
+      for (int j = 0; j < mx; ++j) std::swap(Q[k][j], Q[p][j]);
+    for (int i = k + 1; i < mx; ++i) {
+      Q[i][k] = zdiv(Q[i][k], Q[k][k]);
+      for (int j = k + 1; j < mx; ++j) Q[i][j] = zsub(Q[i][j], zmul(Q[i][k], Q[k][j]));
     }
   }
-  __syncthreads();
-  // one thread per right-hand side column
-  if (tid < mx) {
-    const int c = tid;
-    for (int k = 0; k < mx; ++k) {
-      if (piv[k] != k) { double2 tp = P[k][c]; P[k][c] = P[piv[k]][c]; P[piv[k]][c] = tp; }
-    }
+  for (int c = 0; c < mx; ++c) {
+    for (int k = 0; k < mx; ++k)
+      if (piv[k] != k) std::swap(P[k][c], P[piv[k]][c]);
     for (int i = 0; i < mx; ++i)
-      for (int k = 0; k < i; ++k) P[i][c] = csub(P[i][c], cmul(Q[i][k], P[k][c]));
+      for (int k = 0; k < i; ++k) P[i][c] = zsub(P[i][c], zmul(Q[i][k], P[k][c]));
     for (int i = mx - 1; i >= 0; --i) {
-      double2 v = P[i][c];
-      for (int k = i + 1; k < mx; ++k) v = csub(v, cmul(Q[i][k], P[k][c]));
-      P[i][c] = cdiv(v, Q[i][i]);
+      Z v = P[i][c];
+      for (int k = i + 1; k < mx; ++k) v = zsub(v, zmul(Q[i][k], P[k][c]));
+      P[i][c] = zdiv(v, Q[i][i]);
     }
   }
-  __syncthreads();
   // E = 2 E + I
-  for (int e = tid; e < mm; e += blockDim.x) {
-    const int i = e % mx, j = e / mx;
-    double2 v = cscale(P[i][j], 2.0);
-    if (i == j) v.x += 1.0;
-    P[i][j] = v;
-  }
-  __syncthreads();
-  if (s_ns == 0 && iodd) {
-    for (int i = tid; i < mx; i += blockDim.x) E[i] = cscale(P[i][0], -1.0);
+  for (int i = 0; i < mx; ++i)
+    for (int j = 0; j < mx; ++j) P[i][j] = i == j ? Z{2.0 * P[i][j].x + 1.0, 2.0 * P[i][j].y}
+                                                  : zsc(P[i][j], 2.0);
+  if (ns == 0 && iodd) {
+    for (int i = 0; i < mx; ++i) { Eout[2 * i] = -P[i][0].x; Eout[2 * i + 1] = -P[i][0].y; }
     return;
   }
-  double2 (*cur)[PADE_MAX] = P;
-  double2 (*nxt)[PADE_MAX] = F;
-  for (int k = 0; k < s_ns; ++k) {
-    matmul(cur, cur, nxt, 1.0);
-    double2 (*tt)[PADE_MAX] = cur;
-    cur = nxt;
-    nxt = tt;
+  ZM* cur = &P;
+  ZM* nxt = &G;
+  for (int k = 0; k < ns; ++k) {
+    zmm(mx, *cur, *cur, *nxt, 1.0);
+    std::swap(cur, nxt);
   }
-  for (int i = tid; i < mx; i += blockDim.x) E[i] = cur[i][0];
+  for (int i = 0; i < mx; ++i) { Eout[2 * i] = (*cur)[i][0].x; Eout[2 * i + 1] = (*cur)[i][0].y; }
 }
 
 // out = beta * V[:, :mx] E[:mx]   (complex gemv)
@@ -521,15 +638,18 @@ static void zgexpv_dev(ExpWork& w, i64 n, int m, double t, const double2* v, dou
     TTG_CUDA(cudaMemsetAsync(w.ired, 0, sizeof(int), s));
     for (int j = 0; j < m; ++j) {
       mv(w.V + n * j, w.V + n * (j + 1), 1);
-      mgs_kernel<<<1, 1024, 0, s>>>(n, j, mh, w.V, w.H, w.ired, break_tol);
-      TTG_CHECK_LAUNCH();
+      mgs_step(w, n, j, mh, break_tol, s);
     }
     if (st) st->nmult += m;
     mv(w.V + n * m, w.tmp, 1);
     znrm2_kernel<<<1, 1024, 0, s>>>(n, w.tmp, w.red);
     TTG_CHECK_LAUNCH();
+    // one read-back per Krylov step: ||A v_{m+1}||, the breakdown flag and H
+    double* hH = h + 16;
+    double* hE = h + 16 + 2 * PADE_MAX * PADE_MAX;
     TTG_CUDA(cudaMemcpyAsync(h, w.red, sizeof(double), cudaMemcpyDeviceToHost, s));
     TTG_CUDA(cudaMemcpyAsync(h + 1, w.ired, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TTG_CUDA(cudaMemcpyAsync(hH, w.H, sizeof(double2) * mh * mh, cudaMemcpyDeviceToHost, s));
     sync();
     const int brk = *(const int*)(h + 1);
     int k1 = 2, mbrkdwn = m;
@@ -546,15 +666,12 @@ static void zgexpv_dev(ExpWork& w, i64 n, int m, double t, const double2* v, dou
     double err_loc = tol;
     while (true) {
       const int mx = mbrkdwn + k1;
-      zgpadm_kernel<<<1, 256, 0, s>>>(ideg, mx, sgn * t_step, w.H, mh, w.E, w.ired + 8);
-      TTG_CHECK_LAUNCH();
-      TTG_CUDA(cudaMemcpyAsync(h + 2, w.E, sizeof(double2) * mx, cudaMemcpyDeviceToHost, s));
-      sync();
+      zgpadm_host(ideg, mx, sgn * t_step, hH, mh, hE);
       if (k1 == 0) {
         err_loc = tol;
       } else {
-        const double p1 = std::hypot(h[2 + 2 * m], h[3 + 2 * m]) * beta;
-        const double q2 = std::hypot(h[2 + 2 * (m + 1)], h[3 + 2 * (m + 1)]) * beta * avnorm;
+        const double p1 = std::hypot(hE[2 * m], hE[2 * m + 1]) * beta;
+        const double q2 = std::hypot(hE[2 * (m + 1)], hE[2 * (m + 1) + 1]) * beta * avnorm;
         if (p1 > 10.0 * q2) {
           err_loc = q2;
           xm = 1.0 / m;
@@ -574,6 +691,8 @@ static void zgexpv_dev(ExpWork& w, i64 n, int m, double t, const double2* v, dou
       break;
     }
     const int mx = mbrkdwn + std::max(0, k1 - 1);
+    // hE is rewritten only after the next sync, when this copy has run
+    TTG_CUDA(cudaMemcpyAsync(w.E, hE, sizeof(double2) * mx, cudaMemcpyHostToDevice, s));
     zgemv_kernel<<<eb, 256, 0, s>>>(n, mx, w.V, w.E, beta, out);
     TTG_CHECK_LAUNCH();
     znrm2_kernel<<<1, 1024, 0, s>>>(n, out, w.red);

@@ -25,6 +25,7 @@ struct ExpWork {
   double2* E = nullptr;     // (m+2) first column of exp(tH)
   double* red = nullptr;    // small reduction outputs
   int* ired = nullptr;      // small integer outputs
+  double2* part = nullptr;  // per-CTA partial sums of the cooperative Gram-Schmidt
   double* hbuf = nullptr;   // pinned host mirror (4096 doubles)
   static size_t bytes(i64 nmax, int m);
   void bind(void* mem, i64 nmax_, int m_, double* pinned);

@@ -226,7 +226,20 @@ void launch(Args<T> a, int nbatch, cudaStream_t s) {
   // are busy.
   const bool small_tiles = sizeof(T) <= 8 && a.N > 16 && a.M > 16 &&
                            (i64)ceil_div(a.M, 64) * ceil_div(a.N, 64) * nbatch < 2 * 152;
-  if (a.splitk == 1 && a.K >= 128) {
+  if constexpr (sizeof(T) == 16) {
+    // complex128 (the KSL products): small ranks give thin products, so the
+    // tiles are 32 x 16 / 16 x 32 / 32 x 32 and K splits (chunks of >= 16)
+    // until about two CTAs per SM carry the FP64 work
+    if (a.splitk == 1 && a.K >= 32) {
+      const int bm = a.N <= 16 ? 32 : (a.M <= 16 ? 16 : 32);
+      const int bn = a.N <= 16 ? 16 : (a.M <= 16 ? 32 : 32);
+      const i64 ctas = (i64)ceil_div(a.M, bm) * ceil_div(a.N, bn) * nbatch;
+      if (ctas < 152) {
+        const i64 want = (304 + ctas - 1) / ctas;
+        a.splitk = (int)std::max<i64>(1, std::min<i64>(want, a.K / 16));
+      }
+    }
+  } else if (a.splitk == 1 && a.K >= 128) {
     int bm = a.N <= 16 ? 128 : (a.M <= 16 ? 16 : ((sizeof(T) <= 8 && !small_tiles) ? 64 : 32));
     int bn = a.N <= 16 ? 16 : (a.M <= 16 ? 128 : ((sizeof(T) <= 8 && !small_tiles) ? 64 : 32));
     i64 ctas = (i64)ceil_div(a.M, bm) * ceil_div(a.N, bn) * nbatch;
@@ -244,6 +257,22 @@ void launch(Args<T> a, int nbatch, cudaStream_t s) {
     TTG_CHECK_LAUNCH();
   }
   TTG_REQUIRE((i64)nbatch * a.splitk < 65536, "gemm: batch*splitk too large");
+  if constexpr (sizeof(T) == 16) {
+    if (a.N <= 16) {
+      dim3 grid(ceil_div(a.M, 32), ceil_div(a.N, 16), nbatch * a.splitk);
+      gemm_kernel<T, 32, 16, 2, 1><<<grid, NT, 0, s>>>(a);
+    } else if (a.M <= 16) {
+      dim3 grid(ceil_div(a.M, 16), ceil_div(a.N, 32), nbatch * a.splitk);
+      TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
+      gemm_kernel<T, 16, 32, 1, 2><<<grid, NT, 0, s>>>(a);
+    } else {
+      dim3 grid(ceil_div(a.M, 32), ceil_div(a.N, 32), nbatch * a.splitk);
+      TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
+      gemm_kernel<T, 32, 32, 2, 2><<<grid, NT, 0, s>>>(a);
+    }
+    TTG_CHECK_LAUNCH();
+    return;
+  }
   if (a.N <= 16) {
     constexpr int BM = 128, BN = 16;
     dim3 grid(ceil_div(a.M, BM), ceil_div(a.N, BN), nbatch * a.splitk);

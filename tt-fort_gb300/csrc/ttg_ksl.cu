@@ -9,6 +9,7 @@
 // with tau0 = tau/2 for the symmetric scheme (typ = 2), Krylov order 8 and
 // tolerance 1e-8 (tt_ksl.f90:477), anorm from the block 1-norm estimate.
 #include "ttg_expokit.cuh"
+#include "ttg_davidson.cuh"
 #include <algorithm>
 #include <cmath>
 
@@ -71,7 +72,89 @@ struct KslParams {
   const double2* crY0;
   double tau;
   int typ, order, nsteps, verb;
+  int method = TTG_METHOD_PLAIN;
 };
+
+// Chosen form of the K-step product: the complex local operator
+// y = Phi1 A Phi2 x (zbfun3) as ONE real BF16x3 tensor-core operator with
+// doubled ranks.  A complex factor w acts on (re, im) parts as the real 2x2
+// block [[wr, -wi], [wi, wr]]; the re/im part of each contracted index is
+// carried by a rank index: x by b2 (rx2 -> 2 rx2), the Phi2 product by a2,
+// the A product by a1, the Phi1 product (the result) by c1.  Real dims:
+// (rx1, m, 2 rx2, 2 ry1, n, ry2, 2 ra1, 2 ra2).
+__device__ __forceinline__ double cmul_block(double2 w, int o, int c) {
+  return o == c ? w.x : (o == 0 ? -w.y : w.y);
+}
+// The adjoint product y = B^H x (zbfun3_transp) is the same kind of operator
+// with the roles of x and y exchanged: Phi1'[c1,b1,a1] = conj Phi1[b1,c1,a1],
+// A'[a1,i,j,a2] = conj A[a1,j,i,a2], Phi2'[b2,a2,c2] = conj Phi2[c2,a2,b2],
+// so the realify kernels take the dims of the operator they build and, with
+// adj set, read the original operand through that index map.
+__device__ __forceinline__ double2 cadj(double2 w, bool adj) { return adj ? make_double2(w.x, -w.y) : w; }
+// Phi2~[(b2 + rx2 c) + 2 rx2 ((a2 + ra2 o) + 2 ra2 c2)] = M(Phi2[b2, a2, c2])[o, c]
+__global__ void realify_phi2_kernel(i64 rx2, i64 ra2, i64 ry2, const double2* __restrict__ P,
+                                    double* __restrict__ out, bool adj) {
+  const i64 tot = 4 * rx2 * ra2 * ry2;
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x) {
+    i64 t = e;
+    const i64 bc = t % (2 * rx2); t /= 2 * rx2;
+    const i64 ao = t % (2 * ra2); const i64 c2 = t / (2 * ra2);
+    const i64 b2 = bc % rx2, c = bc / rx2, a2 = ao % ra2, o = ao / ra2;
+    const i64 src = adj ? c2 + ry2 * (a2 + ra2 * b2) : b2 + rx2 * (a2 + ra2 * c2);
+    out[e] = cmul_block(cadj(P[src], adj), (int)o, (int)c);
+  }
+}
+// A~[(a1 + ra1 o) + 2 ra1 (i + n (j + m (a2 + ra2 c)))] = M(A[a1, i, j, a2])[o, c]
+__global__ void realify_core_kernel(i64 ra1, i64 n, i64 m, i64 ra2, const double2* __restrict__ A,
+                                    double* __restrict__ out, bool adj) {
+  const i64 tot = 4 * ra1 * n * m * ra2;
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x) {
+    i64 t = e;
+    const i64 ao = t % (2 * ra1); t /= 2 * ra1;
+    const i64 i = t % n; t /= n;
+    const i64 j = t % m; t /= m;
+    const i64 ac = t;
+    const i64 a1 = ao % ra1, o = ao / ra1, a2 = ac % ra2, c = ac / ra2;
+    const i64 src = adj ? a1 + ra1 * (j + m * (i + n * a2)) : a1 + ra1 * (i + n * (j + m * a2));
+    out[e] = cmul_block(cadj(A[src], adj), (int)o, (int)c);
+  }
+}
+// Phi1~[(c1 + ry1 o) + 2 ry1 (b1 + rx1 (a1 + ra1 c))] = M(Phi1[c1, b1, a1])[o, c]
+__global__ void realify_phi1_kernel(i64 ry1, i64 rx1, i64 ra1, const double2* __restrict__ P,
+                                    double* __restrict__ out, bool adj) {
+  const i64 tot = 4 * ry1 * rx1 * ra1;
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x) {
+    i64 t = e;
+    const i64 co = t % (2 * ry1); t /= 2 * ry1;
+    const i64 b1 = t % rx1; const i64 ac = t / rx1;
+    const i64 c1 = co % ry1, o = co / ry1, a1 = ac % ra1, c = ac / ra1;
+    const i64 src = adj ? b1 + rx1 * (c1 + ry1 * a1) : c1 + ry1 * (b1 + rx1 * a1);
+    out[e] = cmul_block(cadj(P[src], adj), (int)o, (int)c);
+  }
+}
+// x~[b1 + rx1 (j + m (b2 + rx2 c))] = part c of x[b1, j, b2] (per vector)
+__global__ void pack_x_kernel(i64 rx1m, i64 rx2, int nv, const double2* __restrict__ x,
+                              double* __restrict__ xt) {
+  const i64 N = rx1m * rx2;
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < N * nv; e += (i64)gridDim.x * blockDim.x) {
+    const i64 v = e / N, r = e % N;
+    const double2 z = x[e];
+    xt[2 * N * v + r] = z.x;
+    xt[2 * N * v + N + r] = z.y;
+  }
+}
+// y[c1, i, c2] = y~[c1 + 2 ry1 (i, c2)] + i y~[c1 + ry1 + 2 ry1 (i, c2)]
+__global__ void unpack_y_kernel(i64 ry1, i64 rest, int nv, const double* __restrict__ yt,
+                                double2* __restrict__ y) {
+  const i64 N = ry1 * rest;
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < N * nv; e += (i64)gridDim.x * blockDim.x) {
+    const i64 v = e / N, r = e % N;
+    const i64 c1 = r % ry1, q = r / ry1;
+    const double* b = yt + 2 * N * v + 2 * ry1 * q;
+    y[e] = make_double2(b[c1], b[c1 + ry1]);
+  }
+}
+inline int ebz(i64 n) { return (int)std::max<i64>(1, std::min<i64>(4096, (n + 255) / 256)); }
 
 static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>& out_cores,
                     std::vector<i64>& out_ry, ExpStats& est) {
@@ -109,6 +192,31 @@ static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>
   total += 5 * alz(sizeof(double2) * capmax) + alz(sizeof(double2) * phimax) +
            2 * alz(sizeof(double2) * rmx * rmx) + alz(sizeof(double2) * rmx * 2) +
            alz(sizeof(double2) * scr) + alz(ExpWork::bytes(Nmax, P.order)) + (1 << 16);
+  // chosen form: realified local operator (doubled ranks) on the tensor cores
+  const bool split = P.method == TTG_METHOD_SPLIT;
+  auto Lreal = [&](const LocalDims& L) {
+    return LocalDims{L.rx1, L.m, 2 * L.rx2, 2 * L.ry1, L.n, L.ry2, 2 * L.ra1, 2 * L.ra2};
+  };
+  auto adjoint = [&](const LocalDims& L) {
+    return LocalDims{L.ry1, L.n, L.ry2, L.rx1, L.m, L.rx2, L.ra1, L.ra2};
+  };
+  const int kNvecSplit = 4;   // block width of the norm estimate
+  i64 amax = 1;
+  size_t split_bytes = 0;
+  if (split) {
+    for (int i = 0; i < d; ++i) {
+      const LocalDims L{Rc[i], n[i], Rc[i + 1], Rc[i], n[i], Rc[i + 1], P.ra[i], P.ra[i + 1]};
+      for (const LocalDims& Lr : {Lreal(L), Lreal(adjoint(L))}) {
+        TTG_REQUIRE(split_op_supported(Lr), "ztt_ksl: local problem too large for the split kernel");
+        split_bytes = std::max(split_bytes, split_matvec_bytes(Lr, kNvecSplit));
+      }
+      amax = std::max(amax, P.ra[i] * n[i] * P.m[i] * P.ra[i + 1]);
+    }
+    // operator and adjoint: realified operands and prepared operators
+    total += 2 * (2 * alz(sizeof(double) * 4 * phimax) + alz(sizeof(double) * 4 * amax) +
+                  alz(split_bytes)) +
+             2 * alz(sizeof(double) * 2 * capmax * kNvecSplit);
+  }
   DevBlockZ mem;
   mem.alloc(total);
   double2* dA = mem.take<double2>(pa[d]);
@@ -126,6 +234,18 @@ static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>
   double2* tau_ws = mem.take<double2>(rmx * 2);
   double2* scratch = mem.take<double2>(scr);
   void* expmem = mem.take<char>(ExpWork::bytes(Nmax, P.order));
+  double *rphi1[2] = {}, *rphi2[2] = {}, *rA[2] = {}, *rx = nullptr, *ryv = nullptr;
+  void* smem[2] = {};
+  if (split) {
+    for (int k = 0; k < 2; ++k) {
+      rphi1[k] = mem.take<double>(4 * phimax);
+      rphi2[k] = mem.take<double>(4 * phimax);
+      rA[k] = mem.take<double>(4 * amax);
+      smem[k] = mem.take<char>(split_bytes);
+    }
+    rx = mem.take<double>(2 * capmax * kNvecSplit);
+    ryv = mem.take<double>(2 * capmax * kNvecSplit);
+  }
   double* pinned = nullptr;
   TTG_CUDA(cudaMallocHost(&pinned, 4096 * sizeof(double)));
   struct PinGuard { double* p; ~PinGuard() { if (p) cudaFreeHost(p); } } pg{pinned};
@@ -176,8 +296,35 @@ static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>
       ZMatvecFn mvT = [=](const double2* X, double2* Y, int t) {
         bfun3_transp_z(L, p1, Ai, p2, X, Y, t, scratch, s);
       };
+      if (split) {
+        // slot 0: the operator, slot 1: its adjoint (the norm estimate's)
+        auto build = [&](int k) -> ZMatvecFn {
+          const LocalDims Lk = k ? adjoint(L) : L;
+          const bool adj = k == 1;
+          realify_phi1_kernel<<<ebz(4 * Lk.ry1 * Lk.rx1 * Lk.ra1), 256, 0, s>>>(Lk.ry1, Lk.rx1, Lk.ra1, p1, rphi1[k], adj);
+          realify_core_kernel<<<ebz(4 * Lk.ra1 * Lk.n * Lk.m * Lk.ra2), 256, 0, s>>>(Lk.ra1, Lk.n, Lk.m, Lk.ra2, Ai, rA[k], adj);
+          realify_phi2_kernel<<<ebz(4 * Lk.rx2 * Lk.ra2 * Lk.ry2), 256, 0, s>>>(Lk.rx2, Lk.ra2, Lk.ry2, p2, rphi2[k], adj);
+          TTG_CHECK_LAUNCH();
+          MatvecFn smv;
+          split_matvec_factory(Lreal(Lk), rphi1[k], rA[k], rphi2[k], kNvecSplit, smem[k], s, &smv, k);
+          const i64 Nk = Lk.xsize();
+          return [=](const double2* X, double2* Y, int t) {
+            for (int v0 = 0; v0 < t; v0 += kNvecSplit) {
+              const int nv = std::min(kNvecSplit, t - v0);
+              pack_x_kernel<<<ebz(Nk * nv), 256, 0, s>>>(Lk.rx1 * Lk.m, Lk.rx2, nv, X + Nk * v0, rx);
+              TTG_CHECK_LAUNCH();
+              smv(rx, ryv, nv);
+              unpack_y_kernel<<<ebz(Nk * nv), 256, 0, s>>>(Lk.ry1, Lk.n * Lk.ry2, nv, ryv, Y + Nk * v0);
+              TTG_CHECK_LAUNCH();
+            }
+          };
+        };
+        mv = build(0);
+        mvT = build(1);
+      }
       const double anorm = znormest_dev(w, N, 4, mv, &mvT, counter, s, &est);
       zexp_mv_dev(w, N, P.order, tau0, cr[i], curcr, eps, anorm, mv, s, &est);
+      if (split) split_matvec_check(s);
     };
     auto sstep = [&](i64 rx1, i64 rx2, i64 ra, i64 ry1, i64 ry2, const double2* ph1,
                      const double2* ph2, const double2* Rin) {
@@ -287,7 +434,8 @@ extern "C" int ttg_ksl_z(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_in
   try {
     TTG_CUDA(cudaSetDevice(ctx->device));
     TTG_REQUIRE(d > 0 && n && m && ra && crA && crY0 && ry, "null argument");
-    TTG_REQUIRE(method == TTG_METHOD_PLAIN, "ztt_ksl: only the FP64 method is built");
+    TTG_REQUIRE(method == TTG_METHOD_PLAIN || method == TTG_METHOD_SPLIT,
+                "ztt_ksl: method must be PLAIN (FP64) or SPLIT (BF16x3 K-step products)");
     TTG_REQUIRE(typ == 1 || typ == 2, "typ must be 1 (KSL) or 2 (symmetric KSL)");
     (void)rmax;   // read but unused by the reference as well (tt_ksl.f90:446)
     KslParams P;
@@ -303,6 +451,7 @@ extern "C" int ttg_ksl_z(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_in
     P.order = order > 0 ? order : 8;
     P.nsteps = nsteps > 0 ? (int)nsteps : 1;
     P.verb = verb;
+    P.method = method;
     long long l0 = g_launches;
     ExpStats est;
     std::vector<i64> ry_out;

@@ -725,14 +725,23 @@ __device__ __forceinline__ double2 crecip(double2 a) {
 }
 __device__ __forceinline__ double crecip(double a) { return 1.0 / a; }
 
-template <class T>
-__global__ void __launch_bounds__(QR_NT) qr_kernel(int n, int m, T* A, T* R, T* tau) {
+// SM: the matrix is staged in shared memory (small cores: the column sweeps
+// then wait on shared rather than global memory latency), same arithmetic.
+template <class T, bool SM>
+__global__ void __launch_bounds__(QR_NT) qr_kernel(int n, int m, T* Ag, T* R, T* tau) {
   using C = CT<T>;
   __shared__ double red[33];
   __shared__ T s_tau, s_beta;
+  extern __shared__ __align__(16) unsigned char qr_dyn[];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int nwarp = QR_NT / 32;
   const int r = min(n, m);
+  T* A = Ag;
+  if constexpr (SM) {
+    A = reinterpret_cast<T*>(qr_dyn);
+    for (i64 e = tid; e < (i64)n * m; e += QR_NT) A[e] = Ag[e];
+    __syncthreads();
+  }
   for (int j = 0; j < r; ++j) {
     T* col = A + (i64)n * j;
     double t = 0.0;
@@ -806,17 +815,38 @@ __global__ void __launch_bounds__(QR_NT) qr_kernel(int n, int m, T* A, T* R, T* 
     for (int i = tid; i < j; i += QR_NT) col[i] = C::mk(0.0, 0.0);
     __syncthreads();
   }
+  if constexpr (SM) {
+    __syncthreads();
+    for (i64 e = tid; e < (i64)n * m; e += QR_NT) Ag[e] = A[e];
+  }
+}
+
+constexpr size_t QR_SMEM_MAX = 200 * 1024;
+template <class T>
+static void qr_launch(int n, int m, T* A, T* R, T* tau, cudaStream_t s) {
+  const size_t bytes = (size_t)n * m * sizeof(T);
+  if (bytes <= QR_SMEM_MAX) {
+    static const bool attr_ok = cudaFuncSetAttribute(qr_kernel<T, true>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)QR_SMEM_MAX) == cudaSuccess;
+    if (attr_ok) {
+      qr_kernel<T, true><<<1, QR_NT, bytes, s>>>(n, m, A, R, tau);
+      TTG_CHECK_LAUNCH();
+      return;
+    }
+    (void)cudaGetLastError();
+  }
+  qr_kernel<T, false><<<1, QR_NT, 0, s>>>(n, m, A, R, tau);
+  TTG_CHECK_LAUNCH();
 }
 
 void qr_householder(int n, int m, double* A, double* R, double* tau, cudaStream_t s) {
   if (n <= 0 || m <= 0) return;
-  qr_kernel<double><<<1, QR_NT, 0, s>>>(n, m, A, R, tau);
-  TTG_CHECK_LAUNCH();
+  qr_launch<double>(n, m, A, R, tau, s);
 }
 void qr_householder_z(int n, int m, double2* A, double2* R, double2* tau, cudaStream_t s) {
   if (n <= 0 || m <= 0) return;
-  qr_kernel<double2><<<1, QR_NT, 0, s>>>(n, m, A, R, tau);
-  TTG_CHECK_LAUNCH();
+  qr_launch<double2>(n, m, A, R, tau, s);
 }
 
 }  // namespace ttg

@@ -428,11 +428,16 @@ __global__ void __launch_bounds__(128)
 // flattened rows e = b1 + rx1*(c2 + ry2*v) (64 per block) and the outputs
 // p = (a1, i) (64 per block), K = (j, a2) in chunks of 32; 256 threads with
 // 4 x 4 results each.  A(a1,i,j,a2) sits at A[p + n*ra1*q].
+// Few rows (small ranks, one vector) leave most SMs idle, so K may be split
+// over gridDim.z chunks of qchunk: each chunk then writes its FP32 partial
+// product to part[(z * rows + row) * na + p] and core_finish_kernel adds the
+// chunks in order and splits the sum (deterministic, no atomics).
 constexpr int CT_R = 64, CT_P = 64, CT_Q = 32;
 __global__ void __launch_bounds__(256)
     core_tiled_kernel(const float* __restrict__ T1, i64 ld1, const double* __restrict__ A,
                       int rx1, int m, int ra2, int n, int ra1, int ry2, int nvec, int lgR3,
-                      int ktiles3, bf16* __restrict__ hi, bf16* __restrict__ lo) {
+                      int ktiles3, bf16* __restrict__ hi, bf16* __restrict__ lo, int qchunk,
+                      float* __restrict__ part) {
   __shared__ float Ts[CT_Q][CT_R + 4];
   __shared__ float As[CT_Q][CT_P + 4];
   __shared__ i64 rbase[CT_R];
@@ -457,18 +462,19 @@ __global__ void __launch_bounds__(256)
   for (int x = 0; x < 4; ++x)
 #pragma unroll
     for (int y = 0; y < 4; ++y) acc[x][y] = 0.f;
-  for (int q0 = 0; q0 < ja; q0 += CT_Q) {
+  const int qbeg = blockIdx.z * qchunk, qend = min(ja, qbeg + qchunk);
+  for (int q0 = qbeg; q0 < qend; q0 += CT_Q) {
     __syncthreads();
     for (int l = tid; l < CT_R * CT_Q; l += 256) {
       const int rr = l % CT_R, qq = l / CT_R, q = q0 + qq;
       const i64 base = rbase[rr];
       float val = 0.f;
-      if (base >= 0 && q < ja) val = T1[base + (i64)rx1 * (q % m) + ld1 * (q / m)];
+      if (base >= 0 && q < qend) val = T1[base + (i64)rx1 * (q % m) + ld1 * (q / m)];
       Ts[qq][rr] = val;
     }
     for (int l = tid; l < CT_P * CT_Q; l += 256) {
       const int pp = l % CT_P, qq = l / CT_P, p = p0 + pp, q = q0 + qq;
-      As[qq][pp] = (p < na && q < ja) ? (float)A[p + (i64)na * q] : 0.f;
+      As[qq][pp] = (p < na && q < qend) ? (float)A[p + (i64)na * q] : 0.f;
     }
     __syncthreads();
 #pragma unroll 8
@@ -481,6 +487,20 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
         for (int y = 0; y < 4; ++y) acc[x][y] = fmaf(tv[x], av[y], acc[x][y]);
     }
+  }
+  if (part) {
+#pragma unroll
+    for (int x = 0; x < 4; ++x) {
+      const i64 row = row0 + ty * 4 + x;
+      if (row >= rows) continue;
+      float* dst = part + ((i64)blockIdx.z * rows + row) * na;
+#pragma unroll
+      for (int y = 0; y < 4; ++y) {
+        const int p = p0 + tx * 4 + y;
+        if (p < na) dst[p] = acc[x][y];
+      }
+    }
+    return;
   }
 #pragma unroll
   for (int x = 0; x < 4; ++x) {
@@ -501,6 +521,42 @@ __global__ void __launch_bounds__(256)
       hi[idx] = h;
       lo[idx] = l;
     }
+  }
+}
+
+// sum of the K chunks of core_tiled_kernel, split into the GEMM3 operand
+__global__ void core_finish_kernel(const float* __restrict__ part, int nz, i64 rows, int na,
+                                   int rx1, int n, int ra1, int lgR3, int ktiles3,
+                                   bf16* __restrict__ hi, bf16* __restrict__ lo) {
+  const i64 total = rows * na;
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total;
+       e += (i64)gridDim.x * blockDim.x) {
+    float acc = 0.f;
+    for (int z = 0; z < nz; ++z) acc += part[(i64)z * total + e];
+    const i64 row = e / na;
+    const int p = (int)(e % na);
+    const int b1 = (int)(row % rx1);
+    const i64 cv = row / rx1;
+    const int a1 = p % ra1, i = p / ra1;
+    const int r = (int)(i + (i64)n * cv);
+    const int k = b1 + rx1 * a1;
+    bf16 h, l;
+    split2f(acc, h, l);
+    const size_t idx = tiled_index_pow2(r, k, lgR3, ktiles3);
+    hi[idx] = h;
+    lo[idx] = l;
+  }
+}
+
+// K chunks of the tiled CORE product for rows x na outputs over ja
+inline void core_chunks(i64 rows, int na, int ja, int& nz, int& qchunk) {
+  const i64 base = ceil_div(rows, (i64)CT_R) * ceil_div(na, CT_P);
+  nz = 1;
+  qchunk = ja;
+  if (base < 152 && ja > CT_Q) {
+    const i64 want = std::min<i64>(ceil_div(ja, CT_Q), ceil_div((i64)304, base));
+    qchunk = (int)ceil_div((i64)ceil_div((i64)ja, want), (i64)CT_Q) * CT_Q;
+    nz = (int)ceil_div((i64)ja, (i64)qchunk);
   }
 }
 
@@ -603,6 +659,7 @@ struct SplitOp {
   i64 ld1;
   const double* A;
   int* err;
+  float* part;          // K-chunk partials of the tiled CORE kernel (or null)
   int coef_kind;        // 0: tiled CORE kernel; 1..4: small CORE with (JA, NA) bound
   float coef[256];      // A as FP32 in its own column-major order (small CORE)
 };
@@ -617,6 +674,19 @@ static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* 
   const i64 ld1 = (i64)ceil_div(M1, 4) * 4;
   size_t t1 = ((size_t)ld1 * ceil_div(N1, 4) * 4 * sizeof(float) + 1023) & ~size_t(1023);
   tot += t1 + 1024 + sizeof(SplitOp) + 1024;
+  // K-chunk partials of the tiled CORE kernel, the largest over 1..nvec_max
+  const int ja = (int)(L.m * L.ra2), na = (int)(L.n * L.ra1);
+  size_t part = 0;
+  if (!(ja <= 16 && na <= 16)) {
+    for (int v = 1; v <= nvec_max; ++v) {
+      int nz, qc;
+      tc::core_chunks(L.rx1 * L.ry2 * v, na, ja, nz, qc);
+      const size_t b = (size_t)(nz * L.rx1 * L.ry2 * v * na) * sizeof(float);
+      if (nz > 1 && b > part) part = b;
+    }
+  }
+  part = (part + 1023) & ~size_t(1023);
+  tot += part;
   if (op && base) {
     char* p = base;
     op->L = L;
@@ -629,6 +699,7 @@ static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* 
     op->T1 = (float*)p; p += t1;
     op->ld1 = ld1;
     op->err = (int*)p; p += 1024;
+    op->part = part ? (float*)p : nullptr; p += part;
   }
   return tot;
 }
@@ -704,10 +775,20 @@ static void core_apply(SplitOp* op, int nvec, cudaStream_t s) {
 #undef TTG_CORE_SMALL
   } else {
     const i64 rows = L.rx1 * L.ry2 * nvec;
-    dim3 grid((unsigned)ceil_div(rows, (i64)tc::CT_R), (unsigned)ceil_div(na, tc::CT_P));
+    int nz, qchunk;
+    tc::core_chunks(rows, na, ja, nz, qchunk);
+    if (nz > 1 && !op->part) nz = 1, qchunk = ja;
+    float* part = nz > 1 ? op->part : nullptr;
+    dim3 grid((unsigned)ceil_div(rows, (i64)tc::CT_R), (unsigned)ceil_div(na, tc::CT_P), nz);
     tc::core_tiled_kernel<<<grid, 256, 0, s>>>(op->T1, op->ld1, op->A, (int)L.rx1, (int)L.m,
                                               (int)L.ra2, (int)L.n, (int)L.ra1, (int)L.ry2, nvec,
-                                              lgR3, T2.ktiles, T2.hi, T2.lo);
+                                              lgR3, T2.ktiles, T2.hi, T2.lo, qchunk, part);
+    if (part) {
+      TTG_CHECK_LAUNCH();
+      const i64 tot = rows * na;
+      tc::core_finish_kernel<<<(int)std::min<i64>(4096, ceil_div(tot, (i64)256)), 256, 0, s>>>(
+          part, nz, rows, na, (int)L.rx1, (int)L.n, (int)L.ra1, lgR3, T2.ktiles, T2.hi, T2.lo);
+    }
   }
   TTG_CHECK_LAUNCH();
 }
@@ -738,14 +819,36 @@ size_t split_matvec_bytes(const LocalDims& L, int nvec_max) {
   return split_op_bytes(L, nvec_max) + 4096;
 }
 
+// Two prepared operators per host thread (an operator and its adjoint).
+constexpr int kSplitSlots = 2;
+static thread_local SplitOp op_store[kSplitSlots];
+static thread_local bool op_store_set[kSplitSlots] = {};
+
 void split_matvec_factory(const LocalDims& L, const double* phi1, const double* A,
                           const double* phi2, int nvec_max, void* mem, cudaStream_t s,
-                          MatvecFn* out) {
-  static thread_local SplitOp op_store;
+                          MatvecFn* out, int slot) {
+  TTG_REQUIRE(slot >= 0 && slot < kSplitSlots, "split matvec: bad operator slot");
   TTG_REQUIRE(split_op_supported(L), "split matvec: local problem too large");
-  split_op_prepare(&op_store, L, nvec_max, phi1, A, phi2, mem, s);
-  SplitOp* op = &op_store;
+  op_store_set[slot] = true;
+  split_op_prepare(&op_store[slot], L, nvec_max, phi1, A, phi2, mem, s);
+  SplitOp* op = &op_store[slot];
   *out = [op, s](const double* X, double* Y, int nv) { split_op_apply(op, X, Y, nv, s); };
+}
+
+// Reads the bounded-wait flags of the calling thread's prepared split
+// operators (set by a GEMM whose mbarrier wait gave up); throws when set.
+void split_matvec_check(cudaStream_t s) {
+  int herr[kSplitSlots] = {};
+  bool any = false;
+  for (int k = 0; k < kSplitSlots; ++k) {
+    if (!op_store_set[k] || !op_store[k].err) continue;
+    TTG_CUDA(cudaMemcpyAsync(&herr[k], op_store[k].err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    any = true;
+  }
+  if (!any) return;
+  TTG_CUDA(cudaStreamSynchronize(s));
+  for (int k = 0; k < kSplitSlots; ++k)
+    if (herr[k]) throw Error{TTG_ERR_CUDA, "split gemm: mbarrier wait timed out"};
 }
 
 }  // namespace ttg

@@ -164,3 +164,28 @@ def random_tt_complex(d, n, r, seed=0):
         sz = ry[k] * n[k] * ry[k + 1]
         cores.append(rng.standard_normal(sz) + 1j * rng.standard_normal(sz))
     return list(n), ry, np.concatenate(cores)
+
+
+def tt_dot(d, n, rx, x, ry, y):
+    """Inner product sum(conj(x) * y) of two TT vectors given as flat
+    Fortran-ordered cores (r_k x n_k x r_{k+1}), contracted left to right."""
+    if np.isscalar(n):
+        n = [int(n)] * d
+    P = np.ones((1, 1), dtype=np.result_type(x, y))
+    ox = oy = 0
+    for k in range(d):
+        sx, sy = rx[k] * n[k] * rx[k + 1], ry[k] * n[k] * ry[k + 1]
+        X = np.asarray(x[ox:ox + sx]).reshape(rx[k], n[k], rx[k + 1], order="F")
+        Y = np.asarray(y[oy:oy + sy]).reshape(ry[k], n[k], ry[k + 1], order="F")
+        ox += sx
+        oy += sy
+        P = np.einsum("aic,ab,bie->ce", np.conj(X), P, Y, optimize=True)
+    return P[0, 0]
+
+
+def tt_rel_diff(d, n, rx, x, ry, y):
+    """||x - y|| / ||y|| of two TT vectors through TT inner products."""
+    xx = tt_dot(d, n, rx, x, rx, x).real
+    yy = tt_dot(d, n, ry, y, ry, y).real
+    xy = tt_dot(d, n, rx, x, ry, y).real
+    return float(np.sqrt(max(xx - 2 * xy + yy, 0.0) / yy))
