@@ -209,11 +209,13 @@ def bench_extra(args, torch, ttgpu, ctx):
         for meth in ("split", "plain"):
             ttgpu.ztt_ksl(16, n_, m_, ra_, crA_, y_, ry_, 1e-3, 64, nsteps=2, method=meth, ctx=ctx)
     res = {}
+    methods = args.methods.split(",")
     with ClockSampler() as clk:
-        for meth in ("split", "plain"):
+        for meth in methods:
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
             l0 = ttgpu.launch_count()
+            torch.cuda.profiler.start()   # the region a profiler started with capture off records
             e0.record()
             if args.workload == "xxz100":
                 d, Bx = 100, 8
@@ -228,8 +230,8 @@ def bench_extra(args, torch, ttgpu, ctx):
                 _, ry, y = random_tt_complex(d, nn, r, seed=2)
                 y = y.copy()
                 y[:ry[1] * nn] /= np.sqrt(tt_dot(d, n_, ry, y, ry, y).real)
-                cores, ry_out = ttgpu.ztt_ksl(d, n_, m_, ra, crA, y, ry, 1e-3, 64, nsteps=200,
-                                              method=meth, ctx=ctx)
+                cores, ry_out = ttgpu.ztt_ksl(d, n_, m_, ra, crA, y, ry, 1e-3, 64,
+                                              nsteps=args.ksl_steps, method=meth, ctx=ctx)
                 out = {"cores": cores, "ry": ry_out, "n": n_, "max_rank": max(ry_out)}
             else:
                 d, nn = 10, 64
@@ -241,10 +243,17 @@ def bench_extra(args, torch, ttgpu, ctx):
                 out = {"max_rank": max(rx_out), "res": ctx.stats()["res"]}
             e1.record()
             torch.cuda.synchronize()
+            torch.cuda.profiler.stop()
             out["time"] = e0.elapsed_time(e1) / 1e3
             out["launches"] = ttgpu.launch_count() - l0
             out["matvecs"] = ctx.stats()["matvecs"]
             res[meth] = out
+    if len(methods) != 2:
+        # one method only (profiling runs): its time and launches
+        print(json.dumps({"workload": args.workload, "ksl_steps": args.ksl_steps,
+                          **{m: {"time": res[m]["time"], "gpu_launches": int(res[m]["launches"])}
+                             for m in methods}}))
+        return
     sp, pl = res["split"], res["plain"]
     if args.workload == "xxz100":
         metric = "tt_eigb time of 2 sweeps (d=100 XXZ, delta=1, B=8, rmax=256)"
@@ -253,10 +262,32 @@ def bench_extra(args, torch, ttgpu, ctx):
         agree = float(np.max(np.abs(sp["lambda"] - pl["lambda"]) / np.abs(pl["lambda"])))
         extra = {"lambda_maxrel_vs_plain": agree, "lambda": sp["lambda"].tolist()}
     elif args.workload == "ksl16":
-        metric = "ztt_ksl time of 200 steps (d=16, n=32, -Laplacian + rank-4 N(0,0.01^2), rank 8)"
-        cfg = {"workload": "ztt_ksl d=16 n=32 ra=6 ry=8 tau=1e-3 nsteps=200 typ=2 order=8"}
+        ns = args.ksl_steps
+        metric = f"ztt_ksl time of {ns} steps (d=16, n=32, -Laplacian + rank-4 N(0,0.01^2), rank 8)"
+        cfg = {"workload": f"ztt_ksl d=16 n=32 ra=6 ry=8 tau=1e-3 nsteps={ns} typ=2 order=8"}
         extra = {"err_vs_fp64": tt_rel_diff(16, sp["n"], sp["ry"], sp["cores"], pl["ry"],
                                             pl["cores"])}
+        if not args.no_cpu:
+            # the oracle restatement on a bounded sample (10 of the 200 steps),
+            # scaled to the workload, and its state against the plain method's
+            from oracle.ksl import ztt_ksl as oracle_ksl
+            n_, m_, ra_, crA_ = ksl_operator(d=16, n=32, rank=4, std=0.01, seed=1)
+            _, ry_, y_ = random_tt_complex(16, 32, 8, seed=2)
+            y_ = y_.copy()
+            y_[:ry_[1] * 32] /= np.sqrt(tt_dot(16, n_, ry_, y_, ry_, y_).real)
+            c_, r_ = y_, list(ry_)
+            t0 = time.perf_counter()
+            for _ in range(10):
+                o = oracle_ksl(16, n_, m_, ra_, crA_, c_, r_, 1e-3, 64)
+                c_, r_ = o["cores"], o["ry"]
+            tc = time.perf_counter() - t0
+            g10, gr10 = ttgpu.ztt_ksl(16, n_, m_, ra_, crA_, y_, ry_, 1e-3, 64, nsteps=10,
+                                      method="plain", ctx=ctx)
+            extra["cpu_baseline"] = {
+                "value": tc * ns / 10, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+                "sample": f"10 of the {ns} steps with the oracle restatement (numpy + OpenBLAS "
+                          f"threads), time x {ns / 10:g}",
+                "plain_vs_oracle_10_steps": tt_rel_diff(16, n_, gr10, g10, r_, c_)}
         for o in (sp, pl):
             for k in ("cores", "ry", "n"):
                 o.pop(k)
@@ -284,6 +315,10 @@ def main():
     ap.add_argument("--method", default="split", choices=["split", "plain"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--methods", default="split,plain",
+                    help="larger workloads: the methods to time (one method: profiling runs)")
+    ap.add_argument("--ksl-steps", type=int, default=200,
+                    help="ksl16: time steps (the workload is 200)")
     ap.add_argument("--workload", default="heisenberg20",
                     choices=["heisenberg20", "xxz100", "amen10", "ksl16"])
     args = ap.parse_args()
