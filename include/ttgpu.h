@@ -139,6 +139,22 @@ int ttg_d2d_fullmat(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int r
                     ttg_int ra2, const double* phi1, const double* A, const double* phi2,
                     double* B);
 
+/* Block-Jacobi preconditioner of the local system, djac_gen
+ * tt_linalg.f90:363-494 (bind(c)): ptype 'c' (diagonals of Phi1 and Phi2, an
+ * n x n block per (b1,b2)), 'l' (Phi1 and the diagonal of Phi2, an
+ * (rx1 n)^2 block per b2) or 'r' (the diagonal of Phi1 and Phi2, an
+ * (n rx2)^2 block per b1); each block inverted by LU with partial pivoting.
+ * Device pointers; jacs receives ttg_djac_size(ptype, rx1, n, rx2) doubles in
+ * the reference's layout.  Blocks larger than 4096 are rejected. */
+ttg_int ttg_djac_size(char ptype, ttg_int rx1, ttg_int n, ttg_int rx2);
+int ttg_djac_gen(ttg_ctx* ctx, char ptype, ttg_int rx1, ttg_int n, ttg_int rx2, ttg_int ra1,
+                 ttg_int ra2, const double* phi1, const double* A, const double* phi2,
+                 double* jacs);
+/* y = P x with the blocks of ttg_djac_gen, djac_apply tt_linalg.f90:497-531;
+ * x and y (rx1, n, rx2) may be the same array. */
+int ttg_djac_apply(ttg_ctx* ctx, char ptype, ttg_int rx1, ttg_int n, ttg_int rx2,
+                   const double* jacs, const double* x, double* y);
+
 /* ------------------------------------------------ dense algebra (device) */
 /* A (n x m) -> Q (n x min(n,m)) in place, R (min(n,m) x m): dqr
  * matrix_util.f90:37-61 (bind(c) twin tt_linalg.f90:30); zqr :64-90. */
@@ -211,8 +227,9 @@ int ttg_ksl_z(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m, const
 /* AMEn linear solve A x = y, tt_amen_solve tt_adapt_als.f90:513-1132
  * (argument order follows it; rx updated in place).  kickrank 4, nswp 20,
  * prec 'n', nrestart 40, niters 2 are the reference's defaults (pass them,
- * or values <= 0 / 0 for the defaults of nswp, nrestart, niters); only the
- * 'n' preconditioner is built (others return TTG_ERR_UNSUPPORTED).  rmax
+ * or values <= 0 / 0 for the defaults of nswp, nrestart, niters); prec 'c',
+ * 'l', 'r' right-precondition each local GMRES with the block-Jacobi blocks
+ * of ttg_djac_gen, regenerated per local system as the reference does.  rmax
  * caps the kept ranks (<= 0: no cap, as in the reference). */
 int ttg_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
                    const ttg_int* ry, const ttg_int* ra, const double* crA, const double* crY,

@@ -21,7 +21,11 @@ AMEn of tt_adapt_als.f90:513-1132, a different algorithm from ``dtt_amen_solve``
   * when a whole half sweep ends with res_max < eps the kick is switched
     off (kickrank = -1) and the next end of a half sweep stops       :1066-1105
 
-Only the 'n' preconditioner (none, the default) is restated.
+Preconditioners: 'n' (none, the default) and the block-Jacobi 'c', 'l', 'r'
+of djac_gen / djac_apply (``oracle/jac.py``), regenerated for every local
+system that GMRES solves (:746-769); GMRES is right-preconditioned, i.e. it
+solves (A P) z = r and the correction is P z (tt_linalg.f90:689-690,733-735;
+tt_adapt_als.f90:776-781).
 
 One detail is kept as the reference has it: ``dbfun3_left``
 (tt_linalg.f90:242-253) transposes Phi1 into a work array but multiplies
@@ -33,6 +37,7 @@ import scipy.linalg as sla
 
 from .ops import F, flat, dtransp, bfun3, phi_left, phi_right, phi2_left, phi2_right, dqr
 from .amen import gmres_hh
+from .jac import jac_gen, jac_apply
 
 
 def bfun3_left(rx1, m, rx2, ry1, n, ra1, ra2, phi1, A, x):
@@ -88,7 +93,7 @@ def uchol(trans, m, n, dA, numvec):
 
 
 def tt_amen_solve(d, n, m, ry, ra, crA, crY, crX0, rx, eps, kickrank=4, nswp=20, nrestart=40,
-                  niters=2):
+                  niters=2, prec="n"):
     """Restatement of tt_amen_solve (tt_adapt_als.f90:513).  Returns a dict
     with ``cores`` (result_core layout), ``rx``, ``sweeps``, ``res_max`` (of
     the last finished half sweep) and ``matvecs``."""
@@ -158,7 +163,14 @@ def tt_amen_solve(d, n, m, ry, ra, crA, crY, crX0, rx, eps, kickrank=4, nswp=20,
         res_max = max(res_max, err)
         tau = eps2 / (err * 2.0)
         if tau < 1.0:
-            dx, k_mv, _ = gmres_hh(lambda v: mvk(i, v), r0, min(nrestart, nn), tau, niters)
+            if prec.lower() in ("c", "l", "r"):
+                jacs = jac_gen(prec, rx[i], n[i], rx[i + 1], ra[i], ra[i + 1], phiA[i], A[i],
+                               phiA[i + 1])
+                pj = lambda v: jac_apply(prec, rx[i], n[i], rx[i + 1], jacs, v)  # noqa: E731
+                z, k_mv, _ = gmres_hh(lambda v: mvk(i, pj(v)), r0, min(nrestart, nn), tau, niters)
+                dx = pj(z)
+            else:
+                dx, k_mv, _ = gmres_hh(lambda v: mvk(i, v), r0, min(nrestart, nn), tau, niters)
             nmv += k_mv
             cr[i] = cr[i] - dx
             res_new = np.linalg.norm(mvk(i, cr[i]) - rhs) / norm_rhs

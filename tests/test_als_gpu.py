@@ -47,4 +47,24 @@ def test_als_without_kick_and_unsupported_prec(ctx):
     xg = tt_full(d, nn, rx1, cores)
     assert np.linalg.norm(A @ xg - yf) <= 10 * eps * np.linalg.norm(yf)
     with pytest.raises(RuntimeError):
-        ttgpu.tt_amen_solve(d, nn, mm, ry, ra, crA, y, x0, rx, eps, prec="c", ctx=ctx)
+        ttgpu.tt_amen_solve(d, nn, mm, ry, ra, crA, y, x0, rx, eps, prec="x", ctx=ctx)
+
+
+@pytest.mark.parametrize("prec", ["c", "l", "r"])
+def test_als_block_jacobi_preconditioners(ctx, prec):
+    """prec 'c' / 'l' / 'r' (djac_gen / djac_apply, right preconditioning):
+    the GPU meets the stopping test against the dense operator and agrees with
+    the oracle run with the same preconditioner."""
+    import ttgpu
+    d, n, eps = 5, 6, 1e-9
+    nn, mm, ra, crA = amen_operator(d=d, n=n)
+    _, ry, y = random_tt(d, n, 2, seed=3)
+    _, rx, x0 = random_tt(d, n, 2, seed=7)
+    cores, rx1 = ttgpu.tt_amen_solve(d, nn, mm, ry, ra, crA, y, x0, rx, eps, prec=prec, ctx=ctx)
+    A = tt_matrix_full(d, nn, ra, crA)
+    yf = tt_full(d, nn, ry, y)
+    xg = tt_full(d, nn, rx1, cores)
+    assert np.linalg.norm(A @ xg - yf) <= eps * np.linalg.norm(yf)
+    ref = oracle_als(d, nn, mm, ry, ra, crA, y, x0, rx, eps, prec=prec)
+    xo = tt_full(d, nn, ref["rx"], ref["cores"])
+    assert np.linalg.norm(xg - xo) <= 100 * eps * np.linalg.norm(xo)

@@ -925,6 +925,28 @@ struct AlsParams {
   double eps;
   i64 rmax;
   int kick, nswp, nrestart, niters, verb;
+  char prec = 0;   // 0 (none) or the block-Jacobi type 'c', 'l', 'r'
+};
+
+// device array that grows on demand (block-Jacobi blocks: their size follows
+// the current ranks, which the rank capacities bound only loosely)
+struct GrowBuf {
+  double* p = nullptr;
+  size_t cap = 0;
+  ~GrowBuf() { if (p) cudaFree(p); }
+  double* ensure(size_t count, cudaStream_t s) {
+    if (count <= cap) return p;
+    TTG_CUDA(cudaStreamSynchronize(s));
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    if (cudaMalloc(&p, count * sizeof(double)) != cudaSuccess) {
+      p = nullptr;
+      throw Error{TTG_ERR_NOMEM, "amen: preconditioner allocation failed"};
+    }
+    cap = count;
+    return p;
+  }
 };
 
 class AlsSolver {
@@ -943,6 +965,7 @@ class AlsSolver {
   int* ired_;
   double* h_ = nullptr;
   long long nmv_ = 0;
+  GrowBuf jacs_, jscr_;
   static constexpr int kBatch = 8;
 
   void sync() { TTG_CUDA(cudaStreamSynchronize(s_)); }
@@ -1239,9 +1262,26 @@ void AlsSolver::run(AmenOut& out) {
     double res_new = err;
     const double tau = eps2 / (err * 2.0);
     if (tau < 1.0) {
-      auto mvf = [&](const double* in, double* o, int nv) { mv(i, in, o, nv); };
-      gmres_cgs2(mvf, N, r0_, sol_, tau, (int)std::min<i64>(std::min<i64>(P_.nrestart, N), 60),
-                 P_.niters, G, s_);
+      const int nrs = (int)std::min<i64>(std::min<i64>(P_.nrestart, N), 60);
+      if (P_.prec) {
+        // right preconditioning (tt_linalg.f90:689-690,733-735): GMRES on A P,
+        // correction P z (tt_adapt_als.f90:746-781); cand_ holds P v
+        const char pt = P_.prec;
+        const i64 nk_ = nk;
+        double* jacs = jacs_.ensure((size_t)jac_size(pt, r1, nk_, r2), s_);
+        double* jscr = jscr_.ensure((size_t)jac_gen_scratch(pt, r1, nk_, r2, ra[i], ra[i + 1]), s_);
+        jac_gen_f64(pt, r1, nk_, r2, ra[i], ra[i + 1], phiA_[i], A_[i], phiA_[i + 1], jacs, jscr, s_);
+        auto mvf = [&](const double* in, double* o, int nv) {
+          jac_apply_f64(pt, r1, nk_, r2, jacs, in, cand_, nv, s_);
+          mv(i, cand_, o, nv);
+        };
+        gmres_cgs2(mvf, N, r0_, sol_, tau, nrs, P_.niters, G, s_);
+        jac_apply_f64(pt, r1, nk_, r2, jacs, sol_, candY_, 1, s_);
+        TTG_CUDA(cudaMemcpyAsync(sol_, candY_, sizeof(double) * N, cudaMemcpyDeviceToDevice, s_));
+      } else {
+        auto mvf = [&](const double* in, double* o, int nv) { mv(i, in, o, nv); };
+        gmres_cgs2(mvf, N, r0_, sol_, tau, nrs, P_.niters, G, s_);
+      }
       sub_kernel<<<eb(N), 256, 0, s_>>>(N, x_[i], sol_, x_[i]);
       TTG_CHECK_LAUNCH();
       mv(i, x_[i], r0_, 1);
@@ -1440,8 +1480,8 @@ extern "C" int ttg_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const t
     TTG_CUDA(cudaSetDevice(ctx->device));
     TTG_REQUIRE(d > 1 && n && m && ry && ra && crA && crY && crX0 && rx, "null argument");
     TTG_REQUIRE(method == TTG_METHOD_PLAIN, "amen: only the FP64 method is built");
-    if (prec != 'n' && prec != 'N' && prec != 0)
-      throw Error{TTG_ERR_UNSUPPORTED, "amen: only the 'n' preconditioner is built"};
+    TTG_REQUIRE(prec == 'n' || prec == 'N' || prec == 0 || jac_type(prec),
+                "amen: prec must be 'n', 'c', 'l' or 'r'");
     for (int k = 0; k < d; ++k) TTG_REQUIRE(n[k] == m[k], "amen needs square cores (n == m)");
     TTG_REQUIRE(kickrank <= 16, "amen: kickrank > 16");
     AlsParams P;
@@ -1458,6 +1498,7 @@ extern "C" int ttg_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const t
     P.nrestart = nrestart > 0 ? (int)nrestart : 40;
     P.niters = niters > 0 ? (int)niters : 2;
     P.verb = verb;
+    P.prec = jac_type(prec);
     long long l0 = g_launches;
     AmenOut out;
     AlsSolver solver(ctx, P);

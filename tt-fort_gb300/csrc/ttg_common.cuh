@@ -209,6 +209,16 @@ void phi_right_z(const LocalDims& L, const double2* phi2_old, const double2* A,
                  const double2* x, const double2* y, double2* phi2_new, double2* scratch,
                  cudaStream_t s);
 
+// Block-Jacobi preconditioners of the local system (ttg_jac.cu; djac_gen /
+// djac_apply): jac_type normalises 'c'/'l'/'r' (0 if none), sizes in doubles.
+char jac_type(char p);
+i64 jac_size(char p, i64 rx1, i64 n, i64 rx2);
+i64 jac_gen_scratch(char p, i64 rx1, i64 n, i64 rx2, i64 ra1, i64 ra2);
+void jac_gen_f64(char p, i64 rx1, i64 n, i64 rx2, i64 ra1, i64 ra2, const double* phi1,
+                 const double* A, const double* phi2, double* jacs, double* scr, cudaStream_t s);
+void jac_apply_f64(char p, i64 rx1, i64 n, i64 rx2, const double* jacs, const double* x,
+                   double* y, int nvec, cudaStream_t s);
+
 // ---------------------------------------------------------------------------
 // Split-precision (BF16x3, FP32 accumulate) tensor-core local operator
 // (ttg_tc.cu).  Operands are prepared once per local problem.

@@ -53,6 +53,8 @@ def lib():
         L.ttg_my_chop3.restype = _i64
         L.ttg_my_chop3.argtypes = [_i64, C.c_void_p, C.c_double]
         L.ttg_launch_count.restype = _i64
+        L.ttg_djac_size.restype = _i64
+        L.ttg_djac_size.argtypes = [C.c_char, _i64, _i64, _i64]
         L.ttg_mlp_nparams.restype = _i64
         L.ttg_mlp_nparams.argtypes = [C.c_void_p]
         _lib = L
@@ -72,7 +74,8 @@ EXPORTED = [
     "ttg_mlp_set_params", "ttg_mlp_get_grads", "ttg_mlp_forward", "ttg_mlp_loss_grad",
     "ttg_mlp_adam_step", "ttg_set_learned", "ttg_record_count", "ttg_record_clear",
     "ttg_mlp_train_recorded", "ttg_batch_create", "ttg_batch_destroy", "ttg_batch_add_eigb",
-    "ttg_batch_run", "ttg_batch_result", "ttg_batch_cores",
+    "ttg_batch_run", "ttg_batch_result", "ttg_batch_cores", "ttg_djac_size", "ttg_djac_gen",
+    "ttg_djac_apply",
 ]
 
 
@@ -266,6 +269,27 @@ def dbfun3(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1, A, phi2, x, y, nvec=1, spli
     f = lib().ttg_dbfun3_split if split else lib().ttg_dbfun3
     ctx.check(f(ctx.handle, *_dims(rx1, m, rx2, ry1, n, ry2, ra1, ra2), _dev(phi1), _dev(A),
                 _dev(phi2), _dev(x), _dev(y), _i64(nvec)))
+
+
+def djac_size(ptype, rx1, n, rx2):
+    """Doubles of the block-Jacobi preconditioner (djac_gen, tt_linalg.f90:363)."""
+    return int(lib().ttg_djac_size(ptype.encode(), rx1, n, rx2))
+
+
+def djac_gen(ptype, rx1, n, rx2, ra1, ra2, phi1, A, phi2, jacs, ctx=None):
+    """Block-Jacobi blocks of the local system into jacs (djac_gen,
+    tt_linalg.f90:363-494); torch CUDA tensors."""
+    ctx = _kctx(ctx)
+    ctx.check(lib().ttg_djac_gen(ctx.handle, C.c_char(ptype.encode()), _i64(rx1), _i64(n),
+                                 _i64(rx2), _i64(ra1), _i64(ra2), _dev(phi1), _dev(A), _dev(phi2),
+                                 _dev(jacs)))
+
+
+def djac_apply(ptype, rx1, n, rx2, jacs, x, y, ctx=None):
+    """y = P x with the blocks of djac_gen (djac_apply, tt_linalg.f90:497-531)."""
+    ctx = _kctx(ctx)
+    ctx.check(lib().ttg_djac_apply(ctx.handle, C.c_char(ptype.encode()), _i64(rx1), _i64(n),
+                                   _i64(rx2), _dev(jacs), _dev(x), _dev(y)))
 
 
 def zbfun3(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1, A, phi2, x, y, nvec=1, transp=False,
