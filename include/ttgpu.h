@@ -224,6 +224,15 @@ int ttg_eigb(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m, const 
 int ttg_ksl_z(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m, const ttg_int* ra,
               const double* crA, const double* crY0, ttg_int* ry, double tau, ttg_int rmax,
               int verb, int typ, int order, int method, ttg_int nsteps);
+/* AMEn matvec y ~ A x, tt_mvk4 tt_adapt_als.f90:67-500 (argument order
+ * follows it; crY0 with ranks ry is the start, ry updated in place).
+ * kickrank 5 and nswp 20 are the reference's defaults (nswp <= 0: 20); the
+ * sweep stops when a sweep's largest relative core change is below eps.  The
+ * reference's rmax only sizes its work arrays; here it caps the kept ranks.
+ * The result cores are read with ttg_result_copy. */
+int ttg_mvk4(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m, const ttg_int* rx,
+             const ttg_int* ra, const double* crA, const double* crX, const double* crY0,
+             ttg_int* ry, double eps, ttg_int rmax, ttg_int kickrank, ttg_int nswp, int verb);
 /* AMEn linear solve A x = y, tt_amen_solve tt_adapt_als.f90:513-1132
  * (argument order follows it; rx updated in place).  kickrank 4, nswp 20,
  * prec 'n', nrestart 40, niters 2 are the reference's defaults (pass them,

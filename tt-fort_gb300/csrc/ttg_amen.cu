@@ -918,6 +918,82 @@ __global__ void uchol_dv_kernel(int k, const double* __restrict__ R, const doubl
 
 }  // namespace
 
+// buffers of uchol_run: small >= 1024 doubles, dd and tmp >= n (and n * k),
+// tau >= 16, h pinned host, ired >= 16 ints
+struct UcholWork {
+  double *small, *dd, *tmp, *tau, *h;
+  int* ired;
+};
+
+// duchol_fort (tt_linalg.f90:540-642).  trans: dA is n x m, else m x n.
+// Writes du (n x real) and returns real (the Fortran loop index: numvec, or
+// the failing step when the pivot vanishes).
+static int uchol_run(bool trans, i64 m, i64 n, const double* dA, int numvec, double* du,
+                     const UcholWork& W, cudaStream_t s) {
+  TTG_REQUIRE(numvec <= 16, "uchol: at most 16 vectors");
+  const i64 si = trans ? 1 : m, sk = trans ? n : 1;
+  double* lam = W.small;          // numvec <= 16
+  double* Rk = W.small + 16;      // k x k
+  double* dv = W.small + 272;     // k x k
+  double* V = W.small + 528;      // k x k
+  double* piv = W.small + 784;
+  TTG_CUDA(cudaMemsetAsync(lam, 0, sizeof(double) * 16, s));
+  TTG_CUDA(cudaMemsetAsync(du, 0, sizeof(double) * n * numvec, s));
+  uchol_diag_kernel<<<eb(n), 256, 0, s>>>(n, m, dA, si, sk, W.dd);
+  TTG_CHECK_LAUNCH();
+  int cnt = 0;
+  bool broke = false;
+  while (cnt < numvec) {
+    argmax_abs_kernel<<<1, 256, 0, s>>>(n, W.dd, W.ired);
+    TTG_CHECK_LAUNCH();
+    uchol_col_kernel<<<eb(n), 256, 0, s>>>(n, m, dA, si, sk, W.ired, cnt, lam, du);
+    TTG_CHECK_LAUNCH();
+    uchol_pick_kernel<<<1, 1, 0, s>>>(n, W.ired, cnt, du, piv);
+    TTG_CHECK_LAUNCH();
+    TTG_CUDA(cudaMemcpyAsync(W.h, piv, sizeof(double), cudaMemcpyDeviceToHost, s));
+    TTG_CUDA(cudaStreamSynchronize(s));
+    if (std::sqrt(std::fabs(W.h[0])) < 1e-300) { broke = true; break; }
+    uchol_scale_kernel<<<eb(n), 256, 0, s>>>(n, cnt, piv, du, W.dd);
+    TTG_CHECK_LAUNCH();
+    const int k = cnt + 1;
+    qr_householder((int)n, k, du, Rk, W.tau, s);          // du[:, :k] = Q, Rk = R
+    uchol_dv_kernel<<<1, 256, 0, s>>>(k, Rk, lam, dv);
+    TTG_CHECK_LAUNCH();
+    syev_jacobi(k, dv, k, lam, V, k, W.ired + 8, s);      // ascending, as dsyev
+    GemmF64 g;
+    g.M = (int)n; g.N = k; g.K = k;
+    g.A = du; g.sAm = 1; g.sAk = n;
+    g.B = V; g.sBk = 1; g.sBn = k;
+    g.C = W.tmp; g.sCm = 1; g.sCn = n;
+    gemm_f64(g, s);
+    TTG_CUDA(cudaMemcpyAsync(du, W.tmp, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, s));
+    ++cnt;
+  }
+  return broke ? cnt + 1 : numvec;
+}
+
+// dbfun3_right (tt_linalg.f90:210-240): y (rx1 ra1) x (n ry2) from x
+// (rx1, m, rx2) and Phi2 (rx2, ra2, ry2); tA, tB hold
+// max(rx1 m ra2 ry2, ra1 n ry2 rx1) doubles each.
+static void bfun3_right_run(i64 rx1, i64 m, i64 rx2, i64 n, i64 ry2, i64 ra1, i64 ra2,
+                            const double* A, const double* phi2, const double* x, double* y,
+                            double* tA, double* tB, cudaStream_t s) {
+  auto gemm = [&](int M, int N, int K, const double* Am, i64 sAm, i64 sAk, const double* Bm,
+                  i64 sBk, i64 sBn, double* C, i64 sCm, i64 sCn) {
+    GemmF64 g;
+    g.M = M; g.N = N; g.K = K;
+    g.A = Am; g.sAm = sAm; g.sAk = sAk;
+    g.B = Bm; g.sBk = sBk; g.sBn = sBn;
+    g.C = C; g.sCm = sCm; g.sCn = sCn;
+    gemm_f64(g, s);
+  };
+  gemm((int)(rx1 * m), (int)(ra2 * ry2), (int)rx2, x, 1, rx1 * m, phi2, 1, rx2, tA, 1, rx1 * m);
+  transpose_f64(rx1, m * ra2 * ry2, tA, tB, s);                             // j,a2,c2,b1
+  gemm((int)(ra1 * n), (int)(ry2 * rx1), (int)(m * ra2), A, 1, ra1 * n, tB, 1, m * ra2, tA, 1,
+       ra1 * n);                                                           // a1,i,c2,b1
+  transpose_f64(ra1 * n * ry2, rx1, tA, y, s);                              // b1,a1,i,c2
+}
+
 struct AlsParams {
   int d;
   std::vector<i64> n, ra, ry, rx;
@@ -1048,44 +1124,8 @@ int AlsSolver::scan(int i, int rmin, const double* L, i64 ldl, const double* Rr,
   return 1;
 }
 
-// duchol_fort (tt_linalg.f90:540-642).  trans: dA is n x m, else m x n.
-// Writes du (n x real) and returns real (the Fortran loop index: numvec, or
-// the failing step when the pivot vanishes).
 int AlsSolver::uchol(bool trans, i64 m, i64 n, const double* dA, int numvec, double* du) {
-  const i64 si = trans ? 1 : m, sk = trans ? n : 1;
-  double* lam = small_;          // numvec <= 16
-  double* Rk = small_ + 16;      // k x k
-  double* dv = small_ + 272;     // k x k
-  double* V = small_ + 528;      // k x k
-  double* piv = small_ + 784;
-  TTG_CUDA(cudaMemsetAsync(lam, 0, sizeof(double) * 16, s_));
-  TTG_CUDA(cudaMemsetAsync(du, 0, sizeof(double) * n * numvec, s_));
-  uchol_diag_kernel<<<eb(n), 256, 0, s_>>>(n, m, dA, si, sk, dd_);
-  TTG_CHECK_LAUNCH();
-  int cnt = 0;
-  bool broke = false;
-  while (cnt < numvec) {
-    argmax_abs_kernel<<<1, 256, 0, s_>>>(n, dd_, ired_);
-    TTG_CHECK_LAUNCH();
-    uchol_col_kernel<<<eb(n), 256, 0, s_>>>(n, m, dA, si, sk, ired_, cnt, lam, du);
-    TTG_CHECK_LAUNCH();
-    uchol_pick_kernel<<<1, 1, 0, s_>>>(n, ired_, cnt, du, piv);
-    TTG_CHECK_LAUNCH();
-    TTG_CUDA(cudaMemcpyAsync(h_, piv, sizeof(double), cudaMemcpyDeviceToHost, s_));
-    sync();
-    if (std::sqrt(std::fabs(h_[0])) < 1e-300) { broke = true; break; }
-    uchol_scale_kernel<<<eb(n), 256, 0, s_>>>(n, cnt, piv, du, dd_);
-    TTG_CHECK_LAUNCH();
-    const int k = cnt + 1;
-    qr(n, k, du, Rk);                                     // du[:, :k] = Q, Rk = R
-    uchol_dv_kernel<<<1, 256, 0, s_>>>(k, Rk, lam, dv);
-    TTG_CHECK_LAUNCH();
-    syev_jacobi(k, dv, k, lam, V, k, ired_ + 8, s_);      // ascending, as dsyev
-    gemm((int)n, k, k, du, 1, n, V, 1, k, tmp_, 1, n);
-    TTG_CUDA(cudaMemcpyAsync(du, tmp_, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, s_));
-    ++cnt;
-  }
-  return broke ? cnt + 1 : numvec;
+  return uchol_run(trans, m, n, dA, numvec, du, UcholWork{small_, dd_, tmp_, tau_, h_, ired_}, s_);
 }
 
 // dbfun3_left as the reference writes it (tt_linalg.f90:242-253): Phi1's
@@ -1108,14 +1148,8 @@ void AlsSolver::bfun3_left(int i, const double* x, double* y) {
 
 // dbfun3_right (tt_linalg.f90:210-240): y (rx1 ra1) x (n ry2), ry2 = rx2
 void AlsSolver::bfun3_right(int i, const double* x, double* y) {
-  const i64 rx1 = rx_[i], m = n_[i], rx2 = rx_[i + 1], ry2 = rx2, n = m;
-  const i64 ra1 = P_.ra[i], ra2 = P_.ra[i + 1];
-  gemm((int)(rx1 * m), (int)(ra2 * ry2), (int)rx2, x, 1, rx1 * m, phiA_[i + 1], 1, rx2, tA_, 1,
-       rx1 * m);                                                           // b1,j,a2,c2
-  transpose_f64(rx1, m * ra2 * ry2, tA_, tB_, s_);                          // j,a2,c2,b1
-  gemm((int)(ra1 * n), (int)(ry2 * rx1), (int)(m * ra2), A_[i], 1, ra1 * n, tB_, 1, m * ra2, tA_,
-       1, ra1 * n);                                                        // a1,i,c2,b1
-  transpose_f64(ra1 * n * ry2, rx1, tA_, y, s_);                            // b1,a1,i,c2
+  bfun3_right_run(rx_[i], n_[i], rx_[i + 1], n_[i], rx_[i + 1], P_.ra[i], P_.ra[i + 1], A_[i],
+                  phiA_[i + 1], x, y, tA_, tB_, s_);
 }
 
 void AlsSolver::run(AmenOut& out) {
@@ -1417,6 +1451,282 @@ void AlsSolver::run(AmenOut& out) {
   out.matvecs = nmv_;
 }
 
+// ---------------------------------------------------------------------------
+// tt_mvk4 (tt_adapt_als.f90:67-500): y ~ A x by alternating projections.
+// The interfaces phi = Y'AX (ry, rx, ra) come from dphi_left/right with x and
+// y different tensors; the projected core is dbfun3 of x's core; going left
+// the kept rank is my_chop3 of the SVD plus a kick of min(kickrank, n ry2)
+// incremental-Cholesky vectors of dbfun3_right (the right-going kick is off
+// in the reference, so none is added going right).
+// ---------------------------------------------------------------------------
+struct MvkParams {
+  int d;
+  std::vector<i64> n, m, rx, ra, ry;
+  const double *crA, *crX, *crY0;
+  double eps;
+  i64 rmax;
+  int kick, nswp, verb;
+};
+
+class MvkSolver {
+ public:
+  MvkSolver(ttg_ctx* ctx, const MvkParams& P) : P_(P), s_(ctx->stream) {}
+  void run(AmenOut& out);
+
+ private:
+  MvkParams P_;
+  cudaStream_t s_;
+  Arena mem_;
+  std::vector<i64> ry_, cap_;
+  std::vector<double*> y_, A_, X_, phi_;
+  double *cur_, *diff_, *red_, *U_, *S_, *Vt_, *svScr_, *Um_, *Rm_, *Rq_, *tmp_, *full_, *tA_,
+      *tB_, *scr_, *du_, *dd_, *small_, *tau_;
+  int* ired_;
+  double* h_ = nullptr;
+
+  LocalDims dims(int i) const {
+    return LocalDims{P_.rx[i], P_.m[i], P_.rx[i + 1], ry_[i], P_.n[i], ry_[i + 1], P_.ra[i], P_.ra[i + 1]};
+  }
+  void sync() { TTG_CUDA(cudaStreamSynchronize(s_)); }
+  void gemm(int M, int N, int K, const double* A, i64 sAm, i64 sAk, const double* B, i64 sBk,
+            i64 sBn, double* C, i64 sCm, i64 sCn) {
+    GemmF64 g;
+    g.M = M; g.N = N; g.K = K;
+    g.A = A; g.sAm = sAm; g.sAk = sAk;
+    g.B = B; g.sBk = sBk; g.sBn = sBn;
+    g.C = C; g.sCm = sCm; g.sCn = sCn;
+    gemm_f64(g, s_);
+  }
+  double norm2(const double* v, i64 n) {
+    TTG_CUDA(cudaMemsetAsync(red_, 0, sizeof(double), s_));
+    int bx = (int)std::max<i64>(1, std::min<i64>(256, (n + 2047) / 2048));
+    sqnorm_cols_kernel<<<dim3(bx, 1), 256, 0, s_>>>(n, v, n, red_);
+    TTG_CHECK_LAUNCH();
+    TTG_CUDA(cudaMemcpyAsync(h_, red_, sizeof(double), cudaMemcpyDeviceToHost, s_));
+    sync();
+    return std::sqrt(h_[0]);
+  }
+  // my_chop3 of the rmin singular values in S_, capped at rmax
+  int chop(int rmin, double eps2) {
+    TTG_REQUIRE(rmin <= 4096, "tt_mvk4: rank above 4096");
+    TTG_CUDA(cudaMemcpyAsync(h_, S_, sizeof(double) * rmin, cudaMemcpyDeviceToHost, s_));
+    sync();
+    return (int)std::min<i64>(ttg_my_chop3(rmin, h_, eps2), P_.rmax);
+  }
+};
+
+void MvkSolver::run(AmenOut& out) {
+  const int d = P_.d;
+  const auto& n = P_.n;
+  const auto& m = P_.m;
+  const auto& rx = P_.rx;
+  const auto& ra = P_.ra;
+  ry_ = P_.ry;
+  TTG_REQUIRE(d >= 2, "tt_mvk4: d must be >= 2");
+  TTG_REQUIRE(rx[0] == 1 && rx[d] == 1 && ry_[0] == 1 && ry_[d] == 1 && ra[0] == 1 && ra[d] == 1,
+              "boundary ranks must be 1");
+  const double eps2 = P_.eps / std::sqrt((double)d);
+  const int kick = P_.kick;
+  const int kpad = std::max(kick, 0);
+  std::vector<i64> left(d + 1, 1), right(d + 1, 1);
+  for (int k = 1; k <= d; ++k) left[k] = std::min<i64>(left[k - 1] * n[k - 1], 1ll << 40);
+  for (int k = d - 1; k >= 0; --k) right[k] = std::min<i64>(right[k + 1] * n[k], 1ll << 40);
+  cap_.assign(d + 1, 1);
+  for (int k = 1; k < d; ++k)
+    cap_[k] = std::max(ry_[k], std::min(P_.rmax, std::min(left[k], right[k])) + kpad);
+  i64 Nmax = 1, Mmax = 1, cmax = 1, T = 1, FB = 1, PH = 1, SVDU = 1;
+  size_t scr = 0, svs = 0;
+  for (int k = 0; k <= d; ++k) cmax = std::max(cmax, cap_[k]);
+  for (int k = 0; k < d; ++k) {
+    const i64 c1 = cap_[k], c2 = cap_[k + 1], nk = n[k];
+    Nmax = std::max(Nmax, c1 * nk * c2);
+    Mmax = std::max(Mmax, std::max(c1 * nk, nk * c2));
+    LocalDims L{rx[k], m[k], rx[k + 1], c1, nk, c2, ra[k], ra[k + 1]};
+    scr = std::max(scr, bfun3_f64_scratch(L, 1));
+    scr = std::max(scr, phi_f64_scratch(L));
+    T = std::max(T, std::max(rx[k] * m[k] * ra[k + 1] * c2, ra[k] * nk * c2 * rx[k]));
+    FB = std::max(FB, rx[k] * ra[k] * nk * c2);
+    svs = std::max(svs, svd_scratch((int)(c1 * nk), (int)c2));
+    svs = std::max(svs, svd_scratch((int)c1, (int)(nk * c2)));
+    SVDU = std::max(SVDU, std::max(c1 * nk, nk * c2) * std::min(std::max(c1 * nk, nk * c2), std::max(c1, c2)));
+  }
+  for (int k = 0; k <= d; ++k) PH = std::max(PH, cap_[k] * rx[k] * ra[k]);
+  const i64 M2 = std::max(Nmax, Mmax * (cmax + kpad));
+  const i64 R2 = (cmax + kpad) * (cmax + kpad);
+  i64 at = 0, xt = 0;
+  for (int k = 0; k < d; ++k) {
+    at += ra[k] * n[k] * m[k] * ra[k + 1];
+    xt += rx[k] * m[k] * rx[k + 1];
+  }
+  size_t total = al8(at) + al8(xt);
+  for (int k = 0; k < d; ++k) total += al8(cap_[k] * n[k] * cap_[k + 1]);
+  for (int k = 0; k <= d; ++k) total += al8(std::max<i64>(1, cap_[k] * rx[k] * ra[k]));
+  total += 2 * al8(Nmax) + al8(64) + 2 * al8(SVDU) + al8(4096) + svs + 256 + al8(M2) +
+           2 * al8(R2) + al8(M2) + al8(FB) + 2 * al8(T) + scr + 256 + al8(Mmax * 16) +
+           al8(Mmax) + al8(1024) + al8(8192) + al8(64) + (1 << 16);
+  mem_.alloc(total);
+  double* dA = mem_.take(at);
+  double* dX = mem_.take(xt);
+  A_.resize(d); X_.resize(d); y_.resize(d); phi_.resize(d + 1);
+  {
+    i64 oa = 0, ox = 0;
+    for (int k = 0; k < d; ++k) {
+      A_[k] = dA + oa; oa += ra[k] * n[k] * m[k] * ra[k + 1];
+      X_[k] = dX + ox; ox += rx[k] * m[k] * rx[k + 1];
+    }
+  }
+  for (int k = 0; k < d; ++k) y_[k] = mem_.take(cap_[k] * n[k] * cap_[k + 1]);
+  for (int k = 0; k <= d; ++k) phi_[k] = mem_.take(std::max<i64>(1, cap_[k] * rx[k] * ra[k]));
+  cur_ = mem_.take(Nmax); diff_ = mem_.take(Nmax);
+  red_ = mem_.take(64);
+  U_ = mem_.take(SVDU); Vt_ = mem_.take(SVDU); S_ = mem_.take(4096);
+  svScr_ = (double*)mem_.take(svs / sizeof(double) + 1);
+  Um_ = mem_.take(M2); Rm_ = mem_.take(R2); Rq_ = mem_.take(R2); tmp_ = mem_.take(M2);
+  full_ = mem_.take(FB); tA_ = mem_.take(T); tB_ = mem_.take(T);
+  scr_ = (double*)mem_.take(scr / sizeof(double) + 1);
+  du_ = mem_.take(Mmax * 16); dd_ = mem_.take(Mmax); small_ = mem_.take(1024);
+  tau_ = mem_.take(8192);
+  ired_ = (int*)mem_.take(64);
+  TTG_CUDA(cudaMallocHost(&h_, 4096 * sizeof(double)));
+  struct HG { double* p; ~HG() { if (p) cudaFreeHost(p); } } hg{h_};
+  const UcholWork UW{small_, dd_, tmp_, tau_, h_, ired_};
+
+  TTG_CUDA(cudaMemcpyAsync(dA, P_.crA, sizeof(double) * at, cudaMemcpyHostToDevice, s_));
+  TTG_CUDA(cudaMemcpyAsync(dX, P_.crX, sizeof(double) * xt, cudaMemcpyHostToDevice, s_));
+  {
+    i64 oy = 0;
+    for (int k = 0; k < d; ++k) {
+      const i64 sz = ry_[k] * n[k] * ry_[k + 1];
+      TTG_CUDA(cudaMemcpyAsync(y_[k], P_.crY0 + oy, sizeof(double) * sz, cudaMemcpyHostToDevice, s_));
+      oy += sz;
+    }
+  }
+  fill_f64(phi_[0], 1, 1.0, s_);
+  fill_f64(phi_[d], 1, 1.0, s_);
+  auto upd_left = [&](int i) { phi_left_f64(dims(i), phi_[i], A_[i], X_[i], y_[i], phi_[i + 1], scr_, s_); };
+  auto upd_right = [&](int i) { phi_right_f64(dims(i), phi_[i + 1], A_[i], X_[i], y_[i], phi_[i], scr_, s_); };
+
+  // QR left to right, interfaces (tt_adapt_als.f90:190-223)
+  for (int i = 0; i + 1 < d; ++i) {
+    const i64 m_ = ry_[i] * n[i], rr = ry_[i + 1], p = n[i + 1] * ry_[i + 2];
+    const i64 rnew = std::min(m_, rr);
+    TTG_CUDA(cudaMemcpyAsync(Um_, y_[i], sizeof(double) * m_ * rr, cudaMemcpyDeviceToDevice, s_));
+    qr_householder((int)m_, (int)rr, Um_, Rq_, tau_, s_);
+    TTG_CUDA(cudaMemcpyAsync(y_[i], Um_, sizeof(double) * m_ * rnew, cudaMemcpyDeviceToDevice, s_));
+    gemm((int)rnew, (int)p, (int)rr, Rq_, 1, rnew, y_[i + 1], 1, rr, tmp_, 1, rnew);
+    TTG_CUDA(cudaMemcpyAsync(y_[i + 1], tmp_, sizeof(double) * rnew * p, cudaMemcpyDeviceToDevice, s_));
+    ry_[i + 1] = rnew;
+    upd_left(i);
+  }
+
+  double err_max = 0.0;
+  int i = d - 1, dir = -1, swp = 1;
+  while (swp <= P_.nswp) {
+    const LocalDims L = dims(i);
+    const i64 N = L.ysize();
+    bfun3_f64(L, phi_[i], A_[i], phi_[i + 1], X_[i], cur_, 1, scr_, s_);
+    sub_kernel<<<eb(N), 256, 0, s_>>>(N, y_[i], cur_, diff_);
+    TTG_CHECK_LAUNCH();
+    const double err = norm2(diff_, N) / norm2(cur_, N);
+    err_max = std::max(err_max, err);
+    if (P_.verb > 1)
+      fprintf(stderr, "tt_mvk4: iteration:[%d,%d] err:%.3e ry(i):%lld err_max:%.3e\n", swp, i + 1, err,
+              (long long)ry_[i], err_max);
+    if (dir > 0 && i < d - 1) {
+      // truncation to the right (:269-345)
+      const i64 m_ = ry_[i] * n[i], rr = ry_[i + 1], p = n[i + 1] * ry_[i + 2];
+      i64 rnew = std::min(rr, m_);
+      if (kick > 0) {
+        const int rmin = (int)std::min(m_, rr);
+        svd_jacobi((int)m_, (int)rr, cur_, U_, S_, Vt_, svScr_, ired_ + 16, s_);
+        const int nn = chop(rmin, eps2);
+        scale_rows_f64(rmin, rr, Vt_, rmin, S_, s_);                     // diag(s) Vt
+        TTG_CUDA(cudaMemcpyAsync(Um_, U_, sizeof(double) * m_ * nn, cudaMemcpyDeviceToDevice, s_));
+        copy_rows_f64(rmin, nn, rr, Vt_, Rm_, s_);
+        rnew = nn;
+      } else {
+        TTG_CUDA(cudaMemcpyAsync(Um_, cur_, sizeof(double) * m_ * rr, cudaMemcpyDeviceToDevice, s_));
+        qr_householder((int)m_, (int)rr, Um_, Rm_, tau_, s_);
+      }
+      TTG_REQUIRE(rnew <= cap_[i + 1], "tt_mvk4: rank capacity exceeded");
+      TTG_CUDA(cudaMemcpyAsync(y_[i], Um_, sizeof(double) * m_ * rnew, cudaMemcpyDeviceToDevice, s_));
+      gemm((int)rnew, (int)p, (int)rr, Rm_, 1, rnew, y_[i + 1], 1, rr, tmp_, 1, rnew);
+      TTG_CUDA(cudaMemcpyAsync(y_[i + 1], tmp_, sizeof(double) * rnew * p, cudaMemcpyDeviceToDevice, s_));
+      ry_[i + 1] = rnew;
+      upd_left(i);
+    }
+    if (dir < 0 && i > 0) {
+      // truncation and kick to the left (:351-434)
+      const i64 m_ = n[i] * ry_[i + 1], rl = ry_[i], p = ry_[i - 1] * n[i - 1];
+      i64 rnew = std::min(m_, rl);
+      if (kick > 0) {
+        const int rmin = (int)std::min(m_, rl);
+        svd_jacobi((int)rl, (int)m_, cur_, U_, S_, Vt_, svScr_, ired_ + 16, s_);
+        const int nn = chop(rmin, eps2);
+        scale_cols_f64(rl, rmin, U_, rl, S_, s_);                        // U diag(s)
+        // Cm = Vt[:nn, :]^T (m_ x nn), Rm = (U diag(s))[:, :nn]^T (nn x rl)
+        copy_rows_f64(rmin, nn, m_, Vt_, tmp_, s_);
+        transpose_f64(nn, m_, tmp_, Um_, s_);
+        transpose_f64(rl, nn, U_, Rm_, s_);
+        // kick: dbfun3_right (rx1 ra1) x m_, incremental Cholesky 'N'
+        bfun3_right_run(P_.rx[i], m[i], P_.rx[i + 1], n[i], ry_[i + 1], ra[i], ra[i + 1], A_[i],
+                        phi_[i + 1], X_[i], full_, tA_, tB_, s_);
+        const int mm = uchol_run(false, P_.rx[i] * ra[i], m_, full_, (int)std::min<i64>(kick, m_),
+                                 du_, UW, s_);
+        TTG_CUDA(cudaMemcpyAsync(Um_ + m_ * nn, du_, sizeof(double) * m_ * mm,
+                                 cudaMemcpyDeviceToDevice, s_));
+        pad_rows_kernel<<<eb((nn + mm) * rl), 256, 0, s_>>>(nn, mm, rl, Rm_, tmp_);
+        TTG_CHECK_LAUNCH();
+        rnew = std::min<i64>(m_, nn + mm);
+        qr_householder((int)m_, nn + mm, Um_, Rq_, tau_, s_);
+        gemm((int)rnew, (int)rl, nn + mm, Rq_, 1, rnew, tmp_, 1, nn + mm, Rm_, 1, rnew);
+      } else {
+        transpose_f64(rl, m_, cur_, Um_, s_);                            // m_ x rl
+        qr_householder((int)m_, (int)rl, Um_, Rm_, tau_, s_);
+      }
+      TTG_REQUIRE(rnew <= cap_[i], "tt_mvk4: rank capacity exceeded");
+      transpose_f64(m_, rnew, Um_, y_[i], s_);                           // rnew x m_
+      gemm((int)p, (int)rnew, (int)rl, y_[i - 1], 1, p, Rm_, rnew, 1, tmp_, 1, p);
+      TTG_CUDA(cudaMemcpyAsync(y_[i - 1], tmp_, sizeof(double) * p * rnew, cudaMemcpyDeviceToDevice, s_));
+      ry_[i] = rnew;
+      upd_right(i);
+    }
+    if (dir > 0 && i == d - 1) {
+      TTG_CUDA(cudaMemcpyAsync(y_[i], cur_, sizeof(double) * N, cudaMemcpyDeviceToDevice, s_));
+      if (P_.verb > 0)
+        fprintf(stderr, "tt_mvk4: iteration:%d(%d) max(ry):%lld err_max:%.3e\n", swp, dir,
+                (long long)*std::max_element(ry_.begin(), ry_.end()), err_max);
+      dir = -1;
+      i += 1;
+      ++swp;
+      if (err_max < P_.eps) break;
+      err_max = 0.0;
+    }
+    if (dir < 0 && i == 0) {
+      TTG_CUDA(cudaMemcpyAsync(y_[i], cur_, sizeof(double) * N, cudaMemcpyDeviceToDevice, s_));
+      dir = 1;
+      i -= 1;
+    }
+    i += dir;
+  }
+  sync();
+  i64 tot = 0;
+  for (int k = 0; k < d; ++k) tot += ry_[k] * n[k] * ry_[k + 1];
+  out.cores.resize(tot);
+  i64 off = 0;
+  for (int k = 0; k < d; ++k) {
+    const i64 sz = ry_[k] * n[k] * ry_[k + 1];
+    TTG_CUDA(cudaMemcpyAsync(out.cores.data() + off, y_[k], sizeof(double) * sz,
+                             cudaMemcpyDeviceToHost, s_));
+    off += sz;
+  }
+  sync();
+  out.rx = ry_;
+  out.sweeps = std::min(swp, P_.nswp);
+  out.res_max = err_max;
+  out.matvecs = 0;
+}
+
 }  // namespace ttg
 
 using namespace ttg;
@@ -1507,6 +1817,48 @@ extern "C" int ttg_amen_solve(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const t
     ctx->result_core = std::move(out.cores);
     ctx->zresult_core.clear();
     ctx->stat_matvecs = out.matvecs;
+    ctx->stat_sweeps = out.sweeps;
+    ctx->stat_res = out.res_max;
+    ctx->stat_launches = g_launches - l0;
+  } catch (const ttg::Error& e) {
+    ctx->last_error = e.msg;
+    return e.code;
+  }
+  return TTG_OK;
+}
+
+// tt_mvk4 (tt_adapt_als.f90:67-500)
+extern "C" int ttg_mvk4(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
+                        const ttg_int* rx, const ttg_int* ra, const double* crA, const double* crX,
+                        const double* crY0, ttg_int* ry, double eps, ttg_int rmax, ttg_int kickrank,
+                        ttg_int nswp, int verb) {
+  if (!ctx) return TTG_ERR_ARG;
+  try {
+    TTG_CUDA(cudaSetDevice(ctx->device));
+    TTG_REQUIRE(d > 1 && n && m && rx && ra && crA && crX && crY0 && ry, "null argument");
+    TTG_REQUIRE(rmax > 0, "tt_mvk4: rmax must be positive");
+    TTG_REQUIRE(kickrank <= 16, "tt_mvk4: kickrank > 16");
+    MvkParams P;
+    P.d = (int)d;
+    P.n.assign(n, n + d);
+    P.m.assign(m, m + d);
+    P.rx.assign(rx, rx + d + 1);
+    P.ra.assign(ra, ra + d + 1);
+    P.ry.assign(ry, ry + d + 1);
+    P.crA = crA; P.crX = crX; P.crY0 = crY0;
+    P.eps = eps;
+    P.rmax = rmax;
+    P.kick = (int)kickrank;
+    P.nswp = nswp > 0 ? (int)nswp : 20;
+    P.verb = verb;
+    long long l0 = g_launches;
+    AmenOut out;
+    MvkSolver solver(ctx, P);
+    solver.run(out);
+    for (int k = 0; k <= d; ++k) ry[k] = out.rx[k];
+    ctx->result_core = std::move(out.cores);
+    ctx->zresult_core.clear();
+    ctx->stat_matvecs = 0;
     ctx->stat_sweeps = out.sweeps;
     ctx->stat_res = out.res_max;
     ctx->stat_launches = g_launches - l0;

@@ -75,7 +75,7 @@ EXPORTED = [
     "ttg_mlp_adam_step", "ttg_set_learned", "ttg_record_count", "ttg_record_clear",
     "ttg_mlp_train_recorded", "ttg_batch_create", "ttg_batch_destroy", "ttg_batch_add_eigb",
     "ttg_batch_run", "ttg_batch_result", "ttg_batch_cores", "ttg_djac_size", "ttg_djac_gen",
-    "ttg_djac_apply",
+    "ttg_djac_apply", "ttg_mvk4",
 ]
 
 
@@ -200,6 +200,20 @@ def ztt_ksl(d, n, m, ra, crA, crY0, ry, tau, rmax, kickrank=None, nswp=None, ver
                          C.c_int(order), C.c_int(METHOD[method]), _i64(nsteps))
     ctx.check(rc)
     return _result(ctx, real=False), [int(v) for v in ry_]
+
+
+def tt_mvk4(d, n, m, rx, ra, crA, crX, crY0, ry, eps, rmax, kickrank=5, nswp=20, verb=0,
+            ctx=None):
+    """AMEn matvec y ~ A x (tt_mvk4, tt_adapt_als.f90:67).  Returns (cores, ry)."""
+    ctx = ctx or default_context()
+    n_, m_, rx_, ra_ = _iarr(n), _iarr(m), _iarr(rx), _iarr(ra)
+    ry_ = _iarr(ry).copy()
+    A_, X_, Y_ = _darr(crA), _darr(crX), _darr(crY0)
+    rc = lib().ttg_mvk4(ctx.handle, _i64(d), _p(n_), _p(m_), _p(rx_), _p(ra_), _p(A_), _p(X_),
+                        _p(Y_), _p(ry_), C.c_double(eps), _i64(rmax), _i64(kickrank), _i64(nswp),
+                        C.c_int(verb))
+    ctx.check(rc)
+    return _result(ctx, real=True), [int(v) for v in ry_]
 
 
 def tt_amen_solve(d, n, m, ry, ra, crA, crY, crX0, rx, eps, kickrank=4, nswp=20, verb=0,
