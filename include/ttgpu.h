@@ -155,6 +155,21 @@ int ttg_djac_gen(ttg_ctx* ctx, char ptype, ttg_int rx1, ttg_int n, ttg_int rx2, 
 int ttg_djac_apply(ttg_ctx* ctx, char ptype, ttg_int rx1, ttg_int n, ttg_int rx2,
                    const double* jacs, const double* x, double* y);
 
+/* ------------------------------------------------ TT files (host) */
+/* The reference's binary TT format (.sdv): dtt_write / ztt_write and
+ * dtt_read / ztt_read, ttio.f90:29-399.  Host arrays; cores back to back,
+ * core k of r[k] x n[k] x r[k+1] column-major, float64, or complex128 stored
+ * as interleaved pairs when is_complex (the file does not record which).
+ * Modes are written as l = 1 .. m = d; d <= 1023 (tt_size).  The reader
+ * checks the 'TT' magic and version 1, sets d and nelem (scalars of the
+ * cores), and fills n (d), r (d + 1) and cores when they are not NULL
+ * (nmax = capacity of n; cores must hold nelem scalars).  Both return
+ * TTG_ERR_ARG on I/O or format errors; they need no context or GPU. */
+int ttg_sdv_write(const char* path, ttg_int d, const ttg_int* n, const ttg_int* r,
+                  const double* cores, int is_complex);
+int ttg_sdv_read(const char* path, int is_complex, ttg_int* d, ttg_int* n, ttg_int* r,
+                 ttg_int nmax, double* cores, ttg_int* nelem);
+
 /* ------------------------------------------------ dense algebra (device) */
 /* A (n x m) -> Q (n x min(n,m)) in place, R (min(n,m) x m): dqr
  * matrix_util.f90:37-61 (bind(c) twin tt_linalg.f90:30); zqr :64-90. */

@@ -7,6 +7,7 @@ It reads the reference fixtures (``Heisen_20.sdv``, ``test_ksl.dat``,
 here, plus the exact-diagonalisation spectrum of the Heisenberg chain stored
 in ``Heisen_20.sdv`` (sparse Lanczos on the 2^20 space, tol 1e-13).
 """
+import hashlib
 import json
 import os
 import sys
@@ -41,10 +42,21 @@ def heisenberg_ed(d, k=8):
     return np.sort(w).tolist()
 
 
+def sdv_layout(ref):
+    """The byte layout of the reference's Heisen_20.sdv: its first 16 header
+    bytes ('TT' magic and version) and a hash of everything after the
+    128-byte header (l, m, n, r and the cores)."""
+    raw = open(os.path.join(ref, "Heisen_20.sdv"), "rb").read()
+    with open(os.path.join(HERE, "heisen20_sdv_layout.json"), "w") as f:
+        json.dump({"source": "Heisen_20.sdv", "size": len(raw), "head16_hex": raw[:16].hex(),
+                   "body_sha256": hashlib.sha256(raw[128:]).hexdigest()}, f, indent=1)
+
+
 def main(ref):
     n, r, cores = read_sdv(os.path.join(ref, "Heisen_20.sdv"))
     np.savez_compressed(os.path.join(HERE, "heisen20_sdv.npz"), n=np.array(n), r=np.array(r),
                         cores=cores)
+    sdv_layout(ref)
     for name in ("test_ksl.dat", "test_eye_ksl.dat"):
         D = read_ksl_dat(os.path.join(ref, name))
         np.savez_compressed(os.path.join(HERE, name.replace(".dat", "_dat.npz")),

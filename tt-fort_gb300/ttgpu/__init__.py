@@ -75,7 +75,7 @@ EXPORTED = [
     "ttg_mlp_adam_step", "ttg_set_learned", "ttg_record_count", "ttg_record_clear",
     "ttg_mlp_train_recorded", "ttg_batch_create", "ttg_batch_destroy", "ttg_batch_add_eigb",
     "ttg_batch_run", "ttg_batch_result", "ttg_batch_cores", "ttg_djac_size", "ttg_djac_gen",
-    "ttg_djac_apply", "ttg_mvk4",
+    "ttg_djac_apply", "ttg_mvk4", "ttg_sdv_write", "ttg_sdv_read",
 ]
 
 
@@ -200,6 +200,35 @@ def ztt_ksl(d, n, m, ra, crA, crY0, ry, tau, rmax, kickrank=None, nswp=None, ver
                          C.c_int(order), C.c_int(METHOD[method]), _i64(nsteps))
     ctx.check(rc)
     return _result(ctx, real=False), [int(v) for v in ry_]
+
+
+def sdv_write(path, n, r, cores, complex_=False):
+    """Write a TT tensor in the reference's .sdv format (dtt_write / ztt_write,
+    ttio.f90:29-192); cores flat, column-major, float64 or complex128."""
+    n_, r_ = _iarr(n), _iarr(r)
+    c = np.ascontiguousarray(cores, dtype=np.complex128 if complex_ else np.float64)
+    rc = lib().ttg_sdv_write(str(path).encode(), _i64(len(n_)), _p(n_), _p(r_),
+                             c.ctypes.data_as(C.c_void_p), C.c_int(1 if complex_ else 0))
+    if rc != 0:
+        raise RuntimeError(f"ttg_sdv_write failed ({rc}): {path}")
+
+
+def sdv_read(path, complex_=False):
+    """Read a .sdv file (dtt_read / ztt_read, ttio.f90:196-399): (n, r, cores)."""
+    d = C.c_int64(0)
+    ne = C.c_int64(0)
+    rc = lib().ttg_sdv_read(str(path).encode(), C.c_int(int(complex_)), C.byref(d), None, None,
+                            _i64(0), None, C.byref(ne))
+    if rc != 0:
+        raise RuntimeError(f"ttg_sdv_read failed ({rc}): {path}")
+    n_ = np.zeros(d.value, dtype=np.int64)
+    r_ = np.zeros(d.value + 1, dtype=np.int64)
+    cores = np.zeros(ne.value, dtype=np.complex128 if complex_ else np.float64)
+    rc = lib().ttg_sdv_read(str(path).encode(), C.c_int(int(complex_)), C.byref(d), _p(n_), _p(r_),
+                            _i64(d.value), cores.ctypes.data_as(C.c_void_p), C.byref(ne))
+    if rc != 0:
+        raise RuntimeError(f"ttg_sdv_read failed ({rc}): {path}")
+    return [int(v) for v in n_], [int(v) for v in r_], cores
 
 
 def tt_mvk4(d, n, m, rx, ra, crA, crX, crY0, ry, eps, rmax, kickrank=5, nswp=20, verb=0,
