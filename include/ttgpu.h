@@ -239,6 +239,20 @@ int ttg_eigb(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m, const 
 int ttg_ksl_z(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m, const ttg_int* ra,
               const double* crA, const double* crY0, ttg_int* ry, double tau, ttg_int rmax,
               int verb, int typ, int order, int method, ttg_int nsteps);
+/* KSL for an operator diagonal in the physical index, ztt_diag_ksl
+ * tt_diag_ksl.f90:560-804 (complex, interleaved) and dtt_diag_ksl :315-558
+ * (real): crA holds the cores A(a1, i, a2) (ra[k] x n[k] x ra[k+1]); each
+ * K-step runs one Krylov exponential per slice i of the core, every
+ * exponential with anorm = 1, as the reference does.  Other arguments and
+ * results as ttg_ksl_z (real results through ttg_result_copy, complex through
+ * ttg_zresult_copy); FP64 only.  The real entry runs the same scheme in
+ * complex arithmetic on real data. */
+int ttg_diag_ksl_z(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* ra,
+                   const double* crA, const double* crY0, ttg_int* ry, double tau, ttg_int rmax,
+                   int verb, int typ, int order, ttg_int nsteps);
+int ttg_diag_ksl_d(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* ra,
+                   const double* crA, const double* crY0, ttg_int* ry, double tau, ttg_int rmax,
+                   int verb, int typ, int order, ttg_int nsteps);
 /* AMEn matvec y ~ A x, tt_mvk4 tt_adapt_als.f90:67-500 (argument order
  * follows it; crY0 with ranks ry is the start, ry updated in place).
  * kickrank 5 and nswp 20 are the reference's defaults (nswp <= 0: 20); the

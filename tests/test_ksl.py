@@ -96,3 +96,37 @@ def test_unit_randoms_stream():
     z = unit_randoms(0, 5)
     assert np.allclose(np.abs(z), 1.0)
     assert np.allclose(unit_randoms(2, 3), z[2:5])
+
+
+def diag_sum_operator(d, nn, seed, complex_=True):
+    """A = sum_k I x .. x diag(a_k) x .. x I as diagonal cores A(a1, i, a2)
+    of rank 2, and a rank-1 start: ztt_diag_ksl is exact on it."""
+    rng = np.random.default_rng(seed)
+    a = [rng.standard_normal(nn) + (1j * rng.standard_normal(nn) if complex_ else 0)
+         for _ in range(d)]
+    ra = [1] + [2] * (d - 1) + [1]
+    cores = []
+    for k in range(d):
+        c = np.zeros((ra[k], nn, ra[k + 1]), complex if complex_ else float)
+        if k == 0:
+            c[0, :, 0] = a[k]; c[0, :, 1] = 1
+        elif k == d - 1:
+            c[0, :, 0] = 1; c[1, :, 0] = a[k]
+        else:
+            c[0, :, 0] = 1; c[1, :, 0] = a[k]; c[1, :, 1] = 1
+        cores.append(c.ravel(order="F"))
+    y0 = [rng.standard_normal(nn) + (1j * rng.standard_normal(nn) if complex_ else 0)
+          for _ in range(d)]
+    return ra, np.concatenate(cores), a, y0
+
+
+def test_diag_ksl_oracle_is_exact_on_separable_diagonal_operators():
+    from oracle.ksl import ztt_diag_ksl
+    d, nn, tau = 5, 4, 0.1
+    ra, crA, a, y0 = diag_sum_operator(d, nn, 0)
+    out = ztt_diag_ksl(d, [nn] * d, ra, crA, np.concatenate(y0), [1] * (d + 1), tau, 10)
+    ex = y0[0] * np.exp(tau * a[0])
+    for k in range(1, d):
+        ex = np.kron(y0[k] * np.exp(tau * a[k]), ex)
+    x1 = tt_full(d, [nn] * d, out["ry"], out["cores"])
+    assert np.linalg.norm(x1 - ex) <= 1e-12 * np.linalg.norm(ex)

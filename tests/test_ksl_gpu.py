@@ -88,3 +88,46 @@ def test_ksl_split_eye_fixture(ctx):
     cores, ry1 = ttgpu.ztt_ksl(d, n, m, ra, crA, crY, ry, tau, 150, method="split", ctx=ctx)
     x0 = tt_full(d, n, ry, crY)
     assert _rel(tt_full(d, n, ry1, cores), np.exp(1j * tau) * x0) < 1e-6
+
+
+def _diag_random(d, n, ra_r, ry_r, seed, complex_):
+    rng = np.random.default_rng(seed)
+    ra = [1] + [ra_r] * (d - 1) + [1]
+    ry = [1] + [ry_r] * (d - 1) + [1]
+    def draw(sz):
+        v = rng.standard_normal(sz)
+        return v + 1j * rng.standard_normal(sz) if complex_ else v
+    crA = np.concatenate([0.5 * draw(ra[k] * n * ra[k + 1]) for k in range(d)])
+    y = np.concatenate([draw(ry[k] * n * ry[k + 1]) for k in range(d)])
+    return ra, ry, crA, y
+
+
+@pytest.mark.parametrize("complex_", [True, False])
+def test_diag_ksl_matches_oracle(ctx, complex_):
+    """ztt_diag_ksl / dtt_diag_ksl (tt_diag_ksl.f90:315,560) against the
+    oracle over 3 steps: per-slice Krylov exponentials, anorm = 1."""
+    import ttgpu
+    from oracle.ksl import ztt_diag_ksl
+    d, n, tau = 4, 3, 0.05
+    ra, ry, crA, y = _diag_random(d, n, 2, 3, 11, complex_)
+    cores, ry1 = ttgpu.tt_diag_ksl(d, [n] * d, ra, crA, y, ry, tau, 10, nsteps=3, ctx=ctx)
+    assert np.iscomplexobj(cores) == complex_
+    c, r = y, list(ry)
+    for _ in range(3):
+        out = ztt_diag_ksl(d, [n] * d, ra, crA, c, r, tau, 10)
+        c, r = out["cores"], out["ry"]
+    assert ry1 == r
+    assert _rel(tt_full(d, [n] * d, ry1, cores), tt_full(d, [n] * d, r, c)) < 1e-8
+
+
+def test_diag_ksl_exact_on_separable(ctx):
+    import ttgpu
+    from test_ksl import diag_sum_operator
+    d, nn, tau = 5, 4, 0.1
+    ra, crA, a, y0 = diag_sum_operator(d, nn, 0)
+    cores, ry1 = ttgpu.tt_diag_ksl(d, [nn] * d, ra, crA, np.concatenate(y0), [1] * (d + 1), tau,
+                                   10, ctx=ctx)
+    ex = y0[0] * np.exp(tau * a[0])
+    for k in range(1, d):
+        ex = np.kron(y0[k] * np.exp(tau * a[k]), ex)
+    assert _rel(tt_full(d, [nn] * d, ry1, cores), ex) < 1e-12

@@ -73,7 +73,37 @@ struct KslParams {
   double tau;
   int typ, order, nsteps, verb;
   int method = TTG_METHOD_PLAIN;
+  // diag: the operator is diagonal in the physical index (cores A(a1, i, a2),
+  // crA holds those); ztt_diag_ksl, tt_diag_ksl.f90:560-804
+  bool diag = false;
 };
+
+// A(a1, i, j, a2) = delta_ij D(a1, i, a2): the diagonal TT-matrix core as a
+// full one, so the interfaces are zphi_left/right of it (equal to the slice
+// sums zphi_diag_left/right, tt_diag_ksl.f90:269-301)
+__global__ void expand_diag_kernel(i64 ra1, i64 n, i64 ra2, const double2* __restrict__ D,
+                                   double2* __restrict__ A) {
+  const i64 tot = ra1 * n * n * ra2;
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x) {
+    i64 t = e;
+    const i64 a1 = t % ra1; t /= ra1;
+    const i64 i = t % n; t /= n;
+    const i64 j = t % n; const i64 a2 = t / n;
+    A[e] = i == j ? D[a1 + ra1 * (i + n * a2)] : make_double2(0.0, 0.0);
+  }
+}
+// out[a + r1 b] = in[a + r1 (k + n b)]  (zextract_slice, tt_diag_ksl.f90:236-243)
+__global__ void slice_get_kernel(i64 r1, i64 n, i64 r2, i64 k, const double2* __restrict__ in,
+                                 double2* __restrict__ out) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < r1 * r2; e += (i64)gridDim.x * blockDim.x)
+    out[e] = in[e % r1 + r1 * (k + n * (e / r1))];
+}
+// out[a + r1 (k + n b)] = in[a + r1 b]  (zset_slice, tt_diag_ksl.f90:246-253)
+__global__ void slice_set_kernel(i64 r1, i64 n, i64 r2, i64 k, const double2* __restrict__ in,
+                                 double2* __restrict__ out) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < r1 * r2; e += (i64)gridDim.x * blockDim.x)
+    out[e % r1 + r1 * (k + n * (e / r1))] = in[e];
+}
 
 // Chosen form of the K-step product: the complex local operator
 // y = Phi1 A Phi2 x (zbfun3) as ONE real BF16x3 tensor-core operator with
@@ -217,6 +247,12 @@ static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>
                   alz(split_bytes)) +
              2 * alz(sizeof(double) * 2 * capmax * kNvecSplit);
   }
+  i64 pdiag = 0;
+  if (P.diag) {
+    for (int i = 0; i < d; ++i) pdiag += P.ra[i] * n[i] * P.ra[i + 1];
+    total += alz(sizeof(double2) * pdiag) + 2 * alz(sizeof(double2) * rmx * rmx) +
+             alz(sizeof(double2) * ramax * ramax);
+  }
   DevBlockZ mem;
   mem.alloc(total);
   double2* dA = mem.take<double2>(pa[d]);
@@ -246,13 +282,31 @@ static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>
     rx = mem.take<double>(2 * capmax * kNvecSplit);
     ryv = mem.take<double>(2 * capmax * kNvecSplit);
   }
+  double2 *dD = nullptr, *slc = nullptr, *slc2 = nullptr, *Ak = nullptr;
+  if (P.diag) {
+    dD = mem.take<double2>(pdiag);
+    slc = mem.take<double2>(rmx * rmx);
+    slc2 = mem.take<double2>(rmx * rmx);
+    Ak = mem.take<double2>(ramax * ramax);
+  }
   double* pinned = nullptr;
   TTG_CUDA(cudaMallocHost(&pinned, 4096 * sizeof(double)));
   struct PinGuard { double* p; ~PinGuard() { if (p) cudaFreeHost(p); } } pg{pinned};
   ExpWork w;
   w.bind(expmem, Nmax, P.order, pinned);
 
-  TTG_CUDA(cudaMemcpyAsync(dA, P.crA, sizeof(double2) * pa[d], cudaMemcpyHostToDevice, s));
+  if (P.diag) {
+    TTG_CUDA(cudaMemcpyAsync(dD, P.crA, sizeof(double2) * pdiag, cudaMemcpyHostToDevice, s));
+    i64 od = 0;
+    for (int i = 0; i < d; ++i) {
+      expand_diag_kernel<<<ebz(P.ra[i] * n[i] * n[i] * P.ra[i + 1]), 256, 0, s>>>(
+          P.ra[i], n[i], P.ra[i + 1], dD + od, dA + pa[i]);
+      TTG_CHECK_LAUNCH();
+      od += P.ra[i] * n[i] * P.ra[i + 1];
+    }
+  } else {
+    TTG_CUDA(cudaMemcpyAsync(dA, P.crA, sizeof(double2) * pa[d], cudaMemcpyHostToDevice, s));
+  }
   {
     i64 off = 0;
     for (int i = 0; i < d; ++i) {
@@ -288,7 +342,30 @@ static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>
       phi_left_z(Ld(i), phi[i], A_of(i), cr[i], cr[i], phi[i + 1], scratch, s);
     }
     unsigned long long counter = 0;   // init_seed() at every call, tt_ksl.f90:556
+    auto kstep_diag = [&](int i) {
+      // one Krylov exponential per slice k, local operator bfun3 with
+      // m = n = 1 and A(:, k, :), anorm = 1 (tt_diag_ksl.f90:688-697,727-733)
+      const i64 r1 = ry[i], r2 = ry[i + 1], nk = n[i], N = r1 * r2;
+      const LocalDims Lk{r1, 1, r2, r1, 1, r2, P.ra[i], P.ra[i + 1]};
+      const double2 *p1 = phi[i], *p2 = phi[i + 1];
+      i64 od = 0;
+      for (int q = 0; q < i; ++q) od += P.ra[q] * n[q] * P.ra[q + 1];
+      for (i64 k = 0; k < nk; ++k) {
+        slice_get_kernel<<<ebz(P.ra[i] * P.ra[i + 1]), 256, 0, s>>>(P.ra[i], nk, P.ra[i + 1], k,
+                                                                   dD + od, Ak);
+        slice_get_kernel<<<ebz(N), 256, 0, s>>>(r1, nk, r2, k, cr[i], slc);
+        TTG_CHECK_LAUNCH();
+        const double2* Akc = Ak;
+        ZMatvecFn mv = [=](const double2* X, double2* Y, int t) {
+          bfun3_z(Lk, p1, Akc, p2, X, Y, t, scratch, s);
+        };
+        zexp_mv_dev(w, N, (int)std::min<i64>(P.order, N), tau0, slc, slc2, eps, 1.0, mv, s, &est);
+        slice_set_kernel<<<ebz(N), 256, 0, s>>>(r1, nk, r2, k, slc2, curcr);
+        TTG_CHECK_LAUNCH();
+      }
+    };
     auto kstep = [&](int i) {
+      if (P.diag) return kstep_diag(i);
       const LocalDims L = Ld(i);
       const i64 N = L.xsize();
       const double2 *p1 = phi[i], *p2 = phi[i + 1], *Ai = A_of(i);
@@ -332,7 +409,7 @@ static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>
       ZMatvecFn mv = [=](const double2* X, double2* Y, int t) {
         sfun_apply(rx1, rx2, ra, ry1, ry2, ph1, ph2, X, Y, t, scratch, s);
       };
-      const double anorm = znormest_dev(w, N, 4, mv, nullptr, counter, s, &est);
+      const double anorm = P.diag ? 1.0 : znormest_dev(w, N, 4, mv, nullptr, counter, s, &est);
       zexp_mv_dev(w, N, P.order, -tau0, Rin, Sout, eps, anorm, mv, s, &est);
     };
     int i = d - 1, dir = -1, swp = 0;
@@ -467,4 +544,83 @@ extern "C" int ttg_ksl_z(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_in
     return e.code;
   }
   return TTG_OK;
+}
+
+// ztt_diag_ksl / dtt_diag_ksl (tt_diag_ksl.f90:315-804): KSL for operators
+// diagonal in the physical index.  The real version runs the same scheme in
+// complex arithmetic on real data (the imaginary parts stay zero) and returns
+// the real parts.
+static int diag_ksl_entry(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* ra,
+                          const double2* crA, const double2* crY0, ttg_int* ry, double tau,
+                          int verb, int typ, int order, ttg_int nsteps, bool real_out) {
+  TTG_CUDA(cudaSetDevice(ctx->device));
+  TTG_REQUIRE(typ == 1 || typ == 2, "typ must be 1 (KSL) or 2 (symmetric KSL)");
+  KslParams P;
+  P.d = (int)d;
+  P.n.assign(n, n + d);
+  P.m.assign(n, n + d);
+  P.ra.assign(ra, ra + d + 1);
+  P.ry.assign(ry, ry + d + 1);
+  P.crA = crA;
+  P.crY0 = crY0;
+  P.tau = tau;
+  P.typ = typ;
+  P.order = order > 0 ? order : 8;
+  P.nsteps = nsteps > 0 ? (int)nsteps : 1;
+  P.verb = verb;
+  P.diag = true;
+  long long l0 = g_launches;
+  ExpStats est;
+  std::vector<i64> ry_out;
+  run_ksl(ctx, P, ctx->zresult_core, ry_out, est);
+  for (int k = 0; k <= d; ++k) ry[k] = ry_out[k];
+  ctx->result_core.clear();
+  if (real_out) {
+    ctx->result_core.resize(ctx->zresult_core.size());
+    for (size_t e = 0; e < ctx->zresult_core.size(); ++e) ctx->result_core[e] = ctx->zresult_core[e].real();
+    ctx->zresult_core.clear();
+  }
+  ctx->stat_matvecs = est.nmult;
+  ctx->stat_sweeps = P.nsteps;
+  ctx->stat_res = 0.0;
+  ctx->stat_launches = g_launches - l0;
+  return TTG_OK;
+}
+
+extern "C" int ttg_diag_ksl_z(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* ra,
+                              const double* crA, const double* crY0, ttg_int* ry, double tau,
+                              ttg_int rmax, int verb, int typ, int order, ttg_int nsteps) {
+  if (!ctx) return TTG_ERR_ARG;
+  try {
+    TTG_REQUIRE(d > 0 && n && ra && crA && crY0 && ry, "null argument");
+    (void)rmax;   // read but unused by the reference as well (tt_diag_ksl.f90:600)
+    return diag_ksl_entry(ctx, d, n, ra, (const double2*)crA, (const double2*)crY0, ry, tau, verb,
+                          typ, order, nsteps, false);
+  } catch (const ttg::Error& e) {
+    ctx->last_error = e.msg;
+    return e.code;
+  }
+}
+
+extern "C" int ttg_diag_ksl_d(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* ra,
+                              const double* crA, const double* crY0, ttg_int* ry, double tau,
+                              ttg_int rmax, int verb, int typ, int order, ttg_int nsteps) {
+  if (!ctx) return TTG_ERR_ARG;
+  try {
+    TTG_REQUIRE(d > 0 && n && ra && crA && crY0 && ry, "null argument");
+    (void)rmax;
+    i64 na = 0, ny = 0;
+    for (ttg_int k = 0; k < d; ++k) {
+      na += ra[k] * n[k] * ra[k + 1];
+      ny += ry[k] * n[k] * ry[k + 1];
+    }
+    std::vector<double2> zA(na), zY(ny);
+    for (i64 e = 0; e < na; ++e) zA[e] = make_double2(crA[e], 0.0);
+    for (i64 e = 0; e < ny; ++e) zY[e] = make_double2(crY0[e], 0.0);
+    return diag_ksl_entry(ctx, d, n, ra, zA.data(), zY.data(), ry, tau, verb, typ, order, nsteps,
+                          true);
+  } catch (const ttg::Error& e) {
+    ctx->last_error = e.msg;
+    return e.code;
+  }
 }

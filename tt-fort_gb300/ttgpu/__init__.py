@@ -75,7 +75,8 @@ EXPORTED = [
     "ttg_mlp_adam_step", "ttg_set_learned", "ttg_record_count", "ttg_record_clear",
     "ttg_mlp_train_recorded", "ttg_batch_create", "ttg_batch_destroy", "ttg_batch_add_eigb",
     "ttg_batch_run", "ttg_batch_result", "ttg_batch_cores", "ttg_djac_size", "ttg_djac_gen",
-    "ttg_djac_apply", "ttg_mvk4", "ttg_sdv_write", "ttg_sdv_read",
+    "ttg_djac_apply", "ttg_mvk4", "ttg_sdv_write", "ttg_sdv_read", "ttg_diag_ksl_z",
+    "ttg_diag_ksl_d",
 ]
 
 
@@ -243,6 +244,23 @@ def tt_mvk4(d, n, m, rx, ra, crA, crX, crY0, ry, eps, rmax, kickrank=5, nswp=20,
                         C.c_int(verb))
     ctx.check(rc)
     return _result(ctx, real=True), [int(v) for v in ry_]
+
+
+def tt_diag_ksl(d, n, ra, crA, crY0, ry, tau, rmax, verb=0, typ=2, order=8, nsteps=1,
+                ctx=None):
+    """KSL for an operator diagonal in the physical index (ztt_diag_ksl /
+    dtt_diag_ksl, tt_diag_ksl.f90:315,560): crA holds cores A(a1, i, a2).
+    Complex inputs run ztt_diag_ksl, real ones dtt_diag_ksl.  Returns (cores, ry)."""
+    ctx = ctx or default_context()
+    cplx = np.iscomplexobj(crA) or np.iscomplexobj(crY0)
+    n_, ra_ = _iarr(n), _iarr(ra)
+    ry_ = _iarr(ry).copy()
+    A_, Y_ = (_carr(crA), _carr(crY0)) if cplx else (_darr(crA), _darr(crY0))
+    f = lib().ttg_diag_ksl_z if cplx else lib().ttg_diag_ksl_d
+    rc = f(ctx.handle, _i64(d), _p(n_), _p(ra_), _p(A_), _p(Y_), _p(ry_), C.c_double(tau),
+           _i64(rmax), C.c_int(verb), C.c_int(typ), C.c_int(order), _i64(nsteps))
+    ctx.check(rc)
+    return _result(ctx, real=not cplx), [int(v) for v in ry_]
 
 
 def tt_amen_solve(d, n, m, ry, ra, crA, crY, crX0, rx, eps, kickrank=4, nswp=20, verb=0,
