@@ -575,18 +575,244 @@ __global__ void svd_gather_kernel(int p, int q, const double* M, const double* V
     sigma[rank[j]] = nrm[j];
 }
 
+// ---------------------------------------------------------------------------
+// QR-preconditioned one-sided Jacobi (Drmac and Veselic, "New fast and
+// accurate Jacobi SVD algorithm", SIAM J. Matrix Anal. Appl. 29, 2008).
+// Plain one-sided Jacobi on the truncation blocks of the sweeps, whose
+// singular values fall over fifteen decades, needs 25-35 sweeps; on the
+// transposed triangular factor of a QR of the column-sorted matrix it needs
+// 6-8.  So for M (p x q, p >= q):
+//   M P = Q R   (columns sorted by decreasing norm, blocked Householder QR:
+//                one-CTA panels of QRP_NB columns, trailing update by FP64
+//                GEMMs over the whole GPU with the compact WY form)
+//   R^T = Ux S J^T   (one-sided Jacobi on the q x q matrix R^T)
+//   M = (Q J) S (P Ux)^T.
+// ---------------------------------------------------------------------------
+constexpr int QRP_NB = 32;
+constexpr int QRP_NT = 1024;
+
+// Householder QR of one panel in place: rows 0..m-1 from the panel's
+// diagonal down, columns 0..w-1 (leading dimension lda).  R goes above the
+// diagonal, the reflector vectors below it (unit diagonal implied), tau[c];
+// T (w x w, leading dimension ldt) is the triangular factor of the block
+// reflector H_0 H_1 ... H_{w-1} = I - Y T Y^T (forward, columnwise).
+__global__ void __launch_bounds__(QRP_NT) qr_panel_kernel(int m, int w, double* A, i64 lda,
+                                                          double* tau, double* T, int ldt) {
+  __shared__ double red[33];
+  __shared__ double s_beta, s_tau, s_scale;
+  __shared__ double zt[QRP_NB];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nwarp = QRP_NT / 32;
+  for (int c = 0; c < w; ++c) {
+    double* col = A + lda * c;
+    double t = 0.0;
+    for (int i = c + 1 + tid; i < m; i += QRP_NT) t = fma(col[i], col[i], t);
+    const double xn2 = block_sum<QRP_NT>(t, red);
+    if (tid == 0) {
+      const double alpha = col[c];
+      if (xn2 == 0.0) {
+        s_tau = 0.0; s_beta = alpha; s_scale = 0.0;
+      } else {
+        const double beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+        s_tau = (beta - alpha) / beta;
+        s_beta = beta;
+        s_scale = 1.0 / (alpha - beta);
+      }
+      tau[c] = s_tau;
+    }
+    __syncthreads();
+    const double tc = s_tau, sc = s_scale;
+    if (tc != 0.0)
+      for (int i = c + 1 + tid; i < m; i += QRP_NT) col[i] *= sc;
+    __syncthreads();
+    if (tid == 0) col[c] = s_beta;
+    __syncthreads();
+    // H_c = I - tau v v^T on columns c+1..w-1, one warp per column
+    if (tc != 0.0) {
+      for (int cc = c + 1 + wid; cc < w; cc += nwarp) {
+        double* a = A + lda * cc;
+        double d = lane == 0 ? a[c] : 0.0;
+        for (int i = c + 1 + lane; i < m; i += 32) d = fma(col[i], a[i], d);
+        d = warp_sum(d) * tc;
+        if (lane == 0) a[c] -= d;
+        for (int i = c + 1 + lane; i < m; i += 32) a[i] = fma(-d, col[i], a[i]);
+      }
+    }
+    __syncthreads();
+  }
+  // T: T[i, i] = tau_i, T[0:i, i] = -tau_i T[0:i, 0:i] (Y[:, 0:i]^T y_i)
+  for (int e = tid; e < ldt * w; e += QRP_NT) T[e] = 0.0;
+  __syncthreads();
+  for (int i = 0; i < w; ++i) {
+    for (int j = wid; j < i; j += nwarp) {
+      const double* yj = A + lda * j;
+      const double* yi = A + lda * i;
+      double z = lane == 0 ? yj[i] : 0.0;          // y_i(i) = 1
+      for (int r = i + 1 + lane; r < m; r += 32) z = fma(yj[r], yi[r], z);
+      z = warp_sum(z);
+      if (lane == 0) zt[j] = -tau[i] * z;
+    }
+    __syncthreads();
+    if (tid < i) {
+      double v = 0.0;
+      for (int k = tid; k < i; ++k) v = fma(T[tid + (i64)ldt * k], zt[k], v);
+      T[tid + (i64)ldt * i] = v;
+    }
+    if (tid == 0) T[i + (i64)ldt * i] = tau[i];
+    __syncthreads();
+  }
+}
+
+// Y (m x w) with the unit diagonal and zeros above it, from a factored panel
+__global__ void qr_make_y_kernel(int m, int w, const double* __restrict__ A, i64 lda,
+                                 double* __restrict__ Y) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)m * w; e += (i64)gridDim.x * blockDim.x) {
+    const int r = (int)(e % m), c = (int)(e / m);
+    Y[e] = r > c ? A[r + lda * c] : (r == c ? 1.0 : 0.0);
+  }
+}
+// A[:, rank[j]] = M[:, j]
+__global__ void permute_cols_kernel(int p, int q, const double* __restrict__ M,
+                                    const int* __restrict__ rank, double* __restrict__ A) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)p * q; e += (i64)gridDim.x * blockDim.x) {
+    const int i = (int)(e % p), j = (int)(e / p);
+    A[i + (i64)p * rank[j]] = M[e];
+  }
+}
+// X (q x q) = R^T, R the upper triangle of A's leading q x q block
+__global__ void rt_kernel(int q, const double* __restrict__ A, i64 lda, double* __restrict__ X) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)q * q; e += (i64)gridDim.x * blockDim.x) {
+    const int i = (int)(e % q), j = (int)(e / q);
+    X[e] = j <= i ? A[j + lda * i] : 0.0;
+  }
+}
+// C (p x q) = [Vtx^T; 0]
+__global__ void qr_c0_kernel(int p, int q, const double* __restrict__ Vtx, double* __restrict__ C) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)p * q; e += (i64)gridDim.x * blockDim.x) {
+    const int i = (int)(e % p), k = (int)(e / p);
+    C[e] = i < q ? Vtx[k + (i64)q * i] : 0.0;
+  }
+}
+// Vt[k, j] = Ux[rank[j], k]
+__global__ void qr_vt_kernel(int q, const double* __restrict__ Ux, const int* __restrict__ perm,
+                             double* __restrict__ Vt) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)q * q; e += (i64)gridDim.x * blockDim.x) {
+    const int k = (int)(e % q), j = (int)(e / q);
+    Vt[e] = Ux[perm[j] + (i64)q * k];
+  }
+}
+
+// doubles of the QR-preconditioned path's own workspace
+static size_t svd_qr_work(size_t p, size_t q) {
+  const size_t npan = (q + QRP_NB - 1) / QRP_NB;
+  return p * q + 3 * q * q + npan * QRP_NB * QRP_NB + p * QRP_NB + 2 * QRP_NB * q + 2 * q + 256;
+}
+
 size_t svd_scratch(int p, int q) {
   // working copy of M (max(p,q) x min(p,q)), V (min^2), norms, ranks, counters, Ut,
-  // and for the FP32 pre-sweeps two min^2 and one max x min temporaries
+  // for the FP32 pre-sweeps two min^2 and one max x min temporaries, and the
+  // workspace of the QR-preconditioned path
   size_t pp = std::max(p, q), qq = std::min(p, q);
   return (pp * qq + qq * qq + 2 * qq + 64) * sizeof(double) + pp * qq * sizeof(double) +
-         (2 * qq * qq + pp * qq) * sizeof(double);
+         (2 * qq * qq + pp * qq) * sizeof(double) + svd_qr_work(pp, qq) * sizeof(double);
 }
+
+static inline int gbl(i64 n) { return (int)std::max<i64>(1, std::min<i64>(4096, (n + 255) / 256)); }
 
 static void svd_tall(int p, int q, double* Mw, double* U, double* sigma, double* Vt,
                      double* V, double* nrm, int* rank, int* counters, int* status,
-                     double* tmp, cudaStream_t s) {
+                     double* tmp, cudaStream_t s, double* qrwork = nullptr);
+
+static void svd_tall_qr(int p, int q, double* Mw, double* U, double* sigma, double* Vt,
+                        double* V, double* nrm, int* rank, int* counters, int* status,
+                        double* tmp, double* work, cudaStream_t s) {
+  const int npan = ceil_div(q, QRP_NB);
+  double* A = work;                                     // p x q
+  double* X = A + (size_t)p * q;                        // q x q
+  double* Ux = X + (size_t)q * q;                       // q x q
+  double* Vtx = Ux + (size_t)q * q;                     // q x q
+  double* Tf = Vtx + (size_t)q * q;                     // NB x NB per panel
+  double* Yp = Tf + (size_t)npan * QRP_NB * QRP_NB;     // p x NB
+  double* G1 = Yp + (size_t)p * QRP_NB;                 // NB x q
+  double* G2 = G1 + (size_t)QRP_NB * q;                 // NB x q
+  double* tau = G2 + (size_t)QRP_NB * q;                // q
+  int* perm = (int*)(tau + q);                          // q ints
+  auto gemm = [&](int M, int N, int K, const double* Am, i64 sAm, i64 sAk, const double* Bm,
+                  i64 sBk, i64 sBn, double* C, i64 sCm, i64 sCn, double alpha, double beta) {
+    GemmF64 g;
+    g.M = M; g.N = N; g.K = K;
+    g.A = Am; g.sAm = sAm; g.sAk = sAk;
+    g.B = Bm; g.sBk = sBk; g.sBn = sBn;
+    g.C = C; g.sCm = sCm; g.sCn = sCn;
+    g.alpha = alpha; g.beta = beta;
+    gemm_f64(g, s);
+  };
+  // column norms, descending order (ties by index), permuted copy
+  int nb = std::max(1, std::min(1024, ceil_div((i64)q * 32, 256)));
+  svd_finish_kernel<<<nb, 256, 0, s>>>(p, q, Mw, nullptr, nullptr, nullptr, nullptr, nrm, perm);
+  TTG_CHECK_LAUNCH();
+  svd_rank_kernel<<<ceil_div(q, 256), 256, 0, s>>>(q, nrm, perm);
+  TTG_CHECK_LAUNCH();
+  permute_cols_kernel<<<gbl((i64)p * q), 256, 0, s>>>(p, q, Mw, perm, A);
+  TTG_CHECK_LAUNCH();
+  // blocked Householder QR
+  for (int k = 0; k < npan; ++k) {
+    const int j0 = k * QRP_NB, w = std::min(QRP_NB, q - j0), m = p - j0;
+    double* Ap = A + j0 + (i64)p * j0;
+    double* Tk = Tf + (size_t)k * QRP_NB * QRP_NB;
+    qr_panel_kernel<<<1, QRP_NT, 0, s>>>(m, w, Ap, p, tau + j0, Tk, QRP_NB);
+    TTG_CHECK_LAUNCH();
+    const int n2 = q - j0 - w;
+    if (n2 > 0) {
+      qr_make_y_kernel<<<gbl((i64)m * w), 256, 0, s>>>(m, w, Ap, p, Yp);
+      TTG_CHECK_LAUNCH();
+      double* A2 = Ap + (i64)p * w;
+      gemm(w, n2, m, Yp, m, 1, A2, 1, p, G1, 1, w, 1.0, 0.0);          // G1 = Y^T A2
+      gemm(w, n2, w, Tk, QRP_NB, 1, G1, 1, w, G2, 1, w, 1.0, 0.0);      // G2 = T^T G1
+      gemm(m, n2, w, Yp, 1, m, G2, 1, w, A2, 1, p, -1.0, 1.0);         // A2 -= Y G2
+    }
+  }
+  // one-sided Jacobi on R^T, FP64 sweeps over the grid from the identity
+  // (FP32 pre-sweeps do not pay here: the preconditioned matrix converges in
+  // a few FP64 sweeps, and FP32 cannot resolve its small columns)
+  (void)tmp;
+  rt_kernel<<<gbl((i64)q * q), 256, 0, s>>>(q, A, p, X);
+  TTG_CHECK_LAUNCH();
+  svd_sweeps<double>(q, q, X, V, counters, status, 0, sqrt((double)q) * DBL_EPSILON,
+                     (double)q * DBL_EPSILON, SVD_MAX_SWEEPS, s);
+  svd_finish_kernel<<<nb, 256, 0, s>>>(q, q, X, V, nullptr, nullptr, nullptr, nrm, rank);
+  TTG_CHECK_LAUNCH();
+  svd_rank_kernel<<<ceil_div(q, 256), 256, 0, s>>>(q, nrm, rank);
+  TTG_CHECK_LAUNCH();
+  svd_gather_kernel<<<gbl((i64)q * q), 256, 0, s>>>(q, q, X, V, nrm, rank, Ux, sigma, Vtx);
+  TTG_CHECK_LAUNCH();
+  // U = Q [J; 0], the panels' block reflectors applied in reverse order
+  qr_c0_kernel<<<gbl((i64)p * q), 256, 0, s>>>(p, q, Vtx, U);
+  TTG_CHECK_LAUNCH();
+  for (int k = npan - 1; k >= 0; --k) {
+    const int j0 = k * QRP_NB, w = std::min(QRP_NB, q - j0), m = p - j0;
+    const double* Ap = A + j0 + (i64)p * j0;
+    const double* Tk = Tf + (size_t)k * QRP_NB * QRP_NB;
+    qr_make_y_kernel<<<gbl((i64)m * w), 256, 0, s>>>(m, w, Ap, p, Yp);
+    TTG_CHECK_LAUNCH();
+    double* Cs = U + j0;
+    gemm(w, q, m, Yp, m, 1, Cs, 1, p, G1, 1, w, 1.0, 0.0);             // G1 = Y^T C
+    gemm(w, q, w, Tk, 1, QRP_NB, G1, 1, w, G2, 1, w, 1.0, 0.0);        // G2 = T G1
+    gemm(m, q, w, Yp, 1, m, G2, 1, w, Cs, 1, p, -1.0, 1.0);           // C -= Y G2
+  }
+  qr_vt_kernel<<<gbl((i64)q * q), 256, 0, s>>>(q, Ux, perm, Vt);
+  TTG_CHECK_LAUNCH();
+}
+
+constexpr int SVD_QR_MIN_Q = 16;   // narrower blocks keep the plain sweeps
+
+static void svd_tall(int p, int q, double* Mw, double* U, double* sigma, double* Vt,
+                     double* V, double* nrm, int* rank, int* counters, int* status,
+                     double* tmp, cudaStream_t s, double* qrwork) {
   // Mw (p x q, p >= q) is overwritten.  tmp: 2 q^2 + p q doubles.
+  if (qrwork && q >= SVD_QR_MIN_Q) {
+    svd_tall_qr(p, q, Mw, U, sigma, Vt, V, nrm, rank, counters, status, tmp, qrwork, s);
+    return;
+  }
   int init_v = 0;
   double* Y = tmp;
   double* Z = tmp + (size_t)q * q;
@@ -663,15 +889,16 @@ void svd_jacobi(int p, int q, const double* M, double* U, double* sigma, double*
   int* counters = (int*)(nrm + 2 * r);                    // 2 ints
   double* T = nrm + 2 * r + 64;                           // max x min (for p < q)
   double* tmp = T + (size_t)std::max(p, q) * r;           // 2 min^2 + max x min
+  double* qrw = tmp + 2 * (size_t)r * r + (size_t)std::max(p, q) * r;   // svd_qr_work
   if (p >= q) {
     TTG_CUDA(cudaMemcpyAsync(Mw, M, sizeof(double) * (size_t)p * q, cudaMemcpyDeviceToDevice, s));
-    svd_tall(p, q, Mw, U, sigma, Vt, V, nrm, rank, counters, status, tmp, s);
+    svd_tall(p, q, Mw, U, sigma, Vt, V, nrm, rank, counters, status, tmp, s, qrw);
   } else {
     // M^T = V S U^T: run on the q x p transpose, then U_M = Vt_T^T, Vt_M = U_T^T
     transpose_f64(p, q, M, Mw, s);                        // Mw: q x p
     double* UT = T;                                       // q x p   (left vectors of M^T)
     double* VtT = U;                                      // p x p   written into U's storage
-    svd_tall(q, p, Mw, UT, sigma, VtT, V, nrm, rank, counters, status, tmp, s);
+    svd_tall(q, p, Mw, UT, sigma, VtT, V, nrm, rank, counters, status, tmp, s, qrw);
     // U (p x p) = VtT^T ; VtT currently occupies U: transpose through Mw
     TTG_CUDA(cudaMemcpyAsync(Mw, VtT, sizeof(double) * (size_t)p * p, cudaMemcpyDeviceToDevice, s));
     transpose_f64(p, p, Mw, U, s);

@@ -29,6 +29,10 @@
 // returns; the host turns the code into TTG_ERR_CUDA.
 #include "ttg_davidson.cuh"
 #include <cuda_bf16.h>
+#include <cstdlib>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 namespace ttg {
 namespace tc {
@@ -643,6 +647,94 @@ static void gemm_launch(const Tiled& A, const Tiled& B, int M, int N, OutT* out,
   else gemm_launch_bn<64>(A, B, M, N, out, rpv, vstride, rstride, cstride, err, s);
 }
 
+// Tile-width autotuner.  The first product of each shape class (tile counts
+// ceil(M/128), ceil(N/64), ceil(K/64) and the output type) times the three
+// tile widths on zeroed operands of that shape, three launches each after a
+// warm-up, with CUDA events on the caller's stream, and keeps the fastest;
+// later products of the class reuse it.  The cost model above is the choice
+// while a stream is being captured into a graph and when TTG_AUTOTUNE=0;
+// TTG_AUTOTUNE=2 prints each choice.
+struct TuneKey {
+  int mt, nt, kt, dbl;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(mt, nt, kt, dbl) < std::tie(o.mt, o.nt, o.kt, o.dbl);
+  }
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, int> g_tuned;
+
+template <class OutT>
+static float time_bn(int bn, const Tiled& A, char* bbuf, int M, int N, int K, OutT* out,
+                     int* err, cudaStream_t s) {
+  char* p = bbuf;
+  const Tiled B = make_tiled(N, K, bn, p);
+  cudaEvent_t e0, e1;
+  TTG_CUDA(cudaEventCreate(&e0));
+  TTG_CUDA(cudaEventCreate(&e1));
+  gemm_launch<OutT>(A, B, M, N, out, 1ll << 40, 0, 1, M, err, s);
+  TTG_CUDA(cudaEventRecord(e0, s));
+  for (int r = 0; r < 3; ++r) gemm_launch<OutT>(A, B, M, N, out, 1ll << 40, 0, 1, M, err, s);
+  TTG_CUDA(cudaEventRecord(e1, s));
+  TTG_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  TTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms;
+}
+
+static int tuned_bn(int M, int N, int K, bool out_double, cudaStream_t s) {
+  static const bool enabled = [] {
+    const char* v = std::getenv("TTG_AUTOTUNE");
+    return !(v && v[0] == '0');
+  }();
+  const int model = pick_bn(M, N, K);
+  if (!enabled) return model;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+    return model;
+  const TuneKey key{ceil_div(M, TM), ceil_div(N, 64), ceil_div(K, TK), out_double ? 1 : 0};
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tuned.find(key);
+  if (it != g_tuned.end()) return it->second;
+  // zeroed operands of this shape: A tiles, B tiles at the widest padding,
+  // the output and the wait flag
+  const size_t abytes = tiled_bytes(M, K, TM) + 1024, bbytes = tiled_bytes(N, K, 256) + 1024;
+  const size_t obytes = (size_t)M * N * (out_double ? 8 : 4) + 1024;
+  char* mem = nullptr;
+  if (cudaMalloc(&mem, abytes + bbytes + obytes + 1024) != cudaSuccess) {
+    (void)cudaGetLastError();
+    g_tuned[key] = model;
+    return model;
+  }
+  struct Free { char* p; ~Free() { cudaFree(p); } } fr{mem};
+  TTG_CUDA(cudaMemsetAsync(mem, 0, abytes + bbytes + obytes + 1024, s));
+  char* p = mem;
+  const Tiled A = make_tiled(M, K, TM, p);
+  char* bbuf = mem + abytes;
+  void* out = mem + abytes + bbytes;
+  int* err = (int*)(mem + abytes + bbytes + obytes);
+  int best = model;
+  float best_ms = 1e30f;
+  for (int bn : {64, 128, 256}) {
+    const float ms = out_double ? time_bn<double>(bn, A, bbuf, M, N, K, (double*)out, err, s)
+                                : time_bn<float>(bn, A, bbuf, M, N, K, (float*)out, err, s);
+    if (ms < best_ms * 0.97f || (bn == model && ms < best_ms * 1.03f)) { best_ms = ms; best = bn; }
+  }
+  int herr = 0;
+  TTG_CUDA(cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) throw Error{TTG_ERR_CUDA, "split gemm autotune: mbarrier wait timed out"};
+  g_tuned[key] = best;
+  static const bool verbose = [] {
+    const char* v = std::getenv("TTG_AUTOTUNE");
+    return v && v[0] == '2';
+  }();
+  if (verbose)
+    fprintf(stderr, "[ttg autotune] M=%d N=%d K=%d %s: BN=%d (%.1f us; cost model %d)\n", M, N, K,
+            out_double ? "f64" : "f32", best, best_ms * 1000.f / 3.f, model);
+  return best;
+}
+
 }  // namespace tc
 
 // prepared split operator of one local problem
@@ -664,10 +756,15 @@ struct SplitOp {
   float coef[256];      // A as FP32 in its own column-major order (small CORE)
 };
 
-static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* base) {
+// Sizing (op == nullptr) takes the widest tile padding so that the bytes
+// bound every tile width the autotuner may pick at layout time.
+static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* base,
+                           cudaStream_t s = nullptr) {
   const int M1 = (int)(L.rx1 * L.m * nvec_max), N1 = (int)(L.ra2 * L.ry2), K1 = (int)L.rx2;
   const int M3 = (int)L.ry1, N3 = (int)(L.n * L.ry2 * nvec_max), K3 = (int)(L.rx1 * L.ra1);
-  const int bn1 = tc::pick_bn(M1, N1, K1), bn3 = tc::pick_bn(M3, N3, K3);
+  const bool sizing = !(op && base);
+  const int bn1 = sizing ? 256 : tc::tuned_bn(M1, N1, K1, false, s);
+  const int bn3 = sizing ? 256 : tc::tuned_bn(M3, N3, K3, true, s);
   size_t tot = 0;
   tot += tc::tiled_bytes(M1, K1, tc::TM) + tc::tiled_bytes(N1, K1, bn1);
   tot += tc::tiled_bytes(M3, K3, tc::TM) + tc::tiled_bytes(N3, K3, bn3);
@@ -716,7 +813,7 @@ bool split_op_supported(const LocalDims& L) {
 // memory owned by the caller; mem holds the device buffers.
 void split_op_prepare(SplitOp* op, const LocalDims& L, int nvec_max, const double* phi1,
                       const double* A, const double* phi2, void* mem, cudaStream_t s) {
-  split_layout(L, nvec_max, op, (char*)mem);
+  split_layout(L, nvec_max, op, (char*)mem, s);
   op->A = A;
   // small TT-matrix cores travel as a kernel parameter of the CORE kernel
   const int ja = (int)(L.m * L.ra2), na = (int)(L.n * L.ra1);
