@@ -662,6 +662,117 @@ __global__ void __launch_bounds__(QRP_NT) qr_panel_kernel(int m, int w, double* 
   }
 }
 
+// The same panel factorization spread over a cooperative grid for tall
+// panels (one CTA holds FP64 at two FMAs per clock, so a 2048 x 32 panel is
+// FP64-bound on it): CTA b owns rows [b*chunk, (b+1)*chunk).  Per column,
+// the partial sums of squares and then the partial dot products with the
+// later columns go to per-column slots of part; after each grid barrier every
+// CTA adds the G partials in the same order, so all compute the same
+// reflector.  T comes from the panel's Gram matrix Y^T Y (partial sums per
+// CTA, added by CTA 0, which then runs the recurrence).
+constexpr int QRC_NT = 256;
+constexpr int QRC_GMAX = 32;
+__global__ void __launch_bounds__(QRC_NT) qr_panel_coop_kernel(int m, int w, double* A, i64 lda,
+                                                               double* tau, double* T, int ldt,
+                                                               double* part) {
+  cg::grid_group grid = cg::this_grid();
+  __shared__ double red[33];
+  __shared__ double zt[QRP_NB];
+  __shared__ double gram[QRP_NB * QRP_NB];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nwarp = QRC_NT / 32;
+  const int G = gridDim.x, b = blockIdx.x;
+  const int chunk = (m + G - 1) / G;
+  const int lo = min(m, b * chunk), hi = min(m, lo + chunk);
+  double* pn = part;                                 // [w][G]: sums of squares
+  double* pd = part + (size_t)QRP_NB * QRC_GMAX;     // [w][G][w]: dots
+  double* pg = pd + (size_t)QRP_NB * QRC_GMAX * QRP_NB;   // [G][w*w]: Gram
+  // partial sums of squares of column c below row c over the own rows
+  auto norm_part = [&](int c) {
+    const double* col = A + lda * c;
+    double t = 0.0;
+    for (int i = max(lo, c + 1) + tid; i < hi; i += QRC_NT) t = fma(col[i], col[i], t);
+    t = block_sum<QRC_NT>(t, red);
+    if (tid == 0) pn[(size_t)c * QRC_GMAX + b] = t;
+  };
+  norm_part(0);
+  for (int c = 0; c < w; ++c) {
+    double* col = A + lda * c;
+    grid.sync();   // column c final below the diagonal, its norm partials written
+    // row c may belong to another CTA: read it from L2 (this CTA's L1 may hold
+    // the line from a neighbouring own row); its owner overwrites it only
+    // after the next barrier
+    const double alpha = __ldcg(col + c);
+    double xn2 = 0.0;
+    for (int q = 0; q < G; ++q) xn2 += __ldcg(pn + (size_t)c * QRC_GMAX + q);
+    double tc = 0.0, sc = 0.0, beta = alpha;
+    if (xn2 != 0.0) {
+      beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+      tc = (beta - alpha) / beta;
+      sc = 1.0 / (alpha - beta);
+    }
+    if (b == 0 && tid == 0) tau[c] = tc;
+    if (tc != 0.0)
+      for (int i = max(lo, c + 1) + tid; i < hi; i += QRC_NT) col[i] *= sc;
+    __syncthreads();
+    // partial dots v^T a_cc over the own rows (the owner of row c adds a_cc(c))
+    for (int cc = c + 1 + wid; cc < w; cc += nwarp) {
+      const double* a = A + lda * cc;
+      double d = (lane == 0 && c >= lo && c < hi) ? a[c] : 0.0;
+      for (int i = max(lo, c + 1) + lane; i < hi; i += 32) d = fma(col[i], a[i], d);
+      d = warp_sum(d);
+      if (lane == 0) pd[((size_t)c * QRC_GMAX + b) * QRP_NB + cc] = d;
+    }
+    grid.sync();   // dots complete; every CTA has read alpha
+    if (c >= lo && c < hi && tid == 0) col[c] = beta;
+    if (tc != 0.0) {
+      for (int cc = c + 1 + wid; cc < w; cc += nwarp) {
+        double d = 0.0;
+        for (int q = 0; q < G; ++q) d += __ldcg(pd + ((size_t)c * QRC_GMAX + q) * QRP_NB + cc);
+        d *= tc;
+        double* a = A + lda * cc;
+        if (lane == 0 && c >= lo && c < hi) a[c] -= d;
+        for (int i = max(lo, c + 1) + lane; i < hi; i += 32) a[i] = fma(-d, col[i], a[i]);
+      }
+    }
+    __syncthreads();
+    if (c + 1 < w) norm_part(c + 1);
+  }
+  // Gram of Y (unit diagonal, zeros above) over the own rows
+  for (int e = tid; e < w * w; e += QRC_NT) {
+    const int i = e % w, j = e / w;
+    double g = 0.0;
+    if (i <= j) {
+      for (int r = max(lo, j); r < hi; ++r) {
+        const double yi = r == i ? 1.0 : (r > i ? A[r + lda * i] : 0.0);
+        const double yj = r == j ? 1.0 : A[r + lda * j];
+        g = fma(yi, yj, g);
+      }
+    }
+    pg[(size_t)b * QRP_NB * QRP_NB + e] = g;
+  }
+  grid.sync();
+  if (b != 0) return;
+  for (int e = tid; e < w * w; e += QRC_NT) {
+    double g = 0.0;
+    for (int q = 0; q < G; ++q) g += __ldcg(pg + (size_t)q * QRP_NB * QRP_NB + e);
+    gram[e] = g;
+  }
+  for (int e = tid; e < ldt * w; e += QRC_NT) T[e] = 0.0;
+  __syncthreads();
+  // T[0:i, i] = -tau_i T[0:i, 0:i] (Y[:, 0:i]^T y_i), Y^T y_i = gram[0:i, i]
+  for (int i = 0; i < w; ++i) {
+    if (tid < i) zt[tid] = -tau[i] * gram[tid + w * i];
+    __syncthreads();
+    if (tid < i) {
+      double v = 0.0;
+      for (int k = tid; k < i; ++k) v = fma(T[tid + (i64)ldt * k], zt[k], v);
+      T[tid + (i64)ldt * i] = v;
+    }
+    if (tid == 0) T[i + (i64)ldt * i] = tau[i];
+    __syncthreads();
+  }
+}
+
 // Y (m x w) with the unit diagonal and zeros above it, from a factored panel
 __global__ void qr_make_y_kernel(int m, int w, const double* __restrict__ A, i64 lda,
                                  double* __restrict__ Y) {
@@ -704,7 +815,9 @@ __global__ void qr_vt_kernel(int q, const double* __restrict__ Ux, const int* __
 // doubles of the QR-preconditioned path's own workspace
 static size_t svd_qr_work(size_t p, size_t q) {
   const size_t npan = (q + QRP_NB - 1) / QRP_NB;
-  return p * q + 3 * q * q + npan * QRP_NB * QRP_NB + p * QRP_NB + 2 * QRP_NB * q + 2 * q + 256;
+  const size_t coop = QRP_NB * QRC_GMAX + QRP_NB * QRC_GMAX * QRP_NB + QRC_GMAX * QRP_NB * QRP_NB;
+  return p * q + 3 * q * q + npan * QRP_NB * QRP_NB + p * QRP_NB + 2 * QRP_NB * q + 2 * q + 256 +
+         coop + 64;
 }
 
 size_t svd_scratch(int p, int q) {
@@ -736,6 +849,7 @@ static void svd_tall_qr(int p, int q, double* Mw, double* U, double* sigma, doub
   double* G2 = G1 + (size_t)QRP_NB * q;                 // NB x q
   double* tau = G2 + (size_t)QRP_NB * q;                // q
   int* perm = (int*)(tau + q);                          // q ints
+  double* qpart = tau + 2 * (size_t)q + 64;             // cooperative panel partials
   auto gemm = [&](int M, int N, int K, const double* Am, i64 sAm, i64 sAk, const double* Bm,
                   i64 sBk, i64 sBn, double* C, i64 sCm, i64 sCn, double alpha, double beta) {
     GemmF64 g;
@@ -759,8 +873,26 @@ static void svd_tall_qr(int p, int q, double* Mw, double* U, double* sigma, doub
     const int j0 = k * QRP_NB, w = std::min(QRP_NB, q - j0), m = p - j0;
     double* Ap = A + j0 + (i64)p * j0;
     double* Tk = Tf + (size_t)k * QRP_NB * QRP_NB;
-    qr_panel_kernel<<<1, QRP_NT, 0, s>>>(m, w, Ap, p, tau + j0, Tk, QRP_NB);
-    TTG_CHECK_LAUNCH();
+    if (m >= 1024) {
+      static const int coop_max = [] {
+        int dev = 0, nsm = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, qr_panel_coop_kernel, QRC_NT, 0);
+        return std::max(1, nsm * per);
+      }();
+      int G = std::min(std::min(QRC_GMAX, std::max(1, m / 128)), coop_max);
+      int mm = m, ww = w, ldt = QRP_NB;
+      i64 ld = p;
+      double* tk = tau + j0;
+      void* args[] = {&mm, &ww, &Ap, &ld, &tk, &Tk, &ldt, &qpart};
+      TTG_CUDA(cudaLaunchCooperativeKernel((const void*)qr_panel_coop_kernel, dim3(G),
+                                           dim3(QRC_NT), args, 0, s));
+      ++g_launches;
+    } else {
+      qr_panel_kernel<<<1, QRP_NT, 0, s>>>(m, w, Ap, p, tau + j0, Tk, QRP_NB);
+      TTG_CHECK_LAUNCH();
+    }
     const int n2 = q - j0 - w;
     if (n2 > 0) {
       qr_make_y_kernel<<<gbl((i64)m * w), 256, 0, s>>>(m, w, Ap, p, Yp);
