@@ -49,11 +49,64 @@ static void col_dots(i64 N, int t, const double* U, const double* V, double* out
   TTG_CHECK_LAUNCH();
 }
 
-// q[:, j] -= theta_j p[:, j]
+// q[:, j] -= theta_j p[:, j]; block 0 also clears the step's accumulators
+// pq and rr_new (nothing reads them before they are summed again)
 __global__ void shift_kernel(i64 N, int t, const double* __restrict__ theta,
-                             const double* __restrict__ p, double* __restrict__ q) {
+                             const double* __restrict__ p, double* __restrict__ q,
+                             double* __restrict__ pq, double* __restrict__ rr_new) {
+  if (blockIdx.x == 0 && threadIdx.x < t) {
+    pq[threadIdx.x] = 0.0;
+    rr_new[threadIdx.x] = 0.0;
+  }
   for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < N * t; e += (i64)gridDim.x * blockDim.x)
     q[e] -= theta[e / N] * p[e];
+}
+
+// q -= X C (X: N x nb, C: nb x t) and pq[j] += p[:, j]^T q[:, j] (pq cleared
+// by shift_kernel): the projection of the CG step fused with its p^T q
+constexpr int PD_MAXT = 16;
+__global__ void __launch_bounds__(128) proj_dot_kernel(i64 N, int t, int nb,
+                                                       const double* __restrict__ X,
+                                                       const double* __restrict__ C,
+                                                       const double* __restrict__ p,
+                                                       double* __restrict__ q,
+                                                       double* __restrict__ pq) {
+  __shared__ double Cs[PD_MAXT * PD_MAXT];
+  __shared__ double red[4][PD_MAXT];
+  for (int e = threadIdx.x; e < nb * t; e += blockDim.x) Cs[e] = C[e];
+  __syncthreads();
+  double acc[PD_MAXT];
+#pragma unroll
+  for (int j = 0; j < PD_MAXT; ++j) acc[j] = 0.0;
+  for (i64 r = blockIdx.x * (i64)blockDim.x + threadIdx.x; r < N; r += (i64)gridDim.x * blockDim.x) {
+    double xr[PD_MAXT];
+#pragma unroll
+    for (int k = 0; k < PD_MAXT; ++k) xr[k] = k < nb ? X[r + N * k] : 0.0;
+#pragma unroll
+    for (int j = 0; j < PD_MAXT; ++j) {
+      if (j >= t) break;
+      double v = q[r + N * j];
+#pragma unroll
+      for (int k = 0; k < PD_MAXT; ++k)
+        if (k < nb) v = fma(-xr[k], Cs[k + nb * j], v);
+      q[r + N * j] = v;
+      acc[j] = fma(p[r + N * j], v, acc[j]);
+    }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < PD_MAXT; ++j) {
+    if (j >= t) break;
+    double v = acc[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[w][j] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < t) {
+    const double v = red[0][threadIdx.x] + red[1][threadIdx.x] + red[2][threadIdx.x] + red[3][threadIdx.x];
+    atomicAdd(&pq[threadIdx.x], v);
+  }
 }
 
 // CG step on column j (frozen when inactive or when p^T q <= 0):
@@ -205,13 +258,23 @@ struct JdCg {
     TTG_CUDA(cudaMemcpyAsync(p, r, bytes_t, cudaMemcpyDeviceToDevice, s));
     col_dots(N, t, r, r, rr, s);
     TTG_CUDA(cudaMemcpyAsync(rr0, rr, sizeof(double) * t, cudaMemcpyDeviceToDevice, s));
+    const bool fused = t <= PD_MAXT && nb <= PD_MAXT;
+    int pb = (int)std::max<i64>(1, std::min<i64>(1024, (N + 127) / 128));
     for (int it = 0; it < iters; ++it) {
       low(p, q, t);                                   // q = A~ p
-      shift_kernel<<<eb, 256, 0, s>>>(N, t, theta, p, q);   // q -= theta p
+      shift_kernel<<<eb, 256, 0, s>>>(N, t, theta, p, q, pq, rr_new);   // q -= theta p
       TTG_CHECK_LAUNCH();
-      project(q, t, X, nb);                           // q = P q
-      col_dots(N, t, p, q, pq, s);
-      TTG_CUDA(cudaMemsetAsync(rr_new, 0, sizeof(double) * t, s));
+      if (fused) {
+        // q = P q with pq = p^T q in the same pass
+        double* c = sc + 6 * 64;
+        gemm_tn_small(nb, t, N, X, N, q, N, c, nb, 1.0, 0.0, s);
+        proj_dot_kernel<<<pb, 128, 0, s>>>(N, t, nb, X, c, p, q, pq);
+        TTG_CHECK_LAUNCH();
+      } else {
+        project(q, t, X, nb);                         // q = P q
+        col_dots(N, t, p, q, pq, s);
+        TTG_CUDA(cudaMemsetAsync(rr_new, 0, sizeof(double) * t, s));
+      }
       cg_update_kernel<<<dim3(bx, t), 256, 0, s>>>(N, rr, pq, rr0, tol2, p, q, x, r, rr_new);
       TTG_CHECK_LAUNCH();
       cg_dir_kernel<<<eb, 256, 0, s>>>(N, t, rr, rr_new, pq, rr0, tol2, r, p);
