@@ -183,9 +183,54 @@ def tt_dot(d, n, rx, x, ry, y):
     return P[0, 0]
 
 
+def tt_norm(d, n, r, cores):
+    """2-norm of a TT vector by a left-to-right QR sweep (no cancellation)."""
+    if np.isscalar(n):
+        n = [int(n)] * d
+    R = np.ones((1, 1), dtype=np.asarray(cores).dtype)
+    off = 0
+    for k in range(d):
+        sz = r[k] * n[k] * r[k + 1]
+        C = np.asarray(cores[off:off + sz]).reshape(r[k], n[k] * r[k + 1], order="F")
+        off += sz
+        C = (R @ C).reshape(-1, r[k + 1], order="F")
+        if k == d - 1:
+            return float(np.linalg.norm(C))
+        _, R = np.linalg.qr(C)
+    return float(np.linalg.norm(R))
+
+
+def tt_sub(d, n, rx, x, ry, y):
+    """x - y as one TT vector with ranks rx + ry (block cores)."""
+    if np.isscalar(n):
+        n = [int(n)] * d
+    out, r = [], [1]
+    ox = oy = 0
+    for k in range(d):
+        X = np.asarray(x[ox:ox + rx[k] * n[k] * rx[k + 1]]).reshape(rx[k], n[k], rx[k + 1], order="F")
+        Y = np.asarray(y[oy:oy + ry[k] * n[k] * ry[k + 1]]).reshape(ry[k], n[k], ry[k + 1], order="F")
+        ox += X.size
+        oy += Y.size
+        a = 1 if k == 0 else rx[k] + ry[k]
+        b = 1 if k == d - 1 else rx[k + 1] + ry[k + 1]
+        Z = np.zeros((a, n[k], b), dtype=np.result_type(X, Y))
+        if d == 1:
+            Z[:] = X - Y
+        elif k == 0:
+            Z[:, :, :rx[1]] = X
+            Z[:, :, rx[1]:] = -Y
+        elif k == d - 1:
+            Z[:rx[k], :, :] = X
+            Z[rx[k]:, :, :] = Y
+        else:
+            Z[:rx[k], :, :rx[k + 1]] = X
+            Z[rx[k]:, :, rx[k + 1]:] = Y
+        out.append(Z.ravel(order="F"))
+        r.append(b)
+    return r, np.concatenate(out)
+
+
 def tt_rel_diff(d, n, rx, x, ry, y):
-    """||x - y|| / ||y|| of two TT vectors through TT inner products."""
-    xx = tt_dot(d, n, rx, x, rx, x).real
-    yy = tt_dot(d, n, ry, y, ry, y).real
-    xy = tt_dot(d, n, rx, x, ry, y).real
-    return float(np.sqrt(max(xx - 2 * xy + yy, 0.0) / yy))
+    """||x - y|| / ||y|| of two TT vectors, both norms by QR sweeps."""
+    rz, z = tt_sub(d, n, rx, x, ry, y)
+    return tt_norm(d, n, rz, z) / tt_norm(d, n, ry, y)
