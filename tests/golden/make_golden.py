@@ -52,11 +52,30 @@ def sdv_layout(ref):
                    "body_sha256": hashlib.sha256(raw[128:]).hexdigest()}, f, indent=1)
 
 
+def cme_fixture(ref):
+    """The chemical-master-equation KSL case of test_ksl_cme.f90: operator
+    cme20_A.sdv (TT-matrix, mode sizes n*n) and start cme20_u0.sdv, both
+    complex files with zero imaginary parts, stored here as real arrays with
+    the mode sizes n = sqrt(A's mode sizes) (test_ksl_cme.f90:71-79) and
+    tau = T / Nt from test_ksl_cme.inp."""
+    nA, rA, cA = read_sdv(os.path.join(ref, "cme20_A.sdv"), complex_=True)
+    nu, ru, cu = read_sdv(os.path.join(ref, "cme20_u0.sdv"), complex_=True)
+    assert np.abs(cA.imag).max() == 0.0 and np.abs(cu.imag).max() == 0.0
+    n = np.array([int(round(np.sqrt(v))) for v in nA])
+    assert list(n) == list(nu)
+    lines = open(os.path.join(ref, "test_ksl_cme.inp")).read().split()
+    T, Nt = float(lines[3]), int(lines[4])
+    np.savez_compressed(os.path.join(HERE, "cme20_ksl.npz"), n=n, ra=np.array(rA),
+                        crA=cA.real.copy(), ry=np.array(ru), crY=cu.real.copy(),
+                        tau=np.array(T / Nt), nsteps_reference=np.array(Nt))
+
+
 def main(ref):
     n, r, cores = read_sdv(os.path.join(ref, "Heisen_20.sdv"))
     np.savez_compressed(os.path.join(HERE, "heisen20_sdv.npz"), n=np.array(n), r=np.array(r),
                         cores=cores)
     sdv_layout(ref)
+    cme_fixture(ref)
     for name in ("test_ksl.dat", "test_eye_ksl.dat"):
         D = read_ksl_dat(os.path.join(ref, name))
         np.savez_compressed(os.path.join(HERE, name.replace(".dat", "_dat.npz")),

@@ -131,3 +131,36 @@ def test_diag_ksl_exact_on_separable(ctx):
     for k in range(1, d):
         ex = np.kron(y0[k] * np.exp(tau * a[k]), ex)
     assert _rel(tt_full(d, [nn] * d, ry1, cores), ex) < 1e-12
+
+
+def _cme():
+    import os
+    from conftest import GOLDEN
+    f = np.load(os.path.join(GOLDEN, "cme20_ksl.npz"))
+    n = [int(v) for v in f["n"]]
+    return (len(n), n, [int(v) for v in f["ra"]], f["crA"].astype(np.complex128),
+            [int(v) for v in f["ry"]], f["crY"].astype(np.complex128), float(f["tau"]))
+
+
+def test_ksl_cme_fixture_two_steps(ctx):
+    """The reference's own KSL application (test_ksl_cme.f90: the chemical
+    master equation of cme20_A.sdv / cme20_u0.sdv, d = 121, tau = T/Nt = 0.01):
+    two steps on the GPU against two oracle steps, and the chosen (split)
+    method against the plain one.  Each step runs 2d - 1 = 241 local Krylov
+    exponentials, each accurate to Expokit's tolerance 1e-8, so two correct
+    implementations (different summation orders, which move the step-size
+    choices) differ by a few 1e-8 per step (measured 1.9e-8 after one step,
+    4e-8 after two); the bar here is 1e-7 after two steps."""
+    import ttgpu
+    d, n, ra, crA, ry, crY, tau = _cme()
+    cores, ry1 = ttgpu.ztt_ksl(d, n, n, ra, crA, crY, ry, tau, 500, nsteps=2, ctx=ctx)
+    c, r = crY, list(ry)
+    for _ in range(2):
+        out = oracle_ksl(d, n, n, ra, crA, c, r, tau, 500)
+        c, r = out["cores"], out["ry"]
+    assert ry1 == r
+    from ttgpu.operators import tt_rel_diff
+    assert tt_rel_diff(d, n, ry1, cores, r, c) < 1e-7
+    cs, rs = ttgpu.ztt_ksl(d, n, n, ra, crA, crY, ry, tau, 500, nsteps=2, method="split", ctx=ctx)
+    assert rs == ry1
+    assert tt_rel_diff(d, n, rs, cs, ry1, cores) < 1e-4
