@@ -933,18 +933,21 @@ void split_matvec_factory(const LocalDims& L, const double* phi1, const double* 
 }
 
 // Reads the bounded-wait flags of the calling thread's prepared split
-// operators (set by a GEMM whose mbarrier wait gave up); throws when set.
-void split_matvec_check(cudaStream_t s) {
+// operators in slots [0, nslots) (set by a GEMM whose mbarrier wait gave up);
+// throws when set.  Only slots the caller prepared itself may be named: a
+// slot left from an earlier call points into memory that call has freed.
+void split_matvec_check(cudaStream_t s, int nslots) {
+  TTG_REQUIRE(nslots >= 1 && nslots <= kSplitSlots, "split matvec: bad slot count");
   int herr[kSplitSlots] = {};
   bool any = false;
-  for (int k = 0; k < kSplitSlots; ++k) {
+  for (int k = 0; k < nslots; ++k) {
     if (!op_store_set[k] || !op_store[k].err) continue;
     TTG_CUDA(cudaMemcpyAsync(&herr[k], op_store[k].err, sizeof(int), cudaMemcpyDeviceToHost, s));
     any = true;
   }
   if (!any) return;
   TTG_CUDA(cudaStreamSynchronize(s));
-  for (int k = 0; k < kSplitSlots; ++k)
+  for (int k = 0; k < nslots; ++k)
     if (herr[k]) throw Error{TTG_ERR_CUDA, "split gemm: mbarrier wait timed out"};
 }
 
