@@ -239,6 +239,18 @@ int ttg_eigb(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m, const 
 int ttg_ksl_z(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m, const ttg_int* ra,
               const double* crA, const double* crY0, ttg_int* ry, double tau, ttg_int rmax,
               int verb, int typ, int order, int method, ttg_int nsteps);
+/* KSL time stepping with real data, tt_ksl tt_ksl.f90:191-428: the real
+ * routine's own sweep (backward half sweep with the S-step on the bond to
+ * the right of each core, forward half sweep with the S-step before each
+ * K-step), always symmetric (typ is read and unused, as in the reference).
+ * The S operator multiplies with 1 and 0 where the reference's dsfun_matvec
+ * uses its undeclared ONE and ZERO (tt_ksl.f90:122-130).  Every rank must
+ * pass both QR sweeps unchanged.  With d = 1 one call is a forward half step,
+ * as in the reference.  Arguments as ttg_ksl_z, real arrays; results through
+ * ttg_result_copy. */
+int ttg_ksl_d(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m, const ttg_int* ra,
+              const double* crA, const double* crY0, ttg_int* ry, double tau, ttg_int rmax,
+              int verb, int typ, int order, int method, ttg_int nsteps);
 /* KSL for an operator diagonal in the physical index, ztt_diag_ksl
  * tt_diag_ksl.f90:560-804 (complex, interleaved) and dtt_diag_ksl :315-558
  * (real): crA holds the cores A(a1, i, a2) (ra[k] x n[k] x ra[k+1]); each

@@ -144,6 +144,113 @@ def ztt_ksl(d, n, m, ra, crA, crY0, ry, tau, rmax, typ=2, order=8, verb=0):
     return {"cores": cores, "ry": ry, "stats": stats}
 
 
+def tt_ksl_real(d, n, m, ra, crA, crY0, ry, tau, rmax, order=8, usenrm=1):
+    """One step of the real-valued ``tt_ksl`` (tt_ksl.f90:191-428), a
+    different scheme from ``ztt_ksl``: always symmetric (tau/2 everywhere),
+    and one sweep = a backward half sweep i = d..1 (K-step on core i; for
+    i < d the S-step on the bond (i, i+1) from the left QR factor of the new
+    core, folded back into core i; for i > 1 the right QR of core i pushed into
+    core i-1) followed by a forward half sweep i = 1..d (for i < d the S-step
+    of the left QR of core i, then the K-step; for i < d the left QR pushed
+    into core i+1).
+
+    Norm estimates as the reference calls them: the K-step passes ``dmatvec``
+    as its own transpose (tt_ksl.f90:38-45), and the S-step's
+    ``dsfun_matvec_transp`` writes its product into its input, so
+    ``normest_higham`` continues with the sign vectors themselves (identity,
+    as the complex S-step); the estimator is the one-sided Higham iteration
+    of ``oracle/normest.py`` (the reference's real DLACN1 with its own random
+    signs gives other estimates; they only move the Krylov step sizes).
+    usenrm 2 takes anorm = 1.  The reference's ``dsfun_matvec`` multiplies
+    with the undeclared ``ONE`` and ``ZERO`` (tt_ksl.f90:122-130); this
+    restatement uses 1 and 0, the values that code means.  Computed in complex
+    arithmetic on real data; returns dict(cores (real), ry).  The ranks are
+    fixed; they must pass the QR steps unchanged (r_{k+1} <= r_k n_k after
+    the left-to-right QR, r_k <= n_k r_{k+1})."""
+    n = list(map(int, n)); m = list(map(int, m)); ra = list(map(int, ra))
+    ry = list(map(int, ry))
+    crA = np.asarray(crA, dtype=np.complex128)
+    eps = 1e-8
+    pa = compute_ps(d, ra, [n[i] * m[i] for i in range(d)])
+    Acore = [crA[pa[i]:pa[i + 1]] for i in range(d)]
+    cr = []
+    off = 0
+    for i in range(d):
+        sz = ry[i] * n[i] * ry[i + 1]
+        cr.append(np.array(crY0[off:off + sz], dtype=np.complex128))
+        off += sz
+    phi = [None] * (d + 1)
+    phi[0] = np.ones(1, dtype=np.complex128)
+    phi[d] = np.ones(1, dtype=np.complex128)
+    for i in range(d - 1):
+        rnew = min(ry[i] * n[i], ry[i + 1])
+        q, r = zqr_lapack(ry[i] * n[i], ry[i + 1], cr[i])
+        cr[i] = q
+        cr[i + 1] = flat(F(r, rnew, ry[i + 1]) @ F(cr[i + 1], ry[i + 1], n[i + 1] * ry[i + 2]))
+        ry[i + 1] = rnew
+        phi[i + 1] = phi_left(ry[i], m[i], ry[i + 1], ry[i], n[i], ry[i + 1], ra[i], ra[i + 1],
+                              phi[i], Acore[i], cr[i], cr[i], conj=True)
+    for i in range(d - 1):
+        if ry[i] * n[i] < ry[i + 1] or n[i + 1] * ry[i + 2] < ry[i + 1]:
+            raise ValueError("tt_ksl needs ranks its QR steps keep")
+    seed = Seed()
+    t2 = tau / 2
+
+    def kexp(i, x):
+        r1, r2 = ry[i], ry[i + 1]
+        N = r1 * n[i] * r2
+        mv = lambda v: bfun3(r1, n[i], r2, r1, n[i], r2, ra[i], ra[i + 1], phi[i], Acore[i],  # noqa: E731
+                             phi[i + 1], v)
+        anorm = 1.0 if usenrm == 2 else znormest(N, 4, _cols(mv), _cols(mv), seed)
+        w, _ = zexp_mv(N, order, t2, x, eps, anorm, mv)
+        return w
+
+    def sexp(i, ph1, R):
+        r = ry[i + 1]
+        mv = sfun(r, r, ra[i + 1], r, r, ph1, phi[i + 1])
+        anorm = 1.0 if usenrm == 2 else znormest(r * r, 4, _cols(mv), None, seed)
+        w, _ = zexp_mv(r * r, order, -t2, R, eps, anorm, mv)
+        return w
+
+    def left_s(i, core):
+        # QR of core i (ry_i n_i x ry_{i+1}), S-step of R, core i = Q S
+        r1, r2 = ry[i], ry[i + 1]
+        q, R = zqr_lapack(r1 * n[i], r2, core)
+        ph = phi_left(r1, m[i], r2, r1, n[i], r2, ra[i], ra[i + 1], phi[i], Acore[i], q, q,
+                      conj=True)
+        S = sexp(i, ph, R)
+        return flat(F(q, r1 * n[i], r2) @ F(S, r2, r2))
+
+    # backward half sweep; with d = 1 neither branch stores the K-step, so
+    # the reference's result is the forward half step alone
+    for i in range(d - 1, -1, -1):
+        curcr = kexp(i, cr[i])
+        if i < d - 1:
+            curcr = left_s(i, curcr)
+            cr[i] = curcr
+        if i > 0:
+            r1, r2 = ry[i], ry[i + 1]
+            ct = dtransp(r1, n[i] * r2, curcr)                        # (n r2) x r1
+            q, R = zqr_lapack(n[i] * r2, r1, ct)
+            cr[i] = dtransp(n[i] * r2, r1, q)                         # r1 x (n r2)
+            cr[i - 1] = flat(F(cr[i - 1], ry[i - 1] * n[i - 1], r1) @ F(R, r1, r1).T)
+            phi[i] = phi_right(r1, m[i], r2, r1, n[i], r2, ra[i], ra[i + 1], phi[i + 1],
+                               Acore[i], cr[i], cr[i], conj=True)
+    # forward half sweep
+    for i in range(d):
+        curcr = left_s(i, cr[i]) if i < d - 1 else cr[i]
+        cr[i] = kexp(i, curcr)
+        if i < d - 1:
+            r1, r2 = ry[i], ry[i + 1]
+            q, R = zqr_lapack(r1 * n[i], r2, cr[i])
+            cr[i] = q
+            cr[i + 1] = flat(F(R, r2, r2) @ F(cr[i + 1], r2, n[i + 1] * ry[i + 2]))
+            phi[i + 1] = phi_left(r1, m[i], r2, r1, n[i], r2, ra[i], ra[i + 1], phi[i],
+                                  Acore[i], cr[i], cr[i], conj=True)
+    cores = np.concatenate([cr[k][:ry[k] * n[k] * ry[k + 1]] for k in range(d)])
+    return {"cores": cores.real.copy(), "ry": ry}
+
+
 def _slice(a, r1, n, r2, k):
     return flat(F(a, r1, n, r2)[:, k, :])
 

@@ -130,3 +130,73 @@ def test_diag_ksl_oracle_is_exact_on_separable_diagonal_operators():
         ex = np.kron(y0[k] * np.exp(tau * a[k]), ex)
     x1 = tt_full(d, [nn] * d, out["ry"], out["cores"])
     assert np.linalg.norm(x1 - ex) <= 1e-12 * np.linalg.norm(ex)
+
+
+def scaled_identity(d, nn, c):
+    """c * I as a rank-1 TT-matrix (real)."""
+    cores = []
+    for k in range(d):
+        core = np.eye(nn).reshape(1, nn, nn, 1) * (c if k == 0 else 1.0)
+        cores.append(core.ravel(order="F"))
+    return [1] * (d + 1), np.concatenate(cores)
+
+
+def test_tt_ksl_real_scaled_identity_is_exact():
+    """The real tt_ksl scheme on A = c I: every K-step multiplies by
+    exp(c tau/2) and every S-step by exp(-c tau/2); d + d K-steps against
+    (d-1) + (d-1) S-steps leave exp(c tau) y0 for any start of any rank."""
+    from oracle.ksl import tt_ksl_real
+    d, nn, c, tau = 5, 3, 0.7, 0.3
+    ra, crA = scaled_identity(d, nn, c)
+    ry = [1, 3, 4, 4, 3, 1]
+    rng = np.random.default_rng(1)
+    y = np.concatenate([rng.standard_normal(ry[k] * nn * ry[k + 1]) for k in range(d)])
+    out = tt_ksl_real(d, [nn] * d, [nn] * d, ra, crA, y, ry, tau, 10)
+    x0 = tt_full(d, [nn] * d, ry, y)
+    x1 = tt_full(d, [nn] * d, out["ry"], out["cores"])
+    assert out["ry"] == ry
+    assert np.linalg.norm(x1 - np.exp(c * tau) * x0) <= 1e-12 * np.linalg.norm(x0)
+
+
+def test_tt_ksl_real_is_second_order_on_separable_operators():
+    """The real scheme's forward half sweep does the S-step of each bond
+    before the K-step of the core on its left, so unlike ztt_ksl it is not
+    exact on a Kronecker sum with a rank-1 start.  Its one-step error is
+    O(tau^3): halving tau divides it by about 8."""
+    from oracle.ksl import tt_ksl_real
+    d, nn = 5, 3
+    crA, ra, full, y = separable(d, nn, 0)
+    crA, full, y = crA.real.copy(), full.real.copy(), y.real.copy()
+    x0 = tt_full(d, [nn] * d, [1] * (d + 1), y)
+    errs = []
+    for tau in (0.05, 0.025):
+        out = tt_ksl_real(d, [nn] * d, [nn] * d, ra, crA, y, [1] * (d + 1), tau, 10)
+        x1 = tt_full(d, [nn] * d, out["ry"], out["cores"])
+        ref = sla.expm(tau * full) @ x0
+        errs.append(np.linalg.norm(x1 - ref) / np.linalg.norm(ref))
+    assert errs[0] < 1e-3
+    assert 6.0 < errs[0] / errs[1] < 10.0
+
+
+def test_tt_ksl_real_single_core_is_a_half_step():
+    """d = 1: the backward K-step is never stored, so one call returns
+    exp(tau/2 A) y0."""
+    from oracle.ksl import tt_ksl_real
+    rng = np.random.default_rng(2)
+    nn, tau = 6, 0.2
+    a = rng.standard_normal((nn, nn))
+    y = rng.standard_normal(nn)
+    out = tt_ksl_real(1, [nn], [nn], [1, 1], a.ravel(order="F"), y, [1, 1], tau, 10)
+    ref = sla.expm(tau / 2 * a) @ y
+    assert np.linalg.norm(out["cores"] - ref) <= 1e-10 * np.linalg.norm(ref)
+
+
+def test_tt_ksl_real_rejects_ranks_the_qr_would_cut():
+    from oracle.ksl import tt_ksl_real
+    import pytest
+    d, nn = 3, 2
+    ra, crA = scaled_identity(d, nn, 1.0)
+    ry = [1, 2, 4, 1]            # r_2 = 4 > n_3 r_3 = 2
+    y = np.ones(sum(ry[k] * nn * ry[k + 1] for k in range(d)))
+    with pytest.raises(ValueError):
+        tt_ksl_real(d, [nn] * d, [nn] * d, ra, crA, y, ry, 0.1, 10)

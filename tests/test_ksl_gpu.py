@@ -164,3 +164,82 @@ def test_ksl_cme_fixture_two_steps(ctx):
     cs, rs = ttgpu.ztt_ksl(d, n, n, ra, crA, crY, ry, tau, 500, nsteps=2, method="split", ctx=ctx)
     assert rs == ry1
     assert tt_rel_diff(d, n, rs, cs, ry1, cores) < 1e-4
+
+
+def test_tt_ksl_real_scaled_identity(ctx):
+    """Real tt_ksl scheme, A = c I: exp(c tau) y0 for a start of any rank."""
+    import ttgpu
+    from test_ksl import scaled_identity
+    d, nn, c, tau = 5, 3, 0.7, 0.3
+    ra, crA = scaled_identity(d, nn, c)
+    ry = [1, 3, 4, 4, 3, 1]
+    rng = np.random.default_rng(1)
+    y = np.concatenate([rng.standard_normal(ry[k] * nn * ry[k + 1]) for k in range(d)])
+    cores, ry1 = ttgpu.tt_ksl(d, [nn] * d, [nn] * d, ra, crA, y, ry, tau, 10, ctx=ctx)
+    assert cores.dtype == np.float64 and ry1 == ry
+    x0 = tt_full(d, [nn] * d, ry, y)
+    assert _rel(tt_full(d, [nn] * d, ry1, cores), np.exp(c * tau) * x0) < 1e-12
+
+
+@pytest.mark.parametrize("d,n,r,steps", [(6, 8, 4, 3), (4, 4, 2, 2)])
+def test_tt_ksl_real_matches_oracle(ctx, d, n, r, steps):
+    """Real tt_ksl (tt_ksl.f90:191-428) on the KSL operator family with a real
+    start, nsteps on the device against the oracle called step by step."""
+    import ttgpu
+    from oracle.ksl import tt_ksl_real
+    from ttgpu.operators import random_tt
+    tau = 1e-3
+    nn, mm, ra, crA = ksl_operator(d=d, n=n, rank=4, std=0.1, seed=5)
+    _, ry, y = random_tt(d, n, r, seed=6)
+    cores, ry1 = ttgpu.tt_ksl(d, nn, mm, ra, crA, y, ry, tau, 64, nsteps=steps, ctx=ctx)
+    c, rr = y, list(ry)
+    for _ in range(steps):
+        out = tt_ksl_real(d, nn, mm, ra, crA, c, rr, tau, 64)
+        c, rr = out["cores"], out["ry"]
+    assert ry1 == rr
+    assert _rel(tt_full(d, nn, ry1, cores), tt_full(d, nn, rr, c)) < 1e-8
+
+
+def test_tt_ksl_real_split_against_fp64(ctx):
+    """Chosen form for the real scheme: K-step products on the BF16x3
+    tensor-core operator; bar 1e-5 relative to the FP64 state."""
+    import ttgpu
+    from ttgpu.operators import random_tt
+    d, n, r, steps, tau = 5, 16, 8, 3, 1e-3
+    nn, mm, ra, crA = ksl_operator(d=d, n=n, rank=4, std=0.1, seed=7)
+    _, ry, y = random_tt(d, n, r, seed=8)
+    c64, r64 = ttgpu.tt_ksl(d, nn, mm, ra, crA, y, ry, tau, 64, nsteps=steps, ctx=ctx)
+    csp, rsp = ttgpu.tt_ksl(d, nn, mm, ra, crA, y, ry, tau, 64, nsteps=steps, method="split",
+                            ctx=ctx)
+    assert rsp == r64
+    assert _rel(tt_full(d, nn, rsp, csp), tt_full(d, nn, r64, c64)) < 1e-5
+
+
+def test_tt_ksl_real_single_core_half_step(ctx):
+    import ttgpu
+    import scipy.linalg as sla
+    rng = np.random.default_rng(2)
+    nn, tau = 6, 0.2
+    a = rng.standard_normal((nn, nn))
+    y = rng.standard_normal(nn)
+    cores, _ = ttgpu.tt_ksl(1, [nn], [nn], [1, 1], a.ravel(order="F"), y, [1, 1], tau, 10,
+                            ctx=ctx)
+    ref = sla.expm(tau / 2 * a) @ y
+    assert _rel(cores, ref) < 1e-10
+
+
+def test_tt_ksl_real_rejects_ranks_the_qr_would_cut(ctx):
+    import ttgpu
+    from test_ksl import scaled_identity
+    d, nn = 3, 2
+    ra, crA = scaled_identity(d, nn, 1.0)
+    ry = [1, 2, 4, 1]
+    y = np.ones(sum(ry[k] * nn * ry[k + 1] for k in range(d)))
+    with pytest.raises(RuntimeError):
+        ttgpu.tt_ksl(d, [nn] * d, [nn] * d, ra, crA, y, ry, 0.1, 10, ctx=ctx)
+    # the context stays usable
+    ry_ok = [1, 1, 2, 1]
+    y_ok = np.ones(sum(ry_ok[k] * nn * ry_ok[k + 1] for k in range(d)))
+    cores, ry1 = ttgpu.tt_ksl(d, [nn] * d, [nn] * d, ra, crA, y_ok, ry_ok, 0.1, 10, ctx=ctx)
+    x0 = tt_full(d, [nn] * d, ry_ok, y_ok)
+    assert _rel(tt_full(d, [nn] * d, ry1, cores), np.exp(0.1) * x0) < 1e-12

@@ -76,6 +76,9 @@ struct KslParams {
   // diag: the operator is diagonal in the physical index (cores A(a1, i, a2),
   // crA holds those); ztt_diag_ksl, tt_diag_ksl.f90:560-804
   bool diag = false;
+  // real_scheme: the sweep of the real tt_ksl (tt_ksl.f90:191-428) instead
+  // of ztt_ksl's; see run_real_sweep
+  bool real_scheme = false;
 };
 
 // A(a1, i, j, a2) = delta_ij D(a1, i, a2): the diagonal TT-matrix core as a
@@ -322,7 +325,7 @@ static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>
   auto Ld = [&](int i) {
     return LocalDims{ry[i], n[i], ry[i + 1], ry[i], n[i], ry[i + 1], P.ra[i], P.ra[i + 1]};
   };
-  const double tau0 = P.typ == 2 ? P.tau / 2 : P.tau;
+  const double tau0 = P.typ == 2 || P.real_scheme ? P.tau / 2 : P.tau;
 
   for (int step = 0; step < P.nsteps; ++step) {
     // QR sweep, tt_ksl.f90:528-550
@@ -397,11 +400,12 @@ static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>
           };
         };
         mv = build(0);
-        mvT = build(1);
+        if (!P.real_scheme) mvT = build(1);
       }
-      const double anorm = znormest_dev(w, N, 4, mv, &mvT, counter, s, &est);
+      // the real tt_ksl passes dmatvec as its own transpose (tt_ksl.f90:38-45)
+      const double anorm = znormest_dev(w, N, 4, mv, P.real_scheme ? &mv : &mvT, counter, s, &est);
       zexp_mv_dev(w, N, P.order, tau0, cr[i], curcr, eps, anorm, mv, s, &est);
-      if (split) split_matvec_check(s);
+      if (split) split_matvec_check(s, P.real_scheme ? 1 : 2);
     };
     auto sstep = [&](i64 rx1, i64 rx2, i64 ra, i64 ry1, i64 ry2, const double2* ph1,
                      const double2* ph2, const double2* Rin) {
@@ -412,6 +416,83 @@ static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>
       const double anorm = P.diag ? 1.0 : znormest_dev(w, N, 4, mv, nullptr, counter, s, &est);
       zexp_mv_dev(w, N, P.order, -tau0, Rin, Sout, eps, anorm, mv, s, &est);
     };
+    if (P.real_scheme) {
+      // tt_ksl.f90:312-393.  Backward i = d..1: K-step; for i < d the left QR
+      // of the new core and the S-step of R on the bond (i, i+1), core i = Q S;
+      // for i > 1 the right QR pushed into core i-1.  Forward i = 1..d: for
+      // i < d the left QR and S-step first, then the K-step, then the left QR
+      // pushed into core i+1.  tau0 = tau/2 throughout.
+      for (int k = 1; k < d; ++k)
+        TTG_REQUIRE(ry[k] <= n[k] * ry[k + 1],
+                    "tt_ksl: every rank must pass the right-to-left QR unchanged (r_k <= n_k r_{k+1})");
+      // QR of X (ry_i n_i x ry_{i+1}) in place, S-step of R, out = Q S
+      auto left_s = [&](int i, double2* X, double2* out) {
+        const i64 rows = ry[i] * n[i], r2 = ry[i + 1];
+        qr_householder_z((int)rows, (int)r2, X, R, tau_ws, s);
+        phi_left_z(Ld(i), phi[i], A_of(i), X, X, phitmp, scratch, s);
+        sstep(r2, r2, P.ra[i + 1], r2, r2, phitmp, phi[i + 1], R);
+        GemmZ g;
+        g.M = (int)rows; g.N = (int)r2; g.K = (int)r2;
+        g.A = X; g.sAm = 1; g.sAk = rows;
+        g.B = Sout; g.sBk = 1; g.sBn = r2;
+        g.C = out; g.sCm = 1; g.sCn = rows;
+        gemm_z(g, s);
+      };
+      auto copy = [&](double2* dst, const double2* src, i64 count) {
+        TTG_CUDA(cudaMemcpyAsync(dst, src, sizeof(double2) * count, cudaMemcpyDeviceToDevice, s));
+      };
+      // with d = 1 the backward K-step is never stored (crnew(1) is written
+      // only under i < d or i > 1), so one call is the forward half step
+      for (int i = d - 1; i >= 0 && d > 1; --i) {
+        kstep(i);                                          // curcr
+        const double2* cur = curcr;
+        if (i < d - 1) {
+          left_s(i, curcr, t2);
+          cur = t2;
+        }
+        if (i > 0) {
+          const i64 cols = n[i] * ry[i + 1], r1 = ry[i];
+          transpose_z(r1, cols, cur, t1, s);               // cols x r1
+          qr_householder_z((int)cols, (int)r1, t1, R, tau_ws, s);
+          transpose_z(cols, r1, t1, cr[i], s);             // Q^T: r1 x cols
+          transpose_z(r1, r1, R, Rt, s);
+          GemmZ g;   // core_{i-1} = core_{i-1} R^T
+          g.M = (int)(ry[i - 1] * n[i - 1]); g.N = (int)r1; g.K = (int)r1;
+          g.A = cr[i - 1]; g.sAm = 1; g.sAk = ry[i - 1] * n[i - 1];
+          g.B = Rt; g.sBk = 1; g.sBn = r1;
+          g.C = t3; g.sCm = 1; g.sCn = ry[i - 1] * n[i - 1];
+          gemm_z(g, s);
+          copy(cr[i - 1], t3, ry[i - 1] * n[i - 1] * r1);
+          phi_right_z(Ld(i), phi[i + 1], A_of(i), cr[i], cr[i], phi[i], scratch, s);
+        } else {
+          copy(cr[i], cur, Ld(i).xsize());
+        }
+      }
+      for (int i = 0; i < d; ++i) {
+        if (i < d - 1) {
+          left_s(i, cr[i], t2);
+          copy(cr[i], t2, Ld(i).xsize());
+        }
+        kstep(i);                                          // curcr
+        if (i < d - 1) {
+          const i64 rows = ry[i] * n[i], r2 = ry[i + 1];
+          qr_householder_z((int)rows, (int)r2, curcr, R, tau_ws, s);
+          copy(cr[i], curcr, rows * r2);
+          GemmZ g;   // core_{i+1} = R core_{i+1}
+          g.M = (int)r2; g.N = (int)(n[i + 1] * ry[i + 2]); g.K = (int)r2;
+          g.A = R; g.sAm = 1; g.sAk = r2;
+          g.B = cr[i + 1]; g.sBk = 1; g.sBn = r2;
+          g.C = t2; g.sCm = 1; g.sCn = r2;
+          gemm_z(g, s);
+          copy(cr[i + 1], t2, r2 * n[i + 1] * ry[i + 2]);
+          phi_left_z(Ld(i), phi[i], A_of(i), cr[i], cr[i], phi[i + 1], scratch, s);
+        } else {
+          copy(cr[i], curcr, Ld(i).xsize());
+        }
+      }
+      if (P.verb > 0) fprintf(stderr, "tt_ksl: step %d done\n", step + 1);
+      continue;
+    }
     int i = d - 1, dir = -1, swp = 0;
     while (swp < 1) {
       kstep(i);
@@ -483,7 +564,6 @@ static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>
     }
     if (P.verb > 0) fprintf(stderr, "ztt_ksl: step %d done\n", step + 1);
   }
-  (void)t3;
   TTG_CUDA(cudaStreamSynchronize(s));
   i64 tot = 0;
   for (int k = 0; k < d; ++k) tot += ry[k] * n[k] * ry[k + 1];
@@ -503,42 +583,86 @@ static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>
 
 using namespace ttg;
 
+static void ksl_entry(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
+                      const ttg_int* ra, const double2* crA, const double2* crY0, ttg_int* ry,
+                      double tau, int verb, int typ, int order, int method, ttg_int nsteps,
+                      bool real) {
+  TTG_CUDA(cudaSetDevice(ctx->device));
+  TTG_REQUIRE(method == TTG_METHOD_PLAIN || method == TTG_METHOD_SPLIT,
+              "ksl: method must be PLAIN (FP64) or SPLIT (BF16x3 K-step products)");
+  TTG_REQUIRE(typ == 1 || typ == 2, "typ must be 1 (KSL) or 2 (symmetric KSL)");
+  KslParams P;
+  P.d = (int)d;
+  P.n.assign(n, n + d);
+  P.m.assign(m, m + d);
+  P.ra.assign(ra, ra + d + 1);
+  P.ry.assign(ry, ry + d + 1);
+  P.crA = crA;
+  P.crY0 = crY0;
+  P.tau = tau;
+  P.typ = typ;
+  P.order = order > 0 ? order : 8;
+  P.nsteps = nsteps > 0 ? (int)nsteps : 1;
+  P.verb = verb;
+  P.method = method;
+  P.real_scheme = real;
+  long long l0 = g_launches;
+  ExpStats est;
+  std::vector<i64> ry_out;
+  run_ksl(ctx, P, ctx->zresult_core, ry_out, est);
+  for (int k = 0; k <= d; ++k) ry[k] = ry_out[k];
+  ctx->result_core.clear();
+  if (real) {
+    ctx->result_core.resize(ctx->zresult_core.size());
+    for (size_t e = 0; e < ctx->zresult_core.size(); ++e) ctx->result_core[e] = ctx->zresult_core[e].real();
+    ctx->zresult_core.clear();
+  }
+  ctx->stat_matvecs = est.nmult;
+  ctx->stat_sweeps = P.nsteps;
+  ctx->stat_res = 0.0;
+  ctx->stat_launches = g_launches - l0;
+}
+
 extern "C" int ttg_ksl_z(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
                          const ttg_int* ra, const double* crA, const double* crY0, ttg_int* ry,
                          double tau, ttg_int rmax, int verb, int typ, int order, int method,
                          ttg_int nsteps) {
   if (!ctx) return TTG_ERR_ARG;
   try {
-    TTG_CUDA(cudaSetDevice(ctx->device));
     TTG_REQUIRE(d > 0 && n && m && ra && crA && crY0 && ry, "null argument");
-    TTG_REQUIRE(method == TTG_METHOD_PLAIN || method == TTG_METHOD_SPLIT,
-                "ztt_ksl: method must be PLAIN (FP64) or SPLIT (BF16x3 K-step products)");
-    TTG_REQUIRE(typ == 1 || typ == 2, "typ must be 1 (KSL) or 2 (symmetric KSL)");
     (void)rmax;   // read but unused by the reference as well (tt_ksl.f90:446)
-    KslParams P;
-    P.d = (int)d;
-    P.n.assign(n, n + d);
-    P.m.assign(m, m + d);
-    P.ra.assign(ra, ra + d + 1);
-    P.ry.assign(ry, ry + d + 1);
-    P.crA = (const double2*)crA;
-    P.crY0 = (const double2*)crY0;
-    P.tau = tau;
-    P.typ = typ;
-    P.order = order > 0 ? order : 8;
-    P.nsteps = nsteps > 0 ? (int)nsteps : 1;
-    P.verb = verb;
-    P.method = method;
-    long long l0 = g_launches;
-    ExpStats est;
-    std::vector<i64> ry_out;
-    run_ksl(ctx, P, ctx->zresult_core, ry_out, est);
-    for (int k = 0; k <= d; ++k) ry[k] = ry_out[k];
-    ctx->result_core.clear();
-    ctx->stat_matvecs = est.nmult;
-    ctx->stat_sweeps = P.nsteps;
-    ctx->stat_res = 0.0;
-    ctx->stat_launches = g_launches - l0;
+    ksl_entry(ctx, d, n, m, ra, (const double2*)crA, (const double2*)crY0, ry, tau, verb, typ,
+              order, method, nsteps, false);
+  } catch (const ttg::Error& e) {
+    ctx->last_error = e.msg;
+    return e.code;
+  }
+  return TTG_OK;
+}
+
+// tt_ksl (tt_ksl.f90:191-428): real operator and start, the real scheme's
+// sweep, computed in complex arithmetic on real data (the imaginary parts
+// stay zero); the real parts go to the real result.  typ is read but, as in
+// the reference, the scheme is always the symmetric one.
+extern "C" int ttg_ksl_d(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* m,
+                         const ttg_int* ra, const double* crA, const double* crY0, ttg_int* ry,
+                         double tau, ttg_int rmax, int verb, int typ, int order, int method,
+                         ttg_int nsteps) {
+  if (!ctx) return TTG_ERR_ARG;
+  try {
+    TTG_REQUIRE(d > 0 && n && m && ra && crA && crY0 && ry, "null argument");
+    (void)rmax;   // read but unused by the reference as well (tt_ksl.f90:234-245)
+    i64 na = 0, ny = 0;
+    for (ttg_int k = 0; k < d; ++k) {
+      TTG_REQUIRE(n[k] > 0 && m[k] > 0 && ra[k] > 0 && ry[k] > 0, "sizes must be positive");
+      na += ra[k] * n[k] * m[k] * ra[k + 1];
+      ny += ry[k] * n[k] * ry[k + 1];
+    }
+    std::vector<double2> zA(na), zY(ny);
+    for (i64 e = 0; e < na; ++e) zA[e] = make_double2(crA[e], 0.0);
+    for (i64 e = 0; e < ny; ++e) zY[e] = make_double2(crY0[e], 0.0);
+    ksl_entry(ctx, d, n, m, ra, zA.data(), zY.data(), ry, tau, verb, typ, order, method, nsteps,
+              true);
   } catch (const ttg::Error& e) {
     ctx->last_error = e.msg;
     return e.code;

@@ -76,7 +76,7 @@ EXPORTED = [
     "ttg_mlp_train_recorded", "ttg_batch_create", "ttg_batch_destroy", "ttg_batch_add_eigb",
     "ttg_batch_run", "ttg_batch_result", "ttg_batch_cores", "ttg_djac_size", "ttg_djac_gen",
     "ttg_djac_apply", "ttg_mvk4", "ttg_sdv_write", "ttg_sdv_read", "ttg_diag_ksl_z",
-    "ttg_diag_ksl_d",
+    "ttg_diag_ksl_d", "ttg_ksl_d",
 ]
 
 
@@ -201,6 +201,22 @@ def ztt_ksl(d, n, m, ra, crA, crY0, ry, tau, rmax, kickrank=None, nswp=None, ver
                          C.c_int(order), C.c_int(METHOD[method]), _i64(nsteps))
     ctx.check(rc)
     return _result(ctx, real=False), [int(v) for v in ry_]
+
+
+def tt_ksl(d, n, m, ra, crA, crY0, ry, tau, rmax, kickrank=None, nswp=None, verb=0, typ=2,
+           order=8, method="plain", nsteps=1, ctx=None):
+    """KSL time stepping with real data (tt_ksl, tt_ksl.f90:191): the real
+    routine's sweep, ``nsteps`` consecutive steps on the device.  Returns
+    (cores, ry), real."""
+    ctx = ctx or default_context()
+    n_, m_, ra_ = _iarr(n), _iarr(m), _iarr(ra)
+    ry_ = _iarr(ry).copy()
+    A_, Y_ = _darr(crA), _darr(crY0)
+    rc = lib().ttg_ksl_d(ctx.handle, _i64(d), _p(n_), _p(m_), _p(ra_), _p(A_), _p(Y_), _p(ry_),
+                         C.c_double(tau), _i64(rmax), C.c_int(verb), C.c_int(typ),
+                         C.c_int(order), C.c_int(METHOD[method]), _i64(nsteps))
+    ctx.check(rc)
+    return _result(ctx, real=True), [int(v) for v in ry_]
 
 
 def sdv_write(path, n, r, cores, complex_=False):
