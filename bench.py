@@ -380,9 +380,8 @@ def main():
     with ClockSampler() as clk:
         t, tw, launches, (lam, cores, ry_out), st = timed(meth, args.steps)
     if args.gpus > 1:
-        tt = torch.tensor([t, tw], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t, tw = tt.tolist()
+        from ttgpu.replicas import max_over_ranks
+        t, tw = max_over_ranks([t, tw])
     plain = None
     if meth != "plain" and not args.no_plain:
         solve("plain")
