@@ -200,3 +200,20 @@ def test_tt_ksl_real_rejects_ranks_the_qr_would_cut():
     y = np.ones(sum(ry[k] * nn * ry[k + 1] for k in range(d)))
     with pytest.raises(ValueError):
         tt_ksl_real(d, [nn] * d, [nn] * d, ra, crA, y, ry, 0.1, 10)
+
+
+def test_tt_ksl_real_ragged_modes_scaled_identity():
+    """c I on ragged modes, with a start rank the first QR cuts: still
+    exp(c tau) times the start."""
+    from oracle.ksl import tt_ksl_real
+    n, c, tau = [2, 3, 4, 2], -0.4, 0.25
+    cores = [np.eye(nk).reshape(1, nk, nk, 1) * (c if k == 0 else 1.0) for k, nk in enumerate(n)]
+    crA = np.concatenate([x.ravel(order="F") for x in cores])
+    ry = [1, 4, 3, 2, 1]
+    rng = np.random.default_rng(12)
+    y = np.concatenate([rng.standard_normal(ry[k] * n[k] * ry[k + 1]) for k in range(4)])
+    out = tt_ksl_real(4, n, n, [1] * 5, crA, y, ry, tau, 10)
+    assert out["ry"] == [1, 2, 3, 2, 1]
+    x0 = tt_full(4, n, ry, y)
+    x1 = tt_full(4, n, out["ry"], out["cores"])
+    assert np.linalg.norm(x1 - np.exp(c * tau) * x0) <= 1e-12 * np.linalg.norm(x0)

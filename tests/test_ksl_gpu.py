@@ -243,3 +243,31 @@ def test_tt_ksl_real_rejects_ranks_the_qr_would_cut(ctx):
     cores, ry1 = ttgpu.tt_ksl(d, [nn] * d, [nn] * d, ra, crA, y_ok, ry_ok, 0.1, 10, ctx=ctx)
     x0 = tt_full(d, [nn] * d, ry_ok, y_ok)
     assert _rel(tt_full(d, [nn] * d, ry1, cores), np.exp(0.1) * x0) < 1e-12
+
+
+def _ragged_operator(seed):
+    """Real TT-matrix with ragged mode sizes n = [2, 3, 4, 2] and ranks
+    [1, 2, 3, 2, 1], N(0, 0.3^2) entries."""
+    rng = np.random.default_rng(seed)
+    n, ra = [2, 3, 4, 2], [1, 2, 3, 2, 1]
+    crA = np.concatenate([0.3 * rng.standard_normal(ra[k] * n[k] * n[k] * ra[k + 1])
+                          for k in range(4)])
+    return n, ra, crA
+
+
+def test_tt_ksl_real_ragged_modes_and_rank_cut(ctx):
+    """Ragged modes, and a start whose first rank (4) is above what core 1
+    allows (2): the left-to-right QR cuts it, on the GPU as in the oracle."""
+    import ttgpu
+    from oracle.ksl import tt_ksl_real
+    n, ra, crA = _ragged_operator(11)
+    ry = [1, 4, 3, 2, 1]
+    rng = np.random.default_rng(12)
+    y = np.concatenate([rng.standard_normal(ry[k] * n[k] * ry[k + 1]) for k in range(4)])
+    cores, ry1 = ttgpu.tt_ksl(4, n, n, ra, crA, y, ry, 0.05, 10, nsteps=2, ctx=ctx)
+    c, rr = y, list(ry)
+    for _ in range(2):
+        out = tt_ksl_real(4, n, n, ra, crA, c, rr, 0.05, 10)
+        c, rr = out["cores"], out["ry"]
+    assert ry1 == rr == [1, 2, 3, 2, 1]
+    assert _rel(tt_full(4, n, ry1, cores), tt_full(4, n, rr, c)) < 1e-8
