@@ -47,3 +47,15 @@ def test_version_and_null_context(lib):
     # every entry point rejects a null context with TTG_ERR_ARG, never crashes
     assert lib.ttg_synchronize(C.c_void_p()) == -1
     assert lib.ttg_free_result(C.c_void_p()) == -1
+
+
+def test_real_entry_points_refuse_complex_arrays(lib):
+    """A real entry point given complex data raises instead of dropping the
+    imaginary parts (the array check runs before any device work)."""
+    import ttgpu
+    assert ttgpu._darr([1, 2.5]).dtype == np.float64
+    assert ttgpu._darr(np.arange(3, dtype=np.float32)).flags["C_CONTIGUOUS"]
+    with pytest.raises(TypeError):
+        ttgpu._darr(np.array([1.0 + 0.5j]))
+    with pytest.raises(TypeError):
+        ttgpu._darr(np.zeros(2, dtype=np.complex128))

@@ -149,7 +149,12 @@ def _iarr(v):
 
 
 def _darr(v):
-    return np.ascontiguousarray(np.asarray(v, dtype=np.float64))
+    """float64 copy of a real array; complex input is an error (a real entry
+    point would otherwise drop the imaginary parts)."""
+    a = np.asarray(v)
+    if np.iscomplexobj(a):
+        raise TypeError("this entry point takes real arrays; use the complex one (z...) instead")
+    return np.ascontiguousarray(a, dtype=np.float64)
 
 
 def _carr(v):
