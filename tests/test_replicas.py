@@ -2,6 +2,7 @@
 result gather, the max-over-ranks timing and failure reporting, run as two
 ``gloo`` ranks.  The per-chain solver here is a dense eigensolver of small
 chains (no GPU); the library's GPU solvers plug into the same hooks."""
+import datetime
 import os
 import socket
 
@@ -73,7 +74,10 @@ def _worker(rank, world, port, mode, outdir):
     os.environ["MASTER_PORT"] = str(port)
     if mode == "fail":
         os.environ["TTG_TEST_FAIL_JOB"] = "5"
-    dist.init_process_group("gloo", rank=rank, world_size=world)
+    # a short process-group timeout: a rank that never arrives fails the
+    # collective (and the test) instead of hanging it
+    dist.init_process_group("gloo", rank=rank, world_size=world,
+                            timeout=datetime.timedelta(seconds=60))
     try:
         jobs = _jobs(11, 2)
         costs = [float(j[1].shape[0]) ** 3 for j in jobs]
