@@ -61,3 +61,84 @@ def test_rejects_files_that_are_not_tt(tmp_path):
         ttgpu.sdv_read(path)
     with pytest.raises(RuntimeError):
         ttgpu.sdv_read(tmp_path / "missing.sdv")
+
+
+def _good_file(tmp_path, complex_=False):
+    import ttgpu
+    rng = np.random.default_rng(3)
+    n, r = [2, 3, 2], [1, 2, 2, 1]
+    size = sum(r[k] * n[k] * r[k + 1] for k in range(3))
+    cores = rng.standard_normal(size) + (1j * rng.standard_normal(size) if complex_ else 0)
+    path = tmp_path / "good.sdv"
+    ttgpu.sdv_write(path, n, r, cores, complex_=complex_)
+    return path, n, r, cores
+
+
+def test_rejects_corrupted_headers_and_bodies(tmp_path):
+    """Corrupted .sdv files are errors, never partial reads: wrong magic,
+    wrong version, truncated header, a mode or rank record that is zero or
+    negative, a first mode after the last, and a body shorter than the ranks
+    say."""
+    import struct
+    import ttgpu
+    path, n, r, cores = _good_file(tmp_path)
+    raw = path.read_bytes()
+    ttgpu.sdv_read(path)                                        # the intact file reads
+
+    def bad(data, name):
+        p = tmp_path / name
+        p.write_bytes(data)
+        with pytest.raises(RuntimeError):
+            ttgpu.sdv_read(p)
+
+    bad(b"TX" + raw[2:], "magic.sdv")
+    bad(raw[:8] + struct.pack("<i", 2) + raw[12:], "version.sdv")
+    bad(raw[:100], "short_header.sdv")
+    bad(raw[:128] + struct.pack("<ii", 3, 1) + raw[136:], "l_after_m.sdv")
+    off_n = 128 + 8                                             # n(1:d), then r(0:d)
+    bad(raw[:off_n] + struct.pack("<i", 0) + raw[off_n + 4:], "zero_mode.sdv")
+    off_r = off_n + 4 * len(n)
+    bad(raw[:off_r + 4] + struct.pack("<i", -2) + raw[off_r + 8:], "negative_rank.sdv")
+    bad(raw[:-8], "short_body.sdv")
+    bad(raw[:off_r], "no_ranks.sdv")
+
+
+def test_complex_file_read_as_real_is_short(tmp_path):
+    """The file does not say whether it holds float64 or complex128 cores; a
+    real file read as complex runs out of body and is an error."""
+    import ttgpu
+    path, n, r, cores = _good_file(tmp_path, complex_=False)
+    with pytest.raises(RuntimeError):
+        ttgpu.sdv_read(path, complex_=True)
+    n1, r1, c1 = ttgpu.sdv_read(path, complex_=False)
+    assert np.array_equal(c1, cores)
+
+
+def test_writer_rejects_bad_sizes(tmp_path):
+    import ctypes as C
+    import ttgpu
+    with pytest.raises(ValueError):
+        ttgpu.sdv_write(tmp_path / "a.sdv", [2, 0], [1, 1, 1], np.zeros(2))
+    with pytest.raises(ValueError):
+        ttgpu.sdv_write(tmp_path / "b.sdv", [2, 2], [1, -1, 1], np.zeros(4))
+    with pytest.raises(RuntimeError):
+        ttgpu.sdv_write(tmp_path / "no_such_dir" / "c.sdv", [2], [1, 1], np.zeros(2))
+    # the C entry point checks the same itself
+    lib = ttgpu.lib()
+    buf = np.zeros(4)
+    n0, r0 = np.array([2, 0], dtype=np.int64), np.array([1, 1, 1], dtype=np.int64)
+    path = str(tmp_path / "d.sdv").encode()
+    assert lib.ttg_sdv_write(path, C.c_int64(2), n0.ctypes.data_as(C.c_void_p),
+                             r0.ctypes.data_as(C.c_void_p), buf.ctypes.data_as(C.c_void_p),
+                             C.c_int(0)) != 0
+    assert lib.ttg_sdv_write(path, C.c_int64(0), n0.ctypes.data_as(C.c_void_p),
+                             r0.ctypes.data_as(C.c_void_p), buf.ctypes.data_as(C.c_void_p),
+                             C.c_int(0)) != 0
+
+
+def test_writer_checks_the_core_count_against_the_ranks(tmp_path):
+    import ttgpu
+    with pytest.raises(ValueError):
+        ttgpu.sdv_write(tmp_path / "d.sdv", [2, 2], [1, 2, 1], np.zeros(7))
+    with pytest.raises(ValueError):
+        ttgpu.sdv_write(tmp_path / "e.sdv", [2, 2], [1, 2], np.zeros(8))

@@ -229,6 +229,13 @@ def sdv_write(path, n, r, cores, complex_=False):
     ttio.f90:29-192); cores flat, column-major, float64 or complex128."""
     n_, r_ = _iarr(n), _iarr(r)
     c = np.ascontiguousarray(cores, dtype=np.complex128 if complex_ else np.float64)
+    if len(r_) != len(n_) + 1:
+        raise ValueError("sdv_write: r needs len(n) + 1 entries")
+    if len(n_) < 1 or (n_ < 1).any() or (r_ < 1).any():
+        raise ValueError("sdv_write: mode sizes and ranks must be positive")
+    need = sum(int(r_[k]) * int(n_[k]) * int(r_[k + 1]) for k in range(len(n_)))
+    if c.size != need:
+        raise ValueError(f"sdv_write: {c.size} core entries, the ranks need {need}")
     rc = lib().ttg_sdv_write(str(path).encode(), _i64(len(n_)), _p(n_), _p(r_),
                              c.ctypes.data_as(C.c_void_p), C.c_int(1 if complex_ else 0))
     if rc != 0:
