@@ -59,3 +59,31 @@ def test_real_entry_points_refuse_complex_arrays(lib):
         ttgpu._darr(np.array([1.0 + 0.5j]))
     with pytest.raises(TypeError):
         ttgpu._darr(np.zeros(2, dtype=np.complex128))
+
+
+def test_driver_wrappers_check_array_sizes_before_any_device_work(lib):
+    """The C drivers take bare pointers; the Python mirror rejects arrays
+    shorter than their sizes say (TTG_ERR_ARG), before a context exists."""
+    import ttgpu
+    from ttgpu.operators import xxz_mpo, random_tt
+    d, B = 6, 2
+    n, m, ra, crA = xxz_mpo(d)
+    _, ry, cr = random_tt(d, 2, 4, last=B, seed=1)
+    cases = [
+        lambda: ttgpu.tt_eigb(d, n, m, ra, crA[:-1], cr, ry, 1e-8, 16, B),
+        lambda: ttgpu.tt_eigb(d, n, m, ra, crA, cr[:-3], ry, 1e-8, 16, B),
+        lambda: ttgpu.tt_eigb(d, n[:-1], m, ra, crA, cr, ry, 1e-8, 16, B),
+        lambda: ttgpu.tt_eigb(0, n, m, ra, crA, cr, ry, 1e-8, 16, B),
+        lambda: ttgpu.ztt_ksl(d, n, m, ra, crA, cr[:5].astype(complex), [1] + [4] * (d - 1) + [1],
+                              1e-3, 16),
+        lambda: ttgpu.tt_ksl(d, n, m, ra[:-1], crA, cr, ry, 1e-3, 16),
+        lambda: ttgpu.tt_mvk4(d, n, m, ry, ra, crA, cr[:10], cr, ry, 1e-8, 16),
+        lambda: ttgpu.dtt_amen_solve(d, n, m, ry, ra, crA, cr, cr[:7], ry, 1e-8),
+        lambda: ttgpu.tt_amen_solve(d, n, m, ry, ra, crA, cr[:7], cr, ry, 1e-8),
+        lambda: ttgpu.tt_diag_ksl(d, n, [1] * (d + 1), np.ones(2 * d - 1), np.ones(2 * d),
+                                  [1] * (d + 1), 1e-3, 16),
+    ]
+    for k, call in enumerate(cases):
+        with pytest.raises(ttgpu.TTGError) as e:
+            call()
+        assert e.value.code == ttgpu.TTG_ERR_ARG, k

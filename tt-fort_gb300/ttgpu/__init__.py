@@ -24,6 +24,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libttgpu.so")
 
 TTG_OK = 0
+TTG_ERR_ARG = -1
 TTG_ERR_UNSUPPORTED = -7
 METHOD = {"plain": 0, "split": 1}
 
@@ -174,6 +175,37 @@ def _dev(t):
     return C.c_void_p(t.data_ptr())
 
 
+def _tt_len(d, r, n, m=None):
+    """Entries of packed TT cores r[k] x n[k] (x m[k]) x r[k+1], k < d."""
+    return sum(int(r[k]) * int(n[k]) * (int(m[k]) if m is not None else 1) * int(r[k + 1])
+               for k in range(d))
+
+
+def _check_sizes(name, d, modes, ranks, arrays):
+    """Host-side checks before a driver call: the C entry points take bare
+    pointers (as the reference's assumed-size arrays), so a short array
+    would be read past its end.  modes/ranks: {label: array} that need d
+    resp. d + 1 entries; arrays: (label, array, r, n[, m]), the array holding
+    packed cores r[k] x n[k] (x m[k]) x r[k+1].  Failures
+    raise TTGError with TTG_ERR_ARG, the code the library returns for its own
+    argument checks."""
+    d = int(d)
+    if d < 1:
+        raise TTGError(TTG_ERR_ARG, f"{name}: d must be >= 1")
+    for label, a in modes.items():
+        if len(a) < d:
+            raise TTGError(TTG_ERR_ARG, f"{name}: {label} has {len(a)} entries, d = {d} needed")
+    for label, a in ranks.items():
+        if len(a) < d + 1:
+            raise TTGError(TTG_ERR_ARG,
+                           f"{name}: {label} has {len(a)} entries, d + 1 = {d + 1} needed")
+    for label, a, *dims in arrays:
+        need = _tt_len(d, *dims)
+        if a.size < need:
+            raise TTGError(TTG_ERR_ARG,
+                           f"{name}: {label} has {a.size} entries, the sizes need {need}")
+
+
 # ------------------------------------------------------------------ drivers
 def tt_eigb(d, n, m, ra, crA, crY0, ry, eps, rmax, B, kickrank=None, nswp=20,
             max_full_size=2000, verb=0, method="plain", ctx=None):
@@ -181,10 +213,12 @@ def tt_eigb(d, n, m, ra, crA, crY0, ry, eps, rmax, B, kickrank=None, nswp=20,
 
     ``kickrank`` is accepted and ignored, as in the reference (unused there).
     """
-    ctx = ctx or default_context()
     n_, m_, ra_ = _iarr(n), _iarr(m), _iarr(ra)
     ry_ = _iarr(ry).copy()
     A_, Y_ = _darr(crA), _darr(crY0)
+    _check_sizes("tt_eigb", d, {"n": n_, "m": m_}, {"ra": ra_, "ry": ry_},
+                 [("crA", A_, ra_, n_, m_), ("crY0", Y_, ry_, n_)])
+    ctx = ctx or default_context()
     lam = np.zeros(int(B))
     rc = lib().ttg_eigb(ctx.handle, _i64(d), _p(n_), _p(m_), _p(ra_), _p(A_), _p(Y_), _p(ry_),
                         C.c_double(eps), _i64(rmax), _p(lam), _i64(B), _i64(nswp),
@@ -197,10 +231,12 @@ def ztt_ksl(d, n, m, ra, crA, crY0, ry, tau, rmax, kickrank=None, nswp=None, ver
             order=8, method="plain", nsteps=1, ctx=None):
     """KSL time stepping (ztt_ksl, tt_ksl.f90:431): ``nsteps`` consecutive
     steps of size tau on the device.  Returns (cores, ry)."""
-    ctx = ctx or default_context()
     n_, m_, ra_ = _iarr(n), _iarr(m), _iarr(ra)
     ry_ = _iarr(ry).copy()
     A_, Y_ = _carr(crA), _carr(crY0)
+    _check_sizes("ztt_ksl", d, {"n": n_, "m": m_}, {"ra": ra_, "ry": ry_},
+                 [("crA", A_, ra_, n_, m_), ("crY0", Y_, ry_, n_)])
+    ctx = ctx or default_context()
     rc = lib().ttg_ksl_z(ctx.handle, _i64(d), _p(n_), _p(m_), _p(ra_), _p(A_), _p(Y_), _p(ry_),
                          C.c_double(tau), _i64(rmax), C.c_int(verb), C.c_int(typ),
                          C.c_int(order), C.c_int(METHOD[method]), _i64(nsteps))
@@ -213,10 +249,12 @@ def tt_ksl(d, n, m, ra, crA, crY0, ry, tau, rmax, kickrank=None, nswp=None, verb
     """KSL time stepping with real data (tt_ksl, tt_ksl.f90:191): the real
     routine's sweep, ``nsteps`` consecutive steps on the device.  Returns
     (cores, ry), real."""
-    ctx = ctx or default_context()
     n_, m_, ra_ = _iarr(n), _iarr(m), _iarr(ra)
     ry_ = _iarr(ry).copy()
     A_, Y_ = _darr(crA), _darr(crY0)
+    _check_sizes("tt_ksl", d, {"n": n_, "m": m_}, {"ra": ra_, "ry": ry_},
+                 [("crA", A_, ra_, n_, m_), ("crY0", Y_, ry_, n_)])
+    ctx = ctx or default_context()
     rc = lib().ttg_ksl_d(ctx.handle, _i64(d), _p(n_), _p(m_), _p(ra_), _p(A_), _p(Y_), _p(ry_),
                          C.c_double(tau), _i64(rmax), C.c_int(verb), C.c_int(typ),
                          C.c_int(order), C.c_int(METHOD[method]), _i64(nsteps))
@@ -263,10 +301,13 @@ def sdv_read(path, complex_=False):
 def tt_mvk4(d, n, m, rx, ra, crA, crX, crY0, ry, eps, rmax, kickrank=5, nswp=20, verb=0,
             ctx=None):
     """AMEn matvec y ~ A x (tt_mvk4, tt_adapt_als.f90:67).  Returns (cores, ry)."""
-    ctx = ctx or default_context()
     n_, m_, rx_, ra_ = _iarr(n), _iarr(m), _iarr(rx), _iarr(ra)
     ry_ = _iarr(ry).copy()
     A_, X_, Y_ = _darr(crA), _darr(crX), _darr(crY0)
+    _check_sizes("tt_mvk4", d, {"n": n_, "m": m_}, {"rx": rx_, "ra": ra_, "ry": ry_},
+                 [("crA", A_, ra_, n_, m_), ("crX", X_, rx_, m_),
+                  ("crY0", Y_, ry_, n_)])
+    ctx = ctx or default_context()
     rc = lib().ttg_mvk4(ctx.handle, _i64(d), _p(n_), _p(m_), _p(rx_), _p(ra_), _p(A_), _p(X_),
                         _p(Y_), _p(ry_), C.c_double(eps), _i64(rmax), _i64(kickrank), _i64(nswp),
                         C.c_int(verb))
@@ -279,11 +320,13 @@ def tt_diag_ksl(d, n, ra, crA, crY0, ry, tau, rmax, verb=0, typ=2, order=8, nste
     """KSL for an operator diagonal in the physical index (ztt_diag_ksl /
     dtt_diag_ksl, tt_diag_ksl.f90:315,560): crA holds cores A(a1, i, a2).
     Complex inputs run ztt_diag_ksl, real ones dtt_diag_ksl.  Returns (cores, ry)."""
-    ctx = ctx or default_context()
     cplx = np.iscomplexobj(crA) or np.iscomplexobj(crY0)
     n_, ra_ = _iarr(n), _iarr(ra)
     ry_ = _iarr(ry).copy()
     A_, Y_ = (_carr(crA), _carr(crY0)) if cplx else (_darr(crA), _darr(crY0))
+    _check_sizes("tt_diag_ksl", d, {"n": n_}, {"ra": ra_, "ry": ry_},
+                 [("crA", A_, ra_, n_), ("crY0", Y_, ry_, n_)])
+    ctx = ctx or default_context()
     f = lib().ttg_diag_ksl_z if cplx else lib().ttg_diag_ksl_d
     rc = f(ctx.handle, _i64(d), _p(n_), _p(ra_), _p(A_), _p(Y_), _p(ry_), C.c_double(tau),
            _i64(rmax), C.c_int(verb), C.c_int(typ), C.c_int(order), _i64(nsteps))
@@ -294,10 +337,13 @@ def tt_diag_ksl(d, n, ra, crA, crY0, ry, tau, rmax, verb=0, typ=2, order=8, nste
 def tt_amen_solve(d, n, m, ry, ra, crA, crY, crX0, rx, eps, kickrank=4, nswp=20, verb=0,
                   prec="n", nrestart=40, niters=2, rmax=0, method="plain", ctx=None):
     """AMEn solve A x = y (tt_amen_solve, tt_adapt_als.f90:513).  Returns (cores, rx)."""
-    ctx = ctx or default_context()
     n_, m_, ry_, ra_ = _iarr(n), _iarr(m), _iarr(ry), _iarr(ra)
     rx_ = _iarr(rx).copy()
     A_, Y_, X_ = _darr(crA), _darr(crY), _darr(crX0)
+    _check_sizes("tt_amen_solve", d, {"n": n_, "m": m_}, {"ry": ry_, "ra": ra_, "rx": rx_},
+                 [("crA", A_, ra_, n_, m_), ("crY", Y_, ry_, n_),
+                  ("crX0", X_, rx_, m_)])
+    ctx = ctx or default_context()
     rc = lib().ttg_amen_solve(ctx.handle, _i64(d), _p(n_), _p(m_), _p(ry_), _p(ra_), _p(A_),
                               _p(Y_), _p(X_), _p(rx_), C.c_double(eps), _i64(kickrank),
                               _i64(nswp), C.c_int(verb), C.c_char(prec.encode()),
@@ -310,10 +356,13 @@ def dtt_amen_solve(d, n, m, ry, ra, crA, crY, crX0, rx, eps, rmax=1000, kickrank
                    verb=0, method="plain", ctx=None):
     """AMEn solve of ttamen.f90 (dtt_amen_solve, ttamen.f90:29) on packed cores.
     Returns (cores, rx)."""
-    ctx = ctx or default_context()
     n_, m_, ry_, ra_ = _iarr(n), _iarr(m), _iarr(ry), _iarr(ra)
     rx_ = _iarr(rx).copy()
     A_, Y_, X_ = _darr(crA), _darr(crY), _darr(crX0)
+    _check_sizes("dtt_amen_solve", d, {"n": n_, "m": m_}, {"ry": ry_, "ra": ra_, "rx": rx_},
+                 [("crA", A_, ra_, n_, m_), ("crY", Y_, ry_, n_),
+                  ("crX0", X_, rx_, m_)])
+    ctx = ctx or default_context()
     rc = lib().ttg_dtt_amen_solve(ctx.handle, _i64(d), _p(n_), _p(m_), _p(ry_), _p(ra_), _p(A_),
                                   _p(Y_), _p(X_), _p(rx_), C.c_double(eps), _i64(rmax),
                                   _i64(kickrank), _i64(nswp), C.c_int(verb),
@@ -577,6 +626,8 @@ class EigbBatch:
             method="plain"):
         n_, m_, ra_, ry_ = _iarr(n), _iarr(m), _iarr(ra), _iarr(ry)
         A_, Y_ = _darr(crA), _darr(crY0)
+        _check_sizes("EigbBatch.add", d, {"n": n_, "m": m_}, {"ra": ra_, "ry": ry_},
+                     [("crA", A_, ra_, n_, m_), ("crY0", Y_, ry_, n_)])
         idx = _i64()
         self.ctx.check(lib().ttg_batch_add_eigb(self._h, _i64(d), _p(n_), _p(m_), _p(ra_), _p(A_),
                                                 _p(Y_), _p(ry_), C.c_double(eps), _i64(rmax),
