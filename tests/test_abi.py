@@ -87,3 +87,123 @@ def test_driver_wrappers_check_array_sizes_before_any_device_work(lib):
         with pytest.raises(ttgpu.TTGError) as e:
             call()
         assert e.value.code == ttgpu.TTG_ERR_ARG, k
+
+
+class _FakeDev:
+    """Stands in for a contiguous torch CUDA tensor: only what the pointer
+    checks read."""
+    is_cuda = True
+
+    def __init__(self, n, dtype="float64"):
+        self.n, self.dtype = int(n), "torch." + dtype
+
+    def is_contiguous(self):
+        return True
+
+    def numel(self):
+        return self.n
+
+    def data_ptr(self):
+        return 0
+
+
+class _StubCtx:
+    handle = None
+
+    def bind_torch_stream(self):
+        pass
+
+    def check(self, rc):
+        assert rc == 0
+
+
+def test_kernel_wrappers_check_tensor_sizes_and_types(monkeypatch):
+    """Every kernel-level wrapper accepts tensors of exactly the sizes its
+    GPU tests allocate, and rejects one element fewer (TTG_ERR_ARG) or the
+    wrong element type (TypeError) before the library is called."""
+    import ttgpu
+
+    real = ttgpu.lib()
+
+    class _Lib:
+        def __getattr__(self, name):
+            if name == "ttg_djac_size":            # host-side, no device work
+                return real.ttg_djac_size
+            return lambda *a: 0
+
+    monkeypatch.setattr(ttgpu, "lib", lambda: _Lib())
+    ctx = _StubCtx()
+    F = _FakeDev
+    rx1, m, rx2, ry1, n, ry2, ra1, ra2, nv = 7, 3, 11, 5, 2, 9, 2, 3, 2
+    sizes = dict(phi1=ry1 * rx1 * ra1, A=ra1 * n * m * ra2, phi2=rx2 * ra2 * ry2,
+                 x=rx1 * m * rx2 * nv, y=ry1 * n * ry2 * nv)
+    dims = (rx1, m, rx2, ry1, n, ry2, ra1, ra2)
+
+    def calls(sz, dt="float64", ct="complex128"):
+        f = lambda k: F(sz[k], dt)  # noqa: E731
+        z = lambda k: F(sz[k], ct)  # noqa: E731
+        return [
+            lambda: ttgpu.dbfun3(*dims, f("phi1"), f("A"), f("phi2"), f("x"), f("y"), nvec=nv,
+                                 ctx=ctx),
+            lambda: ttgpu.zbfun3(*dims, z("phi1"), z("A"), z("phi2"), z("x"), z("y"), nvec=nv,
+                                 ctx=ctx),
+            lambda: ttgpu.zbfun3(*dims, z("phi1"), z("A"), z("phi2"), z("y"), z("x"), nvec=nv,
+                                 transp=True, ctx=ctx),
+        ]
+
+    for call in calls(sizes):
+        call()
+    for key in sizes:
+        short = dict(sizes)
+        short[key] -= 1
+        for call in calls(short):
+            with pytest.raises(ttgpu.TTGError):
+                call()
+    with pytest.raises(TypeError):
+        calls(sizes, dt="float32")[0]()
+    with pytest.raises(TypeError):
+        calls(sizes, ct="float64")[1]()
+
+    # interface updates, dense algebra, maxvol, block-Jacobi, prepared operator
+    px, py = rx1 * m * rx2, ry1 * n * ry2
+    ok = [
+        lambda s: ttgpu.phi_left(*dims, F(ry1 * rx1 * ra1 - s), F(sizes["A"]), F(px), F(py),
+                                 F(ry2 * rx2 * ra2), ctx=ctx),
+        lambda s: ttgpu.phi_right(*dims, F(rx2 * ra2 * ry2), F(sizes["A"]), F(px), F(py),
+                                  F(rx1 * ra1 * ry1 - s), ctx=ctx),
+        lambda s: ttgpu.phi_left(*dims, F(ry1 * rx1 * ra1, "complex128"),
+                                 F(sizes["A"], "complex128"), F(px - s, "complex128"),
+                                 F(py, "complex128"), F(ry2 * rx2 * ra2, "complex128"),
+                                 complex_=True, ctx=ctx),
+        lambda s: ttgpu.phi2_left(6, 5, 4, 3, 7, F(4 * 6), F(6 * 3 * 5), F(4 * 3 * 7),
+                                  F(7 * 5 - s), ctx=ctx),
+        lambda s: ttgpu.phi2_right(6, 5, 4, 3, 7, F(5 * 7), F(6 * 3 * 5 - s), F(4 * 3 * 7),
+                                   F(6 * 4), ctx=ctx),
+        lambda s: ttgpu.fullmat(4, 2, 5, 3, 4, F(4 * 4 * 3), F(3 * 2 * 2 * 4), F(5 * 4 * 5),
+                                F(40 * 40 - s), ctx=ctx),
+        lambda s: ttgpu.dqr(300, 7, F(2100), F(7 * 7 - s), ctx=ctx),
+        lambda s: ttgpu.dqr(64, 128, F(64 * 128 - s), F(64 * 128), ctx=ctx),
+        lambda s: ttgpu.dqr(40, 9, F(360, "complex128"), F(81 - s, "complex128"),
+                            complex_=True, ctx=ctx),
+        lambda s: ttgpu.dsyev(17, F(289 - s), F(17), ctx=ctx),
+        lambda s: ttgpu.dgesvd(7, 3, F(21), F(21), F(3), F(9 - s), ctx=ctx),
+        lambda s: ttgpu.dgesvd(3, 7, F(21), F(9 - s), F(3), F(21), ctx=ctx),
+        lambda s: ttgpu.dmaxvol(50, 5, F(250), F(5 - s, "int64"), F(250), ctx=ctx),
+        lambda s: ttgpu.dmaxvol(3, 4, F(12 - s), F(4, "int64"), ctx=ctx),
+        lambda s: ttgpu.djac_gen("l", 3, 4, 2, 2, 3, F(18), F(96), F(12),
+                                 F(ttgpu.djac_size("l", 3, 4, 2) - s), ctx=ctx),
+        lambda s: ttgpu.djac_apply("r", 3, 4, 2, F(ttgpu.djac_size("r", 3, 4, 2)), F(24),
+                                   F(24 - s), ctx=ctx),
+    ]
+    for k, call in enumerate(ok):
+        call(0)
+        with pytest.raises(ttgpu.TTGError):
+            call(1)
+    op = ttgpu.LocalOp(24, 2, 40, 24, 2, 40, 5, 4, F(24 * 24 * 5), F(5 * 2 * 2 * 4),
+                       F(40 * 4 * 40), nvec_max=4, ctx=ctx)
+    op.apply(F(24 * 2 * 40 * 3), F(24 * 2 * 40 * 3), 3)
+    with pytest.raises(ttgpu.TTGError):
+        op.apply(F(24 * 2 * 40 * 3), F(24 * 2 * 40 * 3 - 1), 3)
+    op._h = None
+    with pytest.raises(TypeError):
+        ttgpu.dmaxvol(50, 5, F(250), F(5, "int32"), ctx=ctx)

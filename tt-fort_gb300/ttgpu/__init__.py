@@ -166,13 +166,34 @@ def _p(a):
     return a.ctypes.data_as(C.c_void_p)
 
 
-def _dev(t):
-    """Device pointer of a torch CUDA tensor (contiguous)."""
+def _dev(t, need=0, dtype=None, what="tensor"):
+    """Device pointer of a torch CUDA tensor (contiguous).  With ``dtype``
+    ("float64", "complex128", "int64") the element type is checked, and
+    ``need`` is the least number of elements the call reads or writes: the
+    kernels take bare pointers, so a short tensor is an argument error
+    (TTG_ERR_ARG) here rather than an out-of-bounds access on the device."""
     if not getattr(t, "is_cuda", False):
         raise TypeError("kernel-level calls take torch CUDA tensors")
     if not t.is_contiguous():
         raise ValueError("tensor must be contiguous")
+    if dtype is not None and str(t.dtype) != "torch." + dtype:
+        raise TypeError(f"{what}: {t.dtype}, torch.{dtype} expected")
+    if t.numel() < int(need):
+        raise TTGError(TTG_ERR_ARG, f"{what}: {t.numel()} elements, the sizes need {int(need)}")
     return C.c_void_p(t.data_ptr())
+
+
+def _bfun3_ptrs(dims, phi1, A, phi2, x, y, nvec, dtype, transp=False):
+    """Checked pointers of a local product y = Phi1 A Phi2 x: phi1 (ry1, rx1,
+    ra1), A (ra1, n, m, ra2), phi2 (rx2, ra2, ry2), x (rx1, m, rx2) and y
+    (ry1, n, ry2) per vector; the adjoint swaps the shapes of x and y."""
+    rx1, m, rx2, ry1, n, ry2, ra1, ra2 = (int(v) for v in dims)
+    nx, ny = rx1 * m * rx2 * int(nvec), ry1 * n * ry2 * int(nvec)
+    if transp:
+        nx, ny = ny, nx
+    return (_dev(phi1, ry1 * rx1 * ra1, dtype, "phi1"), _dev(A, ra1 * n * m * ra2, dtype, "A"),
+            _dev(phi2, rx2 * ra2 * ry2, dtype, "phi2"), _dev(x, nx, dtype, "x"),
+            _dev(y, ny, dtype, "y"))
 
 
 def _tt_len(d, r, n, m=None):
@@ -403,10 +424,11 @@ def _kctx(ctx):
 def dbfun3(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1, A, phi2, x, y, nvec=1, split=False,
            ctx=None):
     """y = Phi1 A Phi2 x on the device (dbfun3, ttals.f90:9); torch CUDA tensors."""
+    dims = (rx1, m, rx2, ry1, n, ry2, ra1, ra2)
+    ptrs = _bfun3_ptrs(dims, phi1, A, phi2, x, y, nvec, "float64")
     ctx = _kctx(ctx)
     f = lib().ttg_dbfun3_split if split else lib().ttg_dbfun3
-    ctx.check(f(ctx.handle, *_dims(rx1, m, rx2, ry1, n, ry2, ra1, ra2), _dev(phi1), _dev(A),
-                _dev(phi2), _dev(x), _dev(y), _i64(nvec)))
+    ctx.check(f(ctx.handle, *_dims(*dims), *ptrs, _i64(nvec)))
 
 
 def djac_size(ptype, rx1, n, rx2):
@@ -417,83 +439,110 @@ def djac_size(ptype, rx1, n, rx2):
 def djac_gen(ptype, rx1, n, rx2, ra1, ra2, phi1, A, phi2, jacs, ctx=None):
     """Block-Jacobi blocks of the local system into jacs (djac_gen,
     tt_linalg.f90:363-494); torch CUDA tensors."""
+    ptrs = (_dev(phi1, rx1 * rx1 * ra1, "float64", "phi1"),
+            _dev(A, ra1 * n * n * ra2, "float64", "A"),
+            _dev(phi2, rx2 * ra2 * rx2, "float64", "phi2"),
+            _dev(jacs, max(0, djac_size(ptype, rx1, n, rx2)), "float64", "jacs"))
     ctx = _kctx(ctx)
     ctx.check(lib().ttg_djac_gen(ctx.handle, C.c_char(ptype.encode()), _i64(rx1), _i64(n),
-                                 _i64(rx2), _i64(ra1), _i64(ra2), _dev(phi1), _dev(A), _dev(phi2),
-                                 _dev(jacs)))
+                                 _i64(rx2), _i64(ra1), _i64(ra2), *ptrs))
 
 
 def djac_apply(ptype, rx1, n, rx2, jacs, x, y, ctx=None):
     """y = P x with the blocks of djac_gen (djac_apply, tt_linalg.f90:497-531)."""
+    nx = rx1 * n * rx2
+    ptrs = (_dev(jacs, max(0, djac_size(ptype, rx1, n, rx2)), "float64", "jacs"),
+            _dev(x, nx, "float64", "x"), _dev(y, nx, "float64", "y"))
     ctx = _kctx(ctx)
     ctx.check(lib().ttg_djac_apply(ctx.handle, C.c_char(ptype.encode()), _i64(rx1), _i64(n),
-                                   _i64(rx2), _dev(jacs), _dev(x), _dev(y)))
+                                   _i64(rx2), *ptrs))
 
 
 def zbfun3(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1, A, phi2, x, y, nvec=1, transp=False,
            ctx=None):
     """Complex product zbfun3 (ttals.f90:34) / zbfun3_transp (:85); complex128 tensors."""
+    dims = (rx1, m, rx2, ry1, n, ry2, ra1, ra2)
+    ptrs = _bfun3_ptrs(dims, phi1, A, phi2, x, y, nvec, "complex128", transp=transp)
     ctx = _kctx(ctx)
     f = lib().ttg_zbfun3_transp if transp else lib().ttg_zbfun3
-    ctx.check(f(ctx.handle, *_dims(rx1, m, rx2, ry1, n, ry2, ra1, ra2), _dev(phi1), _dev(A),
-                _dev(phi2), _dev(x), _dev(y), _i64(nvec)))
+    ctx.check(f(ctx.handle, *_dims(*dims), *ptrs, _i64(nvec)))
 
 
 def phi_left(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1_old, A, x, y, out, complex_=False,
              ctx=None):
+    dt = "complex128" if complex_ else "float64"
+    ptrs = (_dev(phi1_old, ry1 * rx1 * ra1, dt, "phi1_old"), _dev(A, ra1 * n * m * ra2, dt, "A"),
+            _dev(x, rx1 * m * rx2, dt, "x"), _dev(y, ry1 * n * ry2, dt, "y"),
+            _dev(out, ry2 * rx2 * ra2, dt, "out"))
     ctx = _kctx(ctx)
     f = lib().ttg_zphi_left if complex_ else lib().ttg_dphi_left
-    ctx.check(f(ctx.handle, *_dims(rx1, m, rx2, ry1, n, ry2, ra1, ra2), _dev(phi1_old), _dev(A),
-                _dev(x), _dev(y), _dev(out)))
+    ctx.check(f(ctx.handle, *_dims(rx1, m, rx2, ry1, n, ry2, ra1, ra2), *ptrs))
 
 
 def phi_right(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi2_old, A, x, y, out, complex_=False,
               ctx=None):
+    dt = "complex128" if complex_ else "float64"
+    ptrs = (_dev(phi2_old, rx2 * ra2 * ry2, dt, "phi2_old"), _dev(A, ra1 * n * m * ra2, dt, "A"),
+            _dev(x, rx1 * m * rx2, dt, "x"), _dev(y, ry1 * n * ry2, dt, "y"),
+            _dev(out, rx1 * ra1 * ry1, dt, "out"))
     ctx = _kctx(ctx)
     f = lib().ttg_zphi_right if complex_ else lib().ttg_dphi_right
-    ctx.check(f(ctx.handle, *_dims(rx1, m, rx2, ry1, n, ry2, ra1, ra2), _dev(phi2_old), _dev(A),
-                _dev(x), _dev(y), _dev(out)))
+    ctx.check(f(ctx.handle, *_dims(rx1, m, rx2, ry1, n, ry2, ra1, ra2), *ptrs))
 
 
 def phi2_left(rx1, rx2, ry1, n, ry2, phi1_old, x, y, out, ctx=None):
+    ptrs = (_dev(phi1_old, ry1 * rx1, "float64", "phi1_old"),
+            _dev(x, rx1 * n * rx2, "float64", "x"), _dev(y, ry1 * n * ry2, "float64", "y"),
+            _dev(out, ry2 * rx2, "float64", "out"))
     ctx = _kctx(ctx)
-    ctx.check(lib().ttg_dphi2_left(ctx.handle, *_dims(rx1, rx2, ry1, n, ry2), _dev(phi1_old),
-                                   _dev(x), _dev(y), _dev(out)))
+    ctx.check(lib().ttg_dphi2_left(ctx.handle, *_dims(rx1, rx2, ry1, n, ry2), *ptrs))
 
 
 def phi2_right(rx1, rx2, ry1, n, ry2, phi2_old, x, y, out, ctx=None):
+    ptrs = (_dev(phi2_old, rx2 * ry2, "float64", "phi2_old"),
+            _dev(x, rx1 * n * rx2, "float64", "x"), _dev(y, ry1 * n * ry2, "float64", "y"),
+            _dev(out, rx1 * ry1, "float64", "out"))
     ctx = _kctx(ctx)
-    ctx.check(lib().ttg_dphi2_right(ctx.handle, *_dims(rx1, rx2, ry1, n, ry2), _dev(phi2_old),
-                                    _dev(x), _dev(y), _dev(out)))
+    ctx.check(lib().ttg_dphi2_right(ctx.handle, *_dims(rx1, rx2, ry1, n, ry2), *ptrs))
 
 
 def fullmat(rx1, m, rx2, ra1, ra2, phi1, A, phi2, out, ctx=None):
+    N = rx1 * m * rx2
+    ptrs = (_dev(phi1, rx1 * rx1 * ra1, "float64", "phi1"),
+            _dev(A, ra1 * m * m * ra2, "float64", "A"),
+            _dev(phi2, rx2 * ra2 * rx2, "float64", "phi2"), _dev(out, N * N, "float64", "out"))
     ctx = _kctx(ctx)
-    ctx.check(lib().ttg_d2d_fullmat(ctx.handle, *_dims(rx1, m, rx2, ra1, ra2), _dev(phi1),
-                                    _dev(A), _dev(phi2), _dev(out)))
+    ctx.check(lib().ttg_d2d_fullmat(ctx.handle, *_dims(rx1, m, rx2, ra1, ra2), *ptrs))
 
 
 def dqr(nrows, ncols, A, R, complex_=False, ctx=None):
     """In-place QR (dqr matrix_util.f90:37): A -> Q, R written."""
+    dt = "complex128" if complex_ else "float64"
+    ptrs = (_dev(A, nrows * ncols, dt, "A"), _dev(R, min(nrows, ncols) * ncols, dt, "R"))
     ctx = _kctx(ctx)
     f = lib().ttg_zqr if complex_ else lib().ttg_dqr
-    ctx.check(f(ctx.handle, _i64(nrows), _i64(ncols), _dev(A), _dev(R)))
+    ctx.check(f(ctx.handle, _i64(nrows), _i64(ncols), *ptrs))
 
 
 def dsyev(k, A, w, ctx=None):
+    ptrs = (_dev(A, k * k, "float64", "A"), _dev(w, k, "float64", "w"))
     ctx = _kctx(ctx)
-    ctx.check(lib().ttg_dsyev(ctx.handle, _i64(k), _dev(A), _dev(w)))
+    ctx.check(lib().ttg_dsyev(ctx.handle, _i64(k), *ptrs))
 
 
 def dgesvd(p, q, M, U, s, Vt, ctx=None):
+    r = min(p, q)
+    ptrs = (_dev(M, p * q, "float64", "M"), _dev(U, p * r, "float64", "U"),
+            _dev(s, r, "float64", "s"), _dev(Vt, r * q, "float64", "Vt"))
     ctx = _kctx(ctx)
-    ctx.check(lib().ttg_dgesvd(ctx.handle, _i64(p), _i64(q), _dev(M), _dev(U), _dev(s), _dev(Vt)))
+    ctx.check(lib().ttg_dgesvd(ctx.handle, _i64(p), _i64(q), *ptrs))
 
 
 def dmaxvol(nrows, r, A, p, Z=None, tol=1e-2, maxiters=1024, ctx=None):
+    ptrs = (_dev(A, nrows * r, "float64", "A"), _dev(p, r, "int64", "p"),
+            _dev(Z, nrows * r, "float64", "Z") if Z is not None else C.c_void_p())
     ctx = _kctx(ctx)
-    ctx.check(lib().ttg_dmaxvol(ctx.handle, _i64(nrows), _i64(r), _dev(A), _dev(p),
-                                _dev(Z) if Z is not None else C.c_void_p(), C.c_double(tol),
+    ctx.check(lib().ttg_dmaxvol(ctx.handle, _i64(nrows), _i64(r), *ptrs, C.c_double(tol),
                                 _i64(maxiters)))
 
 
@@ -506,15 +555,22 @@ class LocalOp:
 
     def __init__(self, rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1, A, phi2, nvec_max=8,
                  method="plain", ctx=None):
+        self._h = C.c_void_p()
+        dims = (rx1, m, rx2, ry1, n, ry2, ra1, ra2)
+        self._xy = (rx1 * m * rx2, ry1 * n * ry2)
+        ptrs = (_dev(phi1, ry1 * rx1 * ra1, "float64", "phi1"),
+                _dev(A, ra1 * n * m * ra2, "float64", "A"),
+                _dev(phi2, rx2 * ra2 * ry2, "float64", "phi2"))
         self.ctx = _kctx(ctx)
         self._keep = (phi1, A, phi2)
-        self._h = C.c_void_p()
         self.ctx.check(lib().ttg_localop_create(
-            self.ctx.handle, *_dims(rx1, m, rx2, ry1, n, ry2, ra1, ra2), _dev(phi1), _dev(A),
-            _dev(phi2), _i64(nvec_max), C.c_int(METHOD[method]), C.byref(self._h)))
+            self.ctx.handle, *_dims(*dims), *ptrs, _i64(nvec_max), C.c_int(METHOD[method]),
+            C.byref(self._h)))
 
     def apply(self, X, Y, nvec=1):
-        self.ctx.check(lib().ttg_localop_apply(self._h, _dev(X), _dev(Y), _i64(nvec)))
+        nx, ny = self._xy
+        self.ctx.check(lib().ttg_localop_apply(self._h, _dev(X, nx * nvec, "float64", "X"),
+                                               _dev(Y, ny * nvec, "float64", "Y"), _i64(nvec)))
 
     def close(self):
         if self._h:
