@@ -168,3 +168,18 @@ def test_laplace_and_amen_operators():
     g = np.exp(-((np.arange(4) - 1.5) ** 2) / (0.3 * 4) ** 2)
     pot = np.kron(np.kron(np.diag(g), np.diag(g)), np.diag(g))
     assert np.allclose(full, ref + pot)
+
+
+@pytest.mark.parametrize("shape", [(3, 2, 5, 3, 2, 5, 4, 5), (7, 3, 11, 5, 2, 9, 2, 3)])
+def test_zbfun3_transp_is_the_adjoint(shape):
+    """zbfun3_transp (ttals.f90:85-108), the norm estimate's second product,
+    is the conjugate transpose of zbfun3: <B x, y> = <x, B^H y>, also for
+    rectangular local problems (ry != rx, n != m)."""
+    rx1, m, rx2, ry1, n, ry2, ra1, ra2 = shape
+    rng = np.random.default_rng(sum(shape))
+    c = lambda k: rng.standard_normal(k) + 1j * rng.standard_normal(k)  # noqa: E731
+    phi1, A, phi2 = c(ry1 * rx1 * ra1), c(ra1 * n * m * ra2), c(rx2 * ra2 * ry2)
+    x, y = c(rx1 * m * rx2), c(ry1 * n * ry2)
+    bx = ops.bfun3(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1, A, phi2, x)
+    bhy = ops.zbfun3_transp(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1, A, phi2, y)
+    assert abs(np.vdot(y, bx) - np.vdot(bhy, x)) <= 1e-12 * np.linalg.norm(bx) * np.linalg.norm(y)
