@@ -2,9 +2,9 @@
  * ttgpu.h -- C-ABI of the GB300 tensor-train sweep library (libttgpu.so).
  *
  * Drop-in boundary for the hot path of oseledets/tt-fort: the ALS/AMEn/KSL
- * sweep.  A Fortran host binds these symbols through ISO_C_BINDING (the
- * interface module is in INTEGRATION.md); C and Python (ctypes) callers use
- * them directly.
+ * sweep.  A Fortran host binds these symbols through ISO_C_BINDING (a
+ * bind(c) interface module that mirrors these declarations); C and Python
+ * (ctypes) callers use them directly.
  *
  * Conventions
  *   - integers are 64-bit (ttg_int), fixed for every build (the reference's
@@ -80,9 +80,11 @@ int ttg_dbfun3_split(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_int 
  * The intermediates live in one library-owned device array of
  * TTG_NOALLOC_SCRATCH_DOUBLES doubles (16 MiB, held by every GPU that loads the
  * library until exit).  The first call on a device looks up that array's
- * device address (set-up, once per device).  Sizes with
+ * device address (set-up, once per device and CUDA context, so make that first
+ * call before any stream capture).  Sizes with
  * (rx1*m*ra2*ry2 + rx1*ra1*n*ry2) * nvec > TTG_NOALLOC_SCRATCH_DOUBLES are
- * rejected with TTG_ERR_ARG.  All calls share the array: calls that overlap on
+ * rejected with TTG_ERR_ARG, and so are sizes whose products overflow 64 bits.
+ * All calls share the array: calls that overlap on
  * the GPU race and must be serialised by the caller.  Calls no cudaMalloc,
  * cudaFree or other allocating routine. */
 #define TTG_NOALLOC_SCRATCH_DOUBLES 2097152

@@ -47,6 +47,38 @@ def test_noalloc_matches_dbfun3_twice(torch_cuda):
     ctx.close()
 
 
+def test_noalloc_leaves_device_memory_unchanged(torch_cuda):
+    """The point of the entry point: after the first call's set-up, further
+    calls at the largest shape the fixed array allows take no device memory
+    (free memory as the driver reports it does not move)."""
+    import ttgpu
+    torch = torch_cuda
+    ctx = ttgpu.Context(0)
+    ctx.bind_torch_stream()
+    lib = ttgpu.lib()
+    # (rx1*m*ra2*ry2 + rx1*ra1*n*ry2) * nvec = 2 * 128*2*5*128 * 6 = 1,966,080 <= 2^21
+    rx1 = rx2 = ry1 = ry2 = 128
+    m = n = 2
+    ra1 = ra2 = 5
+    nvec = 6
+    rng = np.random.default_rng(7)
+    t = lambda k: torch.from_numpy(rng.standard_normal(k)).cuda()
+    phi1, A, phi2 = t(ry1 * rx1 * ra1), t(ra1 * n * m * ra2), t(rx2 * ra2 * ry2)
+    X = t(rx1 * m * rx2 * nvec)
+    y = torch.zeros(ry1 * n * ry2 * nvec, dtype=torch.float64, device="cuda")
+    dims = (rx1, m, rx2, ry1, n, ry2, ra1, ra2)
+    ctx.check(_call(lib.ttg_dbfun3_noalloc, ctx, dims, (phi1, A, phi2, X, y), nvec))
+    ctx.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(4):
+        ctx.check(_call(lib.ttg_dbfun3_noalloc, ctx, dims, (phi1, A, phi2, X, y), nvec))
+    ctx.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    assert torch.isfinite(y).all().item()
+    ctx.close()
+
+
 def test_noalloc_rejects_oversized_problem(torch_cuda):
     import ttgpu
     torch = torch_cuda
@@ -56,6 +88,12 @@ def test_noalloc_rejects_oversized_problem(torch_cuda):
     # (rx1*m*ra2*ry2 + rx1*ra1*n*ry2) * nvec = 2 * 256*2*5*256 * 4 > 2^21
     rc = _call(lib.ttg_dbfun3_noalloc, ctx, (256, 2, 256, 256, 2, 256, 5, 5),
                (dummy, dummy, dummy, dummy, dummy), 4)
+    assert rc == -1
+    assert "fixed maximum" in lib.ttg_last_error(ctx.handle).decode()
+    # sizes whose scratch product overflows 64 bits are rejected the same way
+    big = 1 << 40
+    rc = _call(lib.ttg_dbfun3_noalloc, ctx, (1, 1, 1, 1, 1, 1, big, big),
+               (dummy, dummy, dummy, dummy, dummy), big)
     assert rc == -1
     assert "fixed maximum" in lib.ttg_last_error(ctx.handle).decode()
     ctx.close()

@@ -48,7 +48,8 @@ __global__ void scal_kernel(i64 n, const double* sdev, int invert, double* x) {
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
     x[i] *= s;
 }
-// out[j] += sum_i x[i + ld*j]^2  (pre-zeroed), grid (bx, ncols)
+// out[j] = sum_i x[i + ld*j]^2, grid (bx, ncols); the bx CTAs of a column are
+// one cluster and add their partials in rank order (deterministic)
 __global__ void sqnorm_cols_kernel(i64 n, const double* x, i64 ld, double* out) {
   const int j = blockIdx.y;
   double acc = 0.0;
@@ -56,17 +57,13 @@ __global__ void sqnorm_cols_kernel(i64 n, const double* x, i64 ld, double* out) 
     const double v = x[i + ld * j];
     acc = fma(v, v, acc);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  __shared__ double red[32];
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double t = threadIdx.x < (int)(blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (threadIdx.x == 0) atomicAdd(&out[j], t);
-  }
+  const double t = cluster_sum(acc);
+  if (blockIdx.x == 0 && threadIdx.x == 0) out[j] = t;
+}
+void sqnorm_cols(i64 n, const double* x, i64 ld, int ncols, double* out, cudaStream_t s) {
+  const int bx = (int)std::max<i64>(1, std::min<i64>(kMaxCluster, (n + 2047) / 2048));
+  launch_clustered(sqnorm_cols_kernel, dim3(bx, ncols), dim3(256), dim3(bx, 1, 1), 0, s, n, x,
+                   ld, out);
 }
 __global__ void sqrt_kernel(int n, double* x) {
   if (threadIdx.x < n) x[threadIdx.x] = sqrt(x[threadIdx.x]);
@@ -256,12 +253,7 @@ void gmres_cgs2(const MV& mv, i64 N, const double* b, double* x, double tol, int
     mv(x, G.w, 1);
     sub_kernel<<<eb(N), 256, 0, s>>>(N, b, G.w, G.w);
     TTG_CHECK_LAUNCH();
-    TTG_CUDA(cudaMemsetAsync(red, 0, sizeof(double), s));
-    {
-      int bx = (int)std::max<i64>(1, std::min<i64>(256, (N + 2047) / 2048));
-      sqnorm_cols_kernel<<<dim3(bx, 1), 256, 0, s>>>(N, G.w, N, red);
-      TTG_CHECK_LAUNCH();
-    }
+    sqnorm_cols(N, G.w, N, 1, red, s);
     TTG_CUDA(cudaMemcpyAsync(h, red, sizeof(double), cudaMemcpyDeviceToHost, s));
     sync();
     const double beta = std::sqrt(h[0]);
@@ -287,10 +279,7 @@ void gmres_cgs2(const MV& mv, i64 N, const double* b, double* x, double tol, int
       gemm_nn_small(N, 1, j + 1, V, N, H2, j + 2, wv, N, -1.0, 1.0, s);
       axpy_kernel<<<1, 64, 0, s>>>(j + 1, 1.0, H2, H);
       TTG_CHECK_LAUNCH();
-      TTG_CUDA(cudaMemsetAsync(red, 0, sizeof(double), s));
-      int bx = (int)std::max<i64>(1, std::min<i64>(256, (N + 2047) / 2048));
-      sqnorm_cols_kernel<<<dim3(bx, 1), 256, 0, s>>>(N, wv, N, red);
-      TTG_CHECK_LAUNCH();
+      sqnorm_cols(N, wv, N, 1, red, s);
       sqrt_kernel<<<1, 32, 0, s>>>(1, red);
       TTG_CHECK_LAUNCH();
       TTG_CUDA(cudaMemcpyAsync(H + j + 1, red, sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -370,10 +359,7 @@ class AmenSolver {
     return LocalDims{xx.r[k], xx.n[k], xx.r[k + 1], yy.r[k], yy.n[k], yy.r[k + 1], P_.ra[k], P_.ra[k + 1]};
   }
   double norm2(const double* v, i64 n) {
-    TTG_CUDA(cudaMemsetAsync(red_, 0, sizeof(double), s_));
-    int bx = (int)std::max<i64>(1, std::min<i64>(256, (n + 2047) / 2048));
-    sqnorm_cols_kernel<<<dim3(bx, 1), 256, 0, s_>>>(n, v, n, red_);
-    TTG_CHECK_LAUNCH();
+    sqnorm_cols(n, v, n, 1, red_, s_);
     TTG_CUDA(cudaMemcpyAsync(h_, red_, sizeof(double), cudaMemcpyDeviceToHost, s_));
     sync();
     return std::sqrt(h_[0]);
@@ -549,10 +535,7 @@ void AmenSolver::trunc(int k, double tol, const double* rhs, double rhs_norm) {
       sub_cols_kernel<<<eb(N * cnt), 256, 0, s_>>>(N, cnt, candY_, rhs, candY_);
       TTG_CHECK_LAUNCH();
     }
-    TTG_CUDA(cudaMemsetAsync(red_, 0, sizeof(double) * cnt, s_));
-    int bx = (int)std::max<i64>(1, std::min<i64>(128, (N + 2047) / 2048));
-    sqnorm_cols_kernel<<<dim3(bx, cnt), 256, 0, s_>>>(N, candY_, N, red_);
-    TTG_CHECK_LAUNCH();
+    sqnorm_cols(N, candY_, N, cnt, red_, s_);
     TTG_CUDA(cudaMemcpyAsync(h_, red_, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s_));
     sync();
     for (int c = 0; c < cnt; ++c) {
@@ -1059,10 +1042,7 @@ class AlsSolver {
     gemm_f64(g, s_);
   }
   double norm2(const double* v, i64 n) {
-    TTG_CUDA(cudaMemsetAsync(red_, 0, sizeof(double), s_));
-    int bx = (int)std::max<i64>(1, std::min<i64>(256, (n + 2047) / 2048));
-    sqnorm_cols_kernel<<<dim3(bx, 1), 256, 0, s_>>>(n, v, n, red_);
-    TTG_CHECK_LAUNCH();
+    sqnorm_cols(n, v, n, 1, red_, s_);
     TTG_CUDA(cudaMemcpyAsync(h_, red_, sizeof(double), cudaMemcpyDeviceToHost, s_));
     sync();
     return std::sqrt(h_[0]);
@@ -1109,10 +1089,7 @@ int AlsSolver::scan(int i, int rmin, const double* L, i64 ldl, const double* Rr,
     mv(i, cand_, candY_, cnt);
     sub_cols_kernel<<<eb(N * cnt), 256, 0, s_>>>(N, cnt, candY_, rhs, candY_);
     TTG_CHECK_LAUNCH();
-    TTG_CUDA(cudaMemsetAsync(red_, 0, sizeof(double) * cnt, s_));
-    int bx = (int)std::max<i64>(1, std::min<i64>(128, (N + 2047) / 2048));
-    sqnorm_cols_kernel<<<dim3(bx, cnt), 256, 0, s_>>>(N, candY_, N, red_);
-    TTG_CHECK_LAUNCH();
+    sqnorm_cols(N, candY_, N, cnt, red_, s_);
     TTG_CUDA(cudaMemcpyAsync(h_, red_, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s_));
     sync();
     for (int q = 0; q < cnt; ++q) {
@@ -1498,10 +1475,7 @@ class MvkSolver {
     gemm_f64(g, s_);
   }
   double norm2(const double* v, i64 n) {
-    TTG_CUDA(cudaMemsetAsync(red_, 0, sizeof(double), s_));
-    int bx = (int)std::max<i64>(1, std::min<i64>(256, (n + 2047) / 2048));
-    sqnorm_cols_kernel<<<dim3(bx, 1), 256, 0, s_>>>(n, v, n, red_);
-    TTG_CHECK_LAUNCH();
+    sqnorm_cols(n, v, n, 1, red_, s_);
     TTG_CUDA(cudaMemcpyAsync(h_, red_, sizeof(double), cudaMemcpyDeviceToHost, s_));
     sync();
     return std::sqrt(h_[0]);

@@ -9,12 +9,14 @@
 // (ttals.f90:9-32 index comments).
 #pragma once
 #include <cuda_runtime.h>
+#include <cooperative_groups.h>
 #include <cstdint>
 #include <cstdio>
 #include <string>
 #include <vector>
 #include <complex>
 #include <atomic>
+#include <utility>
 
 #include "../../include/ttgpu.h"
 
@@ -52,6 +54,60 @@ extern std::atomic<long long> g_launches;
   do {                                                                          \
     if (!(cond)) throw ::ttg::Error{TTG_ERR_ARG, std::string(msg)};             \
   } while (0)
+
+// -------------------------------------------------------------------------
+// Deterministic reductions across CTAs.  Partial sums of several CTAs are
+// combined inside one thread block cluster through distributed shared memory
+// in a fixed order (lanes, then warps, then cluster ranks), never by atomics,
+// so a result does not depend on which CTA finishes first.  Clusters hold at
+// most kMaxCluster CTAs (the portable limit), which bounds every split.
+// -------------------------------------------------------------------------
+constexpr int kMaxCluster = 8;
+
+// Sum of v over every thread of every CTA in the cluster.  All threads of all
+// CTAs of the cluster must call it (it holds two cluster barriers); the sum is
+// returned in thread 0 of cluster rank 0, every other thread gets 0.  A kernel
+// launched without a cluster is a cluster of one CTA.
+__device__ __forceinline__ double cluster_sum(double v) {
+  namespace cg = cooperative_groups;
+  __shared__ double red[33];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)((blockDim.x + 31) >> 5); ++w) t += red[w];
+    red[32] = t;
+  }
+  cg::cluster_group cl = cg::this_cluster();
+  cl.sync();
+  double out = 0.0;
+  if (cl.block_rank() == 0 && threadIdx.x == 0)
+    for (unsigned r = 0; r < cl.num_blocks(); ++r) out += *cl.map_shared_rank(&red[32], r);
+  cl.sync();
+  return out;
+}
+
+// launch kernel k on grid/block with a cluster of cx x cy x cz CTAs
+template <class... KArgs, class... Args>
+void launch_clustered(void (*k)(KArgs...), dim3 grid, dim3 block, dim3 cluster, size_t smem,
+                      cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = cluster.x;
+  at[0].val.clusterDim.y = cluster.y;
+  at[0].val.clusterDim.z = cluster.z;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  TTG_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...));
+  TTG_CHECK_LAUNCH();
+}
 
 // -------------------------------------------------------------------------
 // device workspace: a bump allocator over one growing cudaMalloc block.
@@ -127,7 +183,8 @@ struct GemmF64 {
   double alpha = 1.0, beta = 0.0;
   int nb1 = 1, nb2 = 1;
   i64 bA1 = 0, bA2 = 0, bB1 = 0, bB2 = 0, bC1 = 0, bC2 = 0;
-  int splitk = 1;   // > 1: K split over CTAs, C accumulated with FP64 atomics
+  int splitk = 1;   // > 1: K split over the CTAs of one cluster (at most kMaxCluster),
+                    // partial tiles added in a fixed order (deterministic)
 };
 void gemm_f64(const GemmF64& g, cudaStream_t s);
 

@@ -9,8 +9,6 @@ namespace ttg {
 static constexpr double CHOL_DROP = 1e-14;
 static constexpr double RESTART_DROP = 1e-10;
 
-int splitk_for(i64 K) { return (int)std::max<i64>(1, std::min<i64>(1024, K / 512)); }
-
 // ---------------------------------------------------------------------------
 // Tall-skinny FP64 products of the Davidson basis.  GB300 runs FP64 at a few
 // GFLOP/s per SM, so these spread the long dimension over every SM instead of
@@ -19,11 +17,13 @@ int splitk_for(i64 K) { return (int)std::max<i64>(1, std::min<i64>(1024, K / 512
 constexpr int TS_MAXN = 16;
 
 // C (M x N, ldc) = alpha * A^T B + beta * C, A (K x M, lda), B (K x N, ldb),
-// N <= 16.  Grid (M, nk): CTA (m, c) reduces k-chunk c of column m of A
-// against all N columns of B and adds with FP64 atomics (C pre-scaled).
+// N <= 16.  Grid (M, nk), one cluster of nk CTAs per column m of A: CTA
+// (m, c) reduces k-chunk c against all N columns of B, then rank 0 adds the
+// nk partials in rank order (deterministic, no atomics, no pre-scaling pass).
 __global__ void tn_small_kernel(int M, int N, i64 K, const double* __restrict__ A, i64 lda,
                                 const double* __restrict__ B, i64 ldb, double* __restrict__ C,
-                                int ldc, double alpha, i64 kchunk) {
+                                int ldc, double alpha, double beta, i64 kchunk) {
+  namespace cgr = cooperative_groups;
   const int m = blockIdx.x;
   const i64 k0 = blockIdx.y * kchunk, k1 = min(K, k0 + kchunk);
   double acc[TS_MAXN];
@@ -37,6 +37,7 @@ __global__ void tn_small_kernel(int M, int N, i64 K, const double* __restrict__ 
       if (n < N) acc[n] = fma(av, B[k + ldb * n], acc[n]);
   }
   __shared__ double red[TS_MAXN][8];
+  __shared__ double part[TS_MAXN];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int n = 0; n < TS_MAXN; ++n) {
@@ -50,30 +51,31 @@ __global__ void tn_small_kernel(int M, int N, i64 K, const double* __restrict__ 
   if (threadIdx.x < N) {
     double v = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[threadIdx.x][w];
-    atomicAdd(&C[m + (i64)ldc * threadIdx.x], alpha * v);
+    part[threadIdx.x] = v;
   }
-}
-
-__global__ void scale_small_kernel(int M, int N, double* C, int ldc, double beta) {
-  for (int e = threadIdx.x; e < M * N; e += blockDim.x) {
-    double* p = C + (e % M) + (i64)ldc * (e / M);
-    *p = beta == 0.0 ? 0.0 : beta * *p;
+  cgr::cluster_group cl = cgr::this_cluster();
+  cl.sync();
+  if (cl.block_rank() == 0 && threadIdx.x < N) {
+    double v = 0.0;
+    for (unsigned r = 0; r < cl.num_blocks(); ++r) v += cl.map_shared_rank(part, r)[threadIdx.x];
+    double* p = C + m + (i64)ldc * threadIdx.x;
+    *p = beta == 0.0 ? alpha * v : fma(beta, *p, alpha * v);
   }
+  cl.sync();
 }
 
 void gemm_tn_small(int M, int N, i64 K, const double* A, i64 lda, const double* B, i64 ldb,
                    double* C, int ldc, double alpha, double beta, cudaStream_t s) {
   if (M <= 0 || N <= 0) return;
   TTG_REQUIRE(N <= TS_MAXN, "gemm_tn_small: N > 16");
-  scale_small_kernel<<<1, 256, 0, s>>>(M, N, C, ldc, beta);
-  TTG_CHECK_LAUNCH();
-  if (K <= 0) return;
-  // about 2 CTAs per SM in total, at least 256 k per CTA
+  TTG_REQUIRE(M < 65536, "gemm_tn_small: M too large");
+  // about 2 CTAs per SM in total, at least 256 k per CTA, at most one cluster
+  // of kMaxCluster CTAs per column
   i64 nk = std::max<i64>(1, std::min<i64>((304 + M - 1) / M, (K + 255) / 256));
-  i64 kchunk = (K + nk - 1) / nk;
-  tn_small_kernel<<<dim3(M, (unsigned)nk), 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha,
-                                                         kchunk);
-  TTG_CHECK_LAUNCH();
+  nk = std::min<i64>(nk, kMaxCluster);
+  i64 kchunk = std::max<i64>(1, (K + nk - 1) / nk);
+  launch_clustered(tn_small_kernel, dim3(M, (unsigned)nk), dim3(256), dim3(1, (unsigned)nk, 1),
+                   0, s, M, N, K, A, lda, B, ldb, C, ldc, alpha, beta, kchunk);
 }
 
 // C (R x N, ldc) = alpha * A (R x K, lda) * B (K x N, ldb) + beta * C, with
@@ -112,7 +114,9 @@ void gemm_nn_small(i64 R, int N, int K, const double* A, i64 lda, const double* 
   TTG_CHECK_LAUNCH();
 }
 
-// R[:, j] = AX[:, j] - theta_j X[:, j];  rn2[j] += ||R[:, j]||^2 (rn2 pre-zeroed)
+// R[:, j] = AX[:, j] - theta_j X[:, j];  rn2[j] = ||R[:, j]||^2.  Grid (bx, nb),
+// the bx CTAs of column j are one cluster and add their partial sums in rank
+// order (deterministic).
 __global__ void residual_kernel(i64 N, const double* __restrict__ AX, const double* __restrict__ X,
                                 const double* __restrict__ theta, double* __restrict__ R,
                                 double* __restrict__ rn2) {
@@ -124,25 +128,15 @@ __global__ void residual_kernel(i64 N, const double* __restrict__ AX, const doub
     R[i + N * j] = r;
     acc = fma(r, r, acc);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  __shared__ double red[32];
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (threadIdx.x == 0) atomicAdd(&rn2[j], t);
-  }
+  const double t = cluster_sum(acc);
+  if (blockIdx.x == 0 && threadIdx.x == 0) rn2[j] = t;
 }
 
 void residual_cols(i64 N, int nb, const double* AX, const double* X, const double* theta,
                    double* R, double* rn2, cudaStream_t s) {
-  TTG_CUDA(cudaMemsetAsync(rn2, 0, sizeof(double) * nb, s));
-  int bx = (int)std::max<i64>(1, std::min<i64>(256, (N + 1023) / 1024));
-  residual_kernel<<<dim3(bx, nb), 256, 0, s>>>(N, AX, X, theta, R, rn2);
-  TTG_CHECK_LAUNCH();
+  int bx = (int)std::max<i64>(1, std::min<i64>(kMaxCluster, (N + 1023) / 1024));
+  launch_clustered(residual_kernel, dim3(bx, nb), dim3(256), dim3(bx, 1, 1), 0, s, N, AX, X,
+                   theta, R, rn2);
 }
 
 __global__ void gather_cols_kernel(i64 N, int t, const int* idx, const double* src, double* dst) {
@@ -398,7 +392,6 @@ DavidsonStats Davidson::solve(const MatvecFn& mv, const double* X0, double tol, 
                               double* X, double* theta_host) {
   DavidsonStats st;
   Lap lap(timer);
-  const int sk = splitk_for(N_);
   const int ldh = maxb_;
   k_ = 0;
   kwarm_ = 0;

@@ -5,8 +5,11 @@
 // tt_ksl.f90:586,614; PRIMME's tall-skinny V'W / V*S products).  Operands are
 // addressed through explicit (row, column) strides, so the reference's
 // dtransp/ztransp passes (ttals.f90:22,26) fold into the index arithmetic
-// instead of running as separate kernels.  A K-split mode with FP64 atomics
-// serves the tall-skinny reductions (K = local problem size, M,N <= 128).
+// instead of running as separate kernels.  A K-split mode serves the
+// tall-skinny reductions (K = local problem size, M,N <= 128): the K-chunks of
+// one output tile run as the CTAs of one thread block cluster and their
+// partial tiles are added in rank order through distributed shared memory, so
+// results are bit-reproducible (no atomics).
 //
 // Tiles: 256 threads, BK = 16, register-prefetched global loads, shared
 // memory staged epilogue so that stores are coalesced along whichever output
@@ -24,7 +27,6 @@ template <> struct Ops<float> {
   static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
   static __device__ __forceinline__ float add(float a, float b) { return a + b; }
   static __device__ __forceinline__ bool is_zero(float a) { return a == 0.f; }
-  static __device__ __forceinline__ void atomic_add(float* p, float v) { atomicAdd(p, v); }
 };
 template <> struct Ops<double> {
   static __device__ __forceinline__ double zero() { return 0.0; }
@@ -33,7 +35,6 @@ template <> struct Ops<double> {
   static __device__ __forceinline__ double mul(double a, double b) { return a * b; }
   static __device__ __forceinline__ double add(double a, double b) { return a + b; }
   static __device__ __forceinline__ bool is_zero(double a) { return a == 0.0; }
-  static __device__ __forceinline__ void atomic_add(double* p, double v) { atomicAdd(p, v); }
 };
 template <> struct Ops<double2> {
   static __device__ __forceinline__ double2 zero() { return make_double2(0.0, 0.0); }
@@ -52,10 +53,6 @@ template <> struct Ops<double2> {
     return make_double2(a.x + b.x, a.y + b.y);
   }
   static __device__ __forceinline__ bool is_zero(double2 a) { return a.x == 0.0 && a.y == 0.0; }
-  static __device__ __forceinline__ void atomic_add(double2* p, double2 v) {
-    atomicAdd(&p->x, v.x);
-    atomicAdd(&p->y, v.y);
-  }
 };
 
 template <class T> struct Args {
@@ -176,6 +173,29 @@ __global__ void __launch_bounds__(NT) gemm_kernel(Args<T> g) {
     for (int j = 0; j < TN; ++j) Cs[(tx + TX * j) * (BM + 1) + ty + TY * i] = acc[i][j];
   __syncthreads();
   const bool c_mfast = (g.sCm == 1) || (g.sCn != 1 && g.sCm < g.sCn);
+  if (g.splitk > 1) {
+    // the splitk CTAs of this tile are one cluster (rank = ks); CTA ks
+    // finishes elements ks*NT + tid + j*NT*splitk, adding the partial tiles of
+    // ranks 0..splitk-1 in that order
+    namespace cgr = cooperative_groups;
+    cgr::cluster_group cl = cgr::this_cluster();
+    cl.sync();
+    for (int e = ks * NT + tid; e < BM * BN; e += NT * g.splitk) {
+      int mm, nn;
+      if (c_mfast) { mm = e % BM; nn = e / BM; } else { nn = e % BN; mm = e / BN; }
+      int gm = m0 + mm, gn = n0 + nn;
+      if (gm >= g.M || gn >= g.N) continue;
+      T acc_e = O::zero();
+      for (int r = 0; r < g.splitk; ++r)
+        acc_e = O::add(acc_e, cl.map_shared_rank(Cs, r)[nn * (BM + 1) + mm]);
+      T v = O::mul(g.alpha, acc_e);
+      T* p = C + (i64)gm * g.sCm + (i64)gn * g.sCn;
+      if (!O::is_zero(g.beta)) v = O::add(v, O::mul(g.beta, *p));
+      *p = v;
+    }
+    cl.sync();   // no CTA leaves while another still reads its tile
+    return;
+  }
   for (int e = tid; e < BM * BN; e += NT) {
     int mm, nn;
     if (c_mfast) { mm = e % BM; nn = e / BM; } else { nn = e % BN; mm = e / BN; }
@@ -183,12 +203,8 @@ __global__ void __launch_bounds__(NT) gemm_kernel(Args<T> g) {
     if (gm >= g.M || gn >= g.N) continue;
     T v = O::mul(g.alpha, Cs[nn * (BM + 1) + mm]);
     T* p = C + (i64)gm * g.sCm + (i64)gn * g.sCn;
-    if (g.splitk > 1) {
-      O::atomic_add(p, v);
-    } else {
-      if (!O::is_zero(g.beta)) v = O::add(v, O::mul(g.beta, *p));
-      *p = v;
-    }
+    if (!O::is_zero(g.beta)) v = O::add(v, O::mul(g.beta, *p));
+    *p = v;
   }
 }
 
@@ -207,11 +223,24 @@ __global__ void scale_kernel(T* C, int M, int N, i64 sCm, i64 sCn, int nb1, i64 
   }
 }
 
+template <class T, int BM, int BN, int TM, int TN>
+void launch_tile(const Args<T>& a, int nbatch, cudaStream_t s) {
+  dim3 grid(ceil_div(a.M, BM), ceil_div(a.N, BN), nbatch * a.splitk);
+  if (a.splitk > 1)
+    launch_clustered(gemm_kernel<T, BM, BN, TM, TN>, grid, dim3(NT), dim3(1, 1, a.splitk), 0, s,
+                     a);
+  else {
+    gemm_kernel<T, BM, BN, TM, TN><<<grid, NT, 0, s>>>(a);
+    TTG_CHECK_LAUNCH();
+  }
+}
+
 template <class T>
 void launch(Args<T> a, int nbatch, cudaStream_t s) {
   if (a.M <= 0 || a.N <= 0 || nbatch <= 0) return;
   if (a.K <= 0) {
     // C = beta*C
+    TTG_REQUIRE(nbatch < 65536, "gemm: batch too large");
     int blocks = std::min<i64>(4096, ((i64)a.M * a.N + 255) / 256);
     scale_kernel<T><<<dim3(blocks, 1, nbatch), 256, 0, s>>>(a.C, a.M, a.N, a.sCm, a.sCn, a.nb1,
                                                             a.bC1, a.bC2, a.beta);
@@ -222,8 +251,8 @@ void launch(Args<T> a, int nbatch, cudaStream_t s) {
   // FP64 runs at about two FMAs per clock per SM on GB300, so a product is
   // only fast when its CTAs cover every SM: real products whose 64 x 64 tiles
   // give fewer than two CTAs per SM use 32 x 32 tiles, and products that still
-  // leave SMs idle split K (atomic accumulation) until about two CTAs per SM
-  // are busy.
+  // leave SMs idle split K over the CTAs of a cluster (at most kMaxCluster
+  // chunks, added in a fixed order).
   const bool small_tiles = sizeof(T) <= 8 && a.N > 16 && a.M > 16 &&
                            (i64)ceil_div(a.M, 64) * ceil_div(a.N, 64) * nbatch < 2 * 152;
   if constexpr (sizeof(T) == 16) {
@@ -248,64 +277,37 @@ void launch(Args<T> a, int nbatch, cudaStream_t s) {
       a.splitk = (int)std::max<i64>(1, std::min<i64>(want, a.K / 64));
     }
   }
+  a.splitk = std::min(a.splitk, kMaxCluster);
   a.kchunk = ceil_div(ceil_div(a.K, a.splitk), BK) * BK;
   a.splitk = ceil_div(a.K, a.kchunk);
-  if (a.splitk > 1) {
-    int blocks = std::min<i64>(4096, ((i64)a.M * a.N + 255) / 256);
-    scale_kernel<T><<<dim3(blocks, 1, nbatch), 256, 0, s>>>(a.C, a.M, a.N, a.sCm, a.sCn, a.nb1,
-                                                            a.bC1, a.bC2, a.beta);
-    TTG_CHECK_LAUNCH();
-  }
+  // every limit is checked before anything is launched, so a rejected call
+  // leaves C untouched
   TTG_REQUIRE((i64)nbatch * a.splitk < 65536, "gemm: batch*splitk too large");
+  TTG_REQUIRE(ceil_div(a.N, 16) < 65536, "gemm: N too large");
   if constexpr (sizeof(T) == 16) {
-    if (a.N <= 16) {
-      dim3 grid(ceil_div(a.M, 32), ceil_div(a.N, 16), nbatch * a.splitk);
-      gemm_kernel<T, 32, 16, 2, 1><<<grid, NT, 0, s>>>(a);
-    } else if (a.M <= 16) {
-      dim3 grid(ceil_div(a.M, 16), ceil_div(a.N, 32), nbatch * a.splitk);
-      TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
-      gemm_kernel<T, 16, 32, 1, 2><<<grid, NT, 0, s>>>(a);
-    } else {
-      dim3 grid(ceil_div(a.M, 32), ceil_div(a.N, 32), nbatch * a.splitk);
-      TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
-      gemm_kernel<T, 32, 32, 2, 2><<<grid, NT, 0, s>>>(a);
-    }
-    TTG_CHECK_LAUNCH();
+    if (a.N <= 16)
+      launch_tile<T, 32, 16, 2, 1>(a, nbatch, s);
+    else if (a.M <= 16)
+      launch_tile<T, 16, 32, 1, 2>(a, nbatch, s);
+    else
+      launch_tile<T, 32, 32, 2, 2>(a, nbatch, s);
     return;
   }
   if (a.N <= 16) {
-    constexpr int BM = 128, BN = 16;
-    dim3 grid(ceil_div(a.M, BM), ceil_div(a.N, BN), nbatch * a.splitk);
-    TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
-    gemm_kernel<T, BM, BN, 4, 2><<<grid, NT, 0, s>>>(a);
+    launch_tile<T, 128, 16, 4, 2>(a, nbatch, s);
   } else if (a.M <= 16) {
-    constexpr int BM = 16, BN = 128;
-    dim3 grid(ceil_div(a.M, BM), ceil_div(a.N, BN), nbatch * a.splitk);
-    TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
-    gemm_kernel<T, BM, BN, 2, 4><<<grid, NT, 0, s>>>(a);
+    launch_tile<T, 16, 128, 2, 4>(a, nbatch, s);
   } else {
     if constexpr (sizeof(T) <= 8) {
-      if (small_tiles) {
-        constexpr int BM = 32, BN = 32;
-        dim3 grid(ceil_div(a.M, BM), ceil_div(a.N, BN), nbatch * a.splitk);
-        TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
-        gemm_kernel<T, BM, BN, 2, 2><<<grid, NT, 0, s>>>(a);
-        TTG_CHECK_LAUNCH();
-        return;
-      }
-      constexpr int BM = 64, BN = 64;
-      dim3 grid(ceil_div(a.M, BM), ceil_div(a.N, BN), nbatch * a.splitk);
-      TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
-      gemm_kernel<T, BM, BN, 4, 4><<<grid, NT, 0, s>>>(a);
+      if (small_tiles)
+        launch_tile<T, 32, 32, 2, 2>(a, nbatch, s);
+      else
+        launch_tile<T, 64, 64, 4, 4>(a, nbatch, s);
     } else {
       // complex128: 32x32 tiles keep the static shared memory under 48 KB
-      constexpr int BM = 32, BN = 32;
-      dim3 grid(ceil_div(a.M, BM), ceil_div(a.N, BN), nbatch * a.splitk);
-      TTG_REQUIRE(grid.y < 65536, "gemm: N too large");
-      gemm_kernel<T, BM, BN, 2, 2><<<grid, NT, 0, s>>>(a);
+      launch_tile<T, 32, 32, 2, 2>(a, nbatch, s);
     }
   }
-  TTG_CHECK_LAUNCH();
 }
 
 }  // namespace

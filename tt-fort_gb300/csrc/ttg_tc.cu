@@ -295,11 +295,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     if (!ok) {
       fail = 1;
       atomicExch(err, 1);
-      // let every copy that was issued land before the CTA can exit
+      // let every copy that was issued land before the CTA can exit: the
+      // copies read valid global memory and complete in microseconds, so
+      // these waits end long before their limit; a drain that still gives up
+      // is reported as its own error code (3)
+      bool drained = true;
       for (int c = 0; c < issued; ++c) {
         const int s = c % STAGES;
-        mbar_wait(smem_u32(&full_bar[s]), (uint32_t)((c / STAGES) & 1));
+        drained = mbar_wait(smem_u32(&full_bar[s]), (uint32_t)((c / STAGES) & 1)) && drained;
       }
+      if (!drained) atomicExch(err, 3);
     }
     mma_commit(smem_u32(&done_bar));
   }
