@@ -168,6 +168,126 @@ def matvec_roofline(torch, ctx, split=False, r=RMAX, nvec=B):
     return bfun3_flops(r, n, r, r, n, r, ra, ra) * nvec, dt
 
 
+def _timed(torch, fn):
+    """fn() bracketed by CUDA events on the current (library) stream."""
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    r = fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return r, e0.elapsed_time(e1) / 1e3
+
+
+def config_block(args, torch, ttgpu, ctx):
+    """The metric's other configurations, one timed run per method after a
+    warm-up, each with its error against FP64 and against an oracle sample:
+
+      ksl16  ztt_ksl, d=16, n=32, A = -(Dirichlet Laplacian) + rank-4
+             N(0, 0.01^2) TT-matrix, x0 rank 8 of norm 1, 200 steps of 1e-3;
+             oracle: 10 steps of the restatement against 10 PLAIN steps
+      amen10 dtt_amen_solve, d=10, n=64, Laplacian + Gaussian potential,
+             rhs rank 4, tol 1e-9, rmax 128, 20 sweeps; oracle: 6 sweeps of
+             the restatement against 6 PLAIN sweeps from the same start
+      xxz100 tt_eigb, XXZ d=100, delta=1, B=8, rmax 256, 2 sweeps per method
+             (a converged run takes minutes: bench.py --workload xxz100)
+    Differences of TT tensors are 2-norms of the difference tensor by QR
+    sweeps.  CPU legs run only without --no-cpu."""
+    from ttgpu.operators import (ksl_operator, random_tt_complex, tt_dot, tt_rel_diff,
+                                 amen_operator, random_tt, xxz_mpo)
+    out = {}
+    # ---- ksl16
+    d, nn = 16, 32
+    n_, m_, ra, crA = ksl_operator(d=d, n=nn, rank=4, std=0.01, seed=1)
+    _, ry, y = random_tt_complex(d, nn, 8, seed=2)
+    y = y.copy()
+    y[:ry[1] * nn] /= np.sqrt(tt_dot(d, n_, ry, y, ry, y).real)
+    res = {}
+    for meth in ("split", "plain"):
+        ttgpu.ztt_ksl(d, n_, m_, ra, crA, y, ry, 1e-3, 64, nsteps=2, method=meth, ctx=ctx)
+        (c, r), t = _timed(torch, lambda: ttgpu.ztt_ksl(d, n_, m_, ra, crA, y, ry, 1e-3, 64,
+                                                         nsteps=args.ksl_steps, method=meth,
+                                                         ctx=ctx))
+        res[meth] = {"cores": c, "ry": r, "time": t, "launches": ctx.stats()["launches"]}
+    sp, pl = res["split"], res["plain"]
+    e = {"workload": f"ztt_ksl d=16 n=32 ra=6 ry=8 tau=1e-3 nsteps={args.ksl_steps}",
+         "chosen_s": sp["time"], "plain_s": pl["time"], "plain_over_chosen": pl["time"] / sp["time"],
+         "gpu_launches": {"chosen": int(sp["launches"]), "plain": int(pl["launches"])},
+         "chosen_vs_fp64": tt_rel_diff(d, n_, sp["ry"], sp["cores"], pl["ry"], pl["cores"])}
+    if not args.no_cpu:
+        from oracle.ksl import ztt_ksl as oracle_ksl
+        c_, r_ = y, list(ry)
+        t0 = time.perf_counter()
+        for _ in range(10):
+            o = oracle_ksl(d, n_, m_, ra, crA, c_, r_, 1e-3, 64)
+            c_, r_ = o["cores"], o["ry"]
+        tc = time.perf_counter() - t0
+        g10, gr10 = ttgpu.ztt_ksl(d, n_, m_, ra, crA, y, ry, 1e-3, 64, nsteps=10, method="plain",
+                                  ctx=ctx)
+        s10, sr10 = ttgpu.ztt_ksl(d, n_, m_, ra, crA, y, ry, 1e-3, 64, nsteps=10, method="split",
+                                  ctx=ctx)
+        e["oracle_sample"] = {"steps": 10, "seconds": tc, "cores": os.cpu_count(),
+                              "plain_vs_oracle": tt_rel_diff(d, n_, gr10, g10, r_, c_),
+                              "chosen_vs_oracle": tt_rel_diff(d, n_, sr10, s10, r_, c_)}
+    out["ksl16"] = e
+    # ---- amen10
+    d, nn = 10, 64
+    n_, m_, ra, crA = amen_operator(d=d, n=nn)
+    _, ry, y = random_tt(d, nn, 4, seed=3)
+    _, rx, x0 = random_tt(d, nn, 2, seed=7)
+    res = {}
+    for meth in ("split", "plain"):
+        ttgpu.dtt_amen_solve(d, n_, m_, ry, ra, crA, y, x0, rx, 1e-9, rmax=128, nswp=2,
+                             method=meth, ctx=ctx)
+        (c, r), t = _timed(torch, lambda: ttgpu.dtt_amen_solve(d, n_, m_, ry, ra, crA, y, x0, rx,
+                                                                1e-9, rmax=128, nswp=20,
+                                                                method=meth, ctx=ctx))
+        st = ctx.stats()
+        res[meth] = {"cores": c, "rx": r, "time": t, "res": st["res"], "sweeps": st["sweeps"],
+                     "launches": st["launches"]}
+    sp, pl = res["split"], res["plain"]
+    e = {"workload": "dtt_amen_solve d=10 n=64 ra=3 ry=4 rx0=2 tol=1e-9 rmax=128 nswp=20",
+         "chosen_s": sp["time"], "plain_s": pl["time"], "plain_over_chosen": pl["time"] / sp["time"],
+         "sweeps": {"chosen": sp["sweeps"], "plain": pl["sweeps"]},
+         "local_residual_max": {"chosen": sp["res"], "plain": pl["res"]},
+         "max_rank": {"chosen": max(sp["rx"]), "plain": max(pl["rx"])},
+         "chosen_vs_fp64": tt_rel_diff(d, n_, sp["rx"], sp["cores"], pl["rx"], pl["cores"])}
+    if not args.no_cpu:
+        from oracle.amen import tt_amen_solve as oracle_amen
+        t0 = time.perf_counter()
+        o = oracle_amen(d, n_, ra, crA, ry, y, rx, x0, 1e-9, nswp=6)
+        tc = time.perf_counter() - t0
+        g6, gr6 = ttgpu.dtt_amen_solve(d, n_, m_, ry, ra, crA, y, x0, rx, 1e-9, rmax=128, nswp=6,
+                                       ctx=ctx)
+        e["oracle_sample"] = {"sweeps": 6, "seconds": tc, "cores": os.cpu_count(),
+                              "plain_vs_oracle": tt_rel_diff(d, n_, gr6, g6, o["rx"], o["cores"]),
+                              "same_ranks": list(gr6) == list(o["rx"])}
+    out["amen10"] = e
+    # ---- xxz100
+    if not args.no_xxz:
+        d, Bx = 100, 8
+        n_, m_, ra, crA = xxz_mpo(d, delta=1.0)
+        _, ry, cr = random_tt(d, 2, 16, last=Bx, seed=5)
+        res = {}
+        for meth in ("split", "plain"):
+            (lam, _, r), t = _timed(torch, lambda: ttgpu.tt_eigb(d, n_, m_, ra, crA, cr, ry, 1e-10,
+                                                                  256, Bx, nswp=2,
+                                                                  max_full_size=200, method=meth,
+                                                                  ctx=ctx))
+            res[meth] = {"lambda": np.asarray(lam), "time": t, "max_rank": max(r[:d]),
+                         "matvecs": ctx.stats()["matvecs"]}
+        sp, pl = res["split"], res["plain"]
+        out["xxz100"] = {
+            "workload": "tt_eigb xxz d=100 n=2 ra=5 delta=1 B=8 start_rank=16 rmax=256 eps=1e-10 "
+                        "nswp=2 max_full_size=200",
+            "chosen_s": sp["time"], "plain_s": pl["time"],
+            "plain_over_chosen": pl["time"] / sp["time"], "max_rank": int(sp["max_rank"]),
+            "matvecs": {"chosen": sp["matvecs"], "plain": pl["matvecs"]},
+            "chosen_vs_fp64_lambda": float(np.max(np.abs(sp["lambda"] - pl["lambda"]) /
+                                                  np.abs(pl["lambda"])))}
+    return out
+
+
 def run_reference(args):
     from oracle.eigb import tt_eigb as oracle_eigb
     n, m, ra, crA, ry, cr = workload()
@@ -221,9 +341,11 @@ def bench_extra(args, torch, ttgpu, ctx):
                 d, Bx = 100, 8
                 n, m, ra, crA = xxz_mpo(d, delta=1.0)
                 _, ry, cr = random_tt(d, 2, 16, last=Bx, seed=5)
-                lam, _, ry_out = ttgpu.tt_eigb(d, n, m, ra, crA, cr, ry, 1e-10, 256, Bx, nswp=2,
-                                               max_full_size=200, method=meth, ctx=ctx)
-                out = {"lambda": np.asarray(lam), "max_rank": max(ry_out[:d])}
+                lam, _, ry_out = ttgpu.tt_eigb(d, n, m, ra, crA, cr, ry, 1e-10, 256, Bx,
+                                               nswp=args.xxz_sweeps, max_full_size=200,
+                                               method=meth, ctx=ctx)
+                out = {"lambda": np.asarray(lam), "max_rank": max(ry_out[:d]),
+                       "sweeps": ctx.stats()["sweeps"], "res": ctx.stats()["res"]}
             elif args.workload == "ksl16":
                 d, nn, r = 16, 32, 8
                 n_, m_, ra, crA = ksl_operator(d=d, n=nn, rank=4, std=0.01, seed=1)
@@ -256,11 +378,14 @@ def bench_extra(args, torch, ttgpu, ctx):
         return
     sp, pl = res["split"], res["plain"]
     if args.workload == "xxz100":
-        metric = "tt_eigb time of 2 sweeps (d=100 XXZ, delta=1, B=8, rmax=256)"
+        ns = args.xxz_sweeps
+        metric = f"tt_eigb time to convergence, at most {ns} sweeps (d=100 XXZ, delta=1, B=8, rmax=256)"
         cfg = {"workload": "tt_eigb xxz d=100 n=2 ra=5 delta=1 B=8 start_rank=16 rmax=256 "
-                           "eps=1e-10 nswp=2 max_full_size=200"}
+                           f"eps=1e-10 nswp={ns} max_full_size=200"}
         agree = float(np.max(np.abs(sp["lambda"] - pl["lambda"]) / np.abs(pl["lambda"])))
-        extra = {"lambda_maxrel_vs_plain": agree, "lambda": sp["lambda"].tolist()}
+        extra = {"lambda_maxrel_vs_plain": agree, "lambda": sp["lambda"].tolist(),
+                 "sweeps": {"split": sp["sweeps"], "plain": pl["sweeps"]},
+                 "res": {"split": sp["res"], "plain": pl["res"]}}
     elif args.workload == "ksl16":
         ns = args.ksl_steps
         metric = f"ztt_ksl time of {ns} steps (d=16, n=32, -Laplacian + rank-4 N(0,0.01^2), rank 8)"
@@ -317,6 +442,12 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--methods", default="split,plain",
                     help="larger workloads: the methods to time (one method: profiling runs)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the block of the metric's other configurations")
+    ap.add_argument("--no-xxz", action="store_true",
+                    help="leave the d=100 XXZ entry out of that block")
+    ap.add_argument("--xxz-sweeps", type=int, default=20,
+                    help="sweep cap of the xxz100 workload (the reference's default nswp)")
     ap.add_argument("--ksl-steps", type=int, default=200,
                     help="ksl16: time steps (the workload is 200)")
     ap.add_argument("--workload", default="heisenberg20",
@@ -389,6 +520,16 @@ def main():
         plain = {"value": tp, "unit": "s", "e2e": twp, "gpu_launches": int(lp),
                  "matvecs": stp["matvecs"], "plain_over_chosen": tp / t,
                  "lambda_maxrel_vs_chosen": float(np.max(np.abs(lam_p - lam) / np.abs(lam_p)))}
+    ablation = None
+    if meth == "split" and not args.no_plain:
+        # the chosen method's local solver (Jacobi-Davidson + CG) on FP64
+        # products: what split precision buys beyond the algorithm
+        solve("jd64")
+        tj, twj, lj, (lam_j, _, _), stj = timed("jd64", 1)
+        ablation = {"jd64": {"value": tj, "unit": "s", "matvecs": stj["matvecs"],
+                             "gpu_launches": int(lj), "jd64_over_chosen": tj / t,
+                             "lambda_maxrel_vs_chosen":
+                                 float(np.max(np.abs(lam_j - lam) / np.abs(lam_j)))}}
     if rank != 0:
         return
     peaks, kind = measured_peaks()
@@ -408,6 +549,7 @@ def main():
         big = {"kernel": "local matvec r=256 n=2 ra=5 block 8 (the d=100 XXZ local size)",
                "achieved": flb / dtb / 1e12, "bf16_issued": 3 * flb / dtb / 1e12,
                "frac": flb / dtb / 1e12 / peak, "launch_us": dtb * 1e6}
+    configs = None if args.no_configs else config_block(args, torch, ttgpu, ctx)
     h2d = (len(crA) + len(cr)) * 8 + (len(n) * 3 + 2 * len(ry)) * 8
     d2h = len(cores) * 8 + B * 8
     cpu = None
@@ -435,7 +577,8 @@ def main():
                          "traffic_source": (SPLIT_MV_TRAFFIC_NOTE if split else None),
                          "peak_source": peak_note,
                          "launch_us": dt * 1e6, "flops_per_launch": fl, "large_local": big},
-            "clocks": clk.summary(), "cpu_baseline": cpu, "plain": plain,
+            "clocks": clk.summary(), "cpu_baseline": cpu, "plain": plain, "ablation": ablation,
+            "configs": configs,
             "solve": {"lambda": lam.tolist(), "matvecs": st["matvecs"], "sweeps": st["sweeps"],
                       "max_rank": max(ry_out[:D])}}
     print(json.dumps(line))

@@ -45,8 +45,12 @@ enum {
 
 enum {
   TTG_METHOD_PLAIN = 0,     /* FP64 contractions, the reference's arithmetic */
-  TTG_METHOD_SPLIT = 1      /* BF16x3 tensor-core contractions, FP32 accumulate,
+  TTG_METHOD_SPLIT = 1,     /* BF16x3 tensor-core contractions, FP32 accumulate,
                                FP64 Rayleigh-Ritz / QR / SVD / Pade          */
+  TTG_METHOD_JD64 = 2       /* ttg_eigb only: the SPLIT method's local solver
+                               (Jacobi-Davidson with CG corrections) on FP64
+                               contractions; separates what the algorithm
+                               gains from what split precision gains        */
 };
 
 /* ---------------------------------------------------------------- context */
@@ -92,6 +96,22 @@ int ttg_dbfun3_noalloc(ttg_ctx* ctx, ttg_int rx1, ttg_int m, ttg_int rx2, ttg_in
                        ttg_int n, ttg_int ry2, ttg_int ra1, ttg_int ra2, const double* phi1,
                        const double* A, const double* phi2, const double* x, double* y,
                        ttg_int nvec);
+/* Local eigensolve of tt_eigb (the dprimme call of tt_eigb.f90:252-283):
+ * lowest B eigenpairs of y = Phi1 A Phi2 x on the square local problem
+ * (r1, n, r2), operator ranks ra1, ra2, device operands.  X (device,
+ * N x B, N = r1 n r2) holds the start block (initSize = B) on entry and the
+ * Ritz vectors on return; lambda (host, B) the eigenvalues; res (host,
+ * optional) the 2-norm of the B residual norms; matvecs (optional) the
+ * matvec count.  tol is PRIMME's eps (residual relative to the operator's
+ * largest Ritz value magnitude), max_matvecs its maxMatvecs (<= 0: 500).
+ * method PLAIN: block GD+k Davidson with FP64 matvecs; SPLIT: Jacobi-Davidson
+ * with BF16x3 tensor-core corrections judged by FP64 residuals; JD64: the
+ * SPLIT solver on FP64 matvecs.  A capped solve is counted (ttg_capped) or,
+ * with strict limits, returns TTG_ERR_NOCONV. */
+int ttg_local_eig(ttg_ctx* ctx, ttg_int r1, ttg_int n, ttg_int r2, ttg_int ra1, ttg_int ra2,
+                  const double* phi1, const double* A, const double* phi2, double* X, ttg_int B,
+                  double tol, ttg_int max_matvecs, int method, double* lambda, double* res,
+                  ttg_int* matvecs);
 /* Prepared local operator: the GPU counterpart of init_bfun_sizes +
  * init_bfun_main + primme_matvec (tt_eigb.f90:15-49, tt_ksl.f90:1-84).
  * create() binds Phi1, A, Phi2 (device pointers, kept by reference) for up to
@@ -157,6 +177,34 @@ int ttg_djac_gen(ttg_ctx* ctx, char ptype, ttg_int rx1, ttg_int n, ttg_int rx2, 
 int ttg_djac_apply(ttg_ctx* ctx, char ptype, ttg_int rx1, ttg_int n, ttg_int rx2,
                    const double* jacs, const double* x, double* y);
 
+/* ------------------------------- reference-named by-reference entry points
+ * The bind(c) kernels of tt_linalg.f90 under their own names and argument
+ * lists, for C and Fortran callers that bind them directly (gmres_3d.c:3-4
+ * declares dbfun3 and djac_apply this way and links against them unchanged).
+ * All sizes are 64-bit (`long`, the i8 presets) and all arrays are HOST
+ * arrays: each call copies its inputs to the device, runs the ttg_* kernel on
+ * a per-thread context (device $TTG_DEVICE, default 0) and copies the result
+ * back.  The workspace arguments of the Fortran interfaces are accepted and
+ * not used.  These routines return nothing, like the reference's; a failed
+ * call prints one line to stderr, fills its output with NaN and sets the
+ * status that ttg_fshim_status() returns (and clears). */
+/* y = Phi1 A Phi2 x, dbfun3 tt_linalg.f90:127-159; x and y may be one array */
+void dbfun3(long* rx1, long* m, long* rx2, long* ry1, long* n, long* ry2, long* ra1, long* ra2,
+            double* phi1, double* A, double* phi2, double* x, double* y, double* res1,
+            double* res2);
+/* block-Jacobi blocks, djac_gen tt_linalg.f90:363-494 */
+void djac_gen(char* ptype, long* rx1, long* n, long* rx2, long* ra1, long* ra2, double* Phi1,
+              double* A, double* Phi2, double* jacs);
+/* y = P x, djac_apply tt_linalg.f90:497-531; x and y may be one array */
+void djac_apply(char* ptype, long* rx1, long* n, long* rx2, double* jacs, double* x, double* y,
+                double* work1);
+/* Householder QR, dqr tt_linalg.f90:30-52: Q overwrites A (n x min(n, m)),
+ * R is min(n, m) x m */
+void dqr(long* n, long* m, double* A, double* R, double* work, long* lwork, double* tau);
+/* status of the last failed by-reference call on this thread (TTG_OK if
+ * none), cleared by the call */
+int ttg_fshim_status(void);
+
 /* ------------------------------------------------ TT files (host) */
 /* The reference's binary TT format (.sdv): dtt_write / ztt_write and
  * dtt_read / ztt_read, ttio.f90:29-399.  Host arrays; cores back to back,
@@ -195,7 +243,9 @@ int ttg_dmaxvol(ttg_ctx* ctx, ttg_int n, ttg_int r, const double* A, ttg_int* p,
 /* ------------------------------------------- learned preconditioner (new) */
 /* No counterpart in the reference: PRIMME's applyPreconditioner hook is left
  * unset by tt_eigb (primme/primme.h:144-145, tt_eigb.f90:252-283).  A ReLU MLP
- * (3 features -> depth x width -> 1, FP32) corrects the classical diagonal
+ * (3 features -> depth x width -> 1; layer products in BF16 on the tensor
+ * cores with FP32 accumulation, or FP32, see ttg_mlp_set_precision; FP32
+ * parameters, activations and Adam state) corrects the classical diagonal
  * Davidson preconditioner of the plain method's local solves; it is trained
  * on local problems that the sweeps record.  Parameters are one flat float
  * array, layer by layer: W_l (in x out, row-major) then b_l. */
@@ -214,6 +264,13 @@ int ttg_mlp_forward(ttg_mlp* mlp, ttg_int P, const float* F, float* h);
 int ttg_mlp_loss_grad(ttg_mlp* mlp, ttg_int N, ttg_int B, const double* D, const double* theta,
                       const double* X, const double* R, const double* V, double* loss);
 int ttg_mlp_adam_step(ttg_mlp* mlp, double lr);
+/* layer products of the forward and backward passes: bf16 = 1 (the default)
+ * runs them in BF16 on the tensor cores (tcgen05, FP32 accumulate), 0 in
+ * FP32 on the CUDA cores */
+int ttg_mlp_set_precision(ttg_mlp* mlp, int bf16);
+/* TTG_ERR_CUDA when a tensor-core product of the network gave up waiting on
+ * its bounded mbarrier waits (synchronises the network's stream) */
+int ttg_mlp_check(ttg_mlp* mlp);
 /* mode bit 0: precondition the plain method's Davidson expansions with mlp;
  * bit 1: record every iterative local problem of the plain method */
 int ttg_set_learned(ttg_ctx* ctx, ttg_mlp* mlp, int mode);
@@ -324,6 +381,19 @@ int ttg_free_result(ttg_ctx* ctx);      /* deallocate_result tt_eigb.f90:60-64 *
 /* counters of the last driver call: total local matvecs, sweeps, residual */
 int ttg_stats(const ttg_ctx* ctx, ttg_int* matvecs, ttg_int* sweeps, double* res,
               ttg_int* launches);
+/* Iteration caps of the local solvers, for the next driver calls on ctx.
+ * max_matvecs: matvec budget of each local eigensolve (PRIMME's maxMatvecs,
+ * 500, tt_eigb.f90:152,269); max_expokit_steps: integration steps of each
+ * Krylov exponential (mxstep of ZGEXPV, 500, expokit.f:2506); 0 keeps the
+ * reference's value.  The reference tolerates a reached cap (PRIMME returns
+ * -3, Expokit sets iflag = 1, its GMRES stops after nrestart x niters, and the
+ * sweep goes on, tt_eigb.f90:285-288, explib.f90:108-111): so does the library
+ * with strict = 0, counting such local solves (ttg_capped).  With strict = 1
+ * the first capped local solve ends the driver call with TTG_ERR_NOCONV. */
+int ttg_set_limits(ttg_ctx* ctx, ttg_int max_matvecs, ttg_int max_expokit_steps, int strict);
+/* local solves of the last driver call that stopped at an iteration cap
+ * before reaching their tolerance (-1 for a null context) */
+ttg_int ttg_capped(const ttg_ctx* ctx);
 /* kernel launches issued by the library since it was loaded (all contexts) */
 ttg_int ttg_launch_count(void);
 

@@ -25,8 +25,10 @@ from .davidson import davidson
 
 
 def local_eig(rx1, n, rx2, ra1, ra2, phi1, A, phi2, X0, B, tol, max_full_size, maxmv=500,
-              maxb=None):
-    """Lowest B eigenpairs of the local operator; returns (lam, V, res, nmv)."""
+              maxb=None, local_solver=None):
+    """Lowest B eigenpairs of the local operator; returns (lam, V, res, nmv).
+    local_solver (optional): (mv, X0, B, tol, max_matvecs) -> (lam, V, res,
+    nmv) in place of oracle/davidson.py, e.g. oracle/primme.py's PRIMME."""
     N = rx1 * n * rx2
     if N < max_full_size:
         H = fullmat(rx1, n, rx2, ra1, ra2, phi1, A, phi2)
@@ -40,18 +42,23 @@ def local_eig(rx1, n, rx2, ra1, ra2, phi1, A, phi2, X0, B, tol, max_full_size, m
         out = bfun3_block(rx1, n, rx2, rx1, n, rx2, ra1, ra2, phi1, A, phi2, flat(X), X.shape[1])
         return F(out, N, X.shape[1])
 
+    if local_solver is not None:
+        return local_solver(mv, np.array(X0, copy=True), B, tol, maxmv)
     lam, V, rn, nmv, _ = davidson(mv, np.array(X0, copy=True), B, tol, maxb=maxb,
                                   max_matvecs=maxmv)
     return lam, V, float(np.linalg.norm(rn)), nmv
 
 
 def tt_eigb(d, n, m, ra, crA, crY0, ry, eps, rmax, B, nswp=20, max_full_size=2000,
-            verb=0, resid_damp=10.0):
+            verb=0, resid_damp=10.0, local_solver=None, record=None):
     """Restatement of ``tt_eigb`` (tt_eigb.f90:110).
 
     Arguments follow the Fortran signature with 0-based Python lists.  Returns
     a dict with ``lambda`` (B,), ``cores`` (flat, result_core layout), ``ry``
     (d+1, ry[d] = B), ``sweeps``, ``matvecs`` and the last local residual.
+    local_solver replaces the iterative local eigensolver (see local_eig);
+    record (a list) receives every iterative local problem as a dict
+    (dims, phi1, A, phi2, X0, tol) before it is solved.
     """
     n = list(map(int, n)); m = list(map(int, m)); ra = list(map(int, ra))
     ry = list(map(int, ry))
@@ -91,8 +98,13 @@ def tt_eigb(d, n, m, ra, crA, crY0, ry, eps, rmax, B, nswp=20, max_full_size=200
     while swp <= nswp:
         N = ry[i] * n[i] * ry[i + 1]
         X0 = F(cr[i][:N * B], N, B)
+        if record is not None and N >= max_full_size:
+            record.append({"dims": (ry[i], n[i], ry[i + 1], ra[i], ra[i + 1]),
+                           "phi1": phi[i].copy(), "A": Acore[i].copy(), "phi2": phi[i + 1].copy(),
+                           "X0": X0.copy(), "tol": eps2 / resid_damp})
         lam, V, res, nmv = local_eig(ry[i], n[i], ry[i + 1], ra[i], ra[i + 1], phi[i], Acore[i],
-                                     phi[i + 1], X0, B, eps2 / resid_damp, max_full_size)
+                                     phi[i + 1], X0, B, eps2 / resid_damp, max_full_size,
+                                     local_solver=local_solver)
         curcr = flat(V)
         fv = float(np.sum(lam))
         erloc = (fvold - fv) / abs(fv)

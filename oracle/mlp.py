@@ -70,15 +70,33 @@ def flatten(grads):
     return np.concatenate([np.concatenate([gW.ravel(), gb.ravel()]) for gW, gb in grads])
 
 
-def forward(params, Fx):
+def to_bf16(x):
+    """float32 values rounded to the nearest bfloat16 (ties to even), as
+    float32 -- the rounding of __float2bfloat16_rn on finite values."""
+    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32)
+
+
+def _mm(a, b, bf16):
+    """a @ b in float64 on operands rounded to bf16 (bf16=True, the library's
+    tensor-core products: exact bf16 products summed in FP32), or as given."""
+    if not bf16:
+        return a @ b
+    return (to_bf16(a).astype(np.float64) @ to_bf16(b).astype(np.float64)).astype(np.float32)
+
+
+def forward(params, Fx, bf16=False):
     """Network output (P,) and the layer inputs/outputs, in the parameters'
-    precision (float32 as on the device; float64 for derivative checks)."""
+    precision (float32 as on the device; float64 for derivative checks).
+    bf16=True rounds both operands of every layer product to bf16, as the
+    tensor-core path does."""
     dt = params[0][0].dtype
     acts = [np.asarray(Fx, dtype=dt)]
     h = acts[0]
     L = len(params)
     for l, (W, b) in enumerate(params):
-        z = h @ W + b
+        z = _mm(h, W, bf16) + b
         h = (np.maximum(z, 0.0) if l < L - 1 else z).astype(dt)
         acts.append(h)
     return acts[-1][:, 0], acts
@@ -121,12 +139,14 @@ def apply_prec(flat, dims, D, theta, R):
     return np.where(np.isfinite(T), T, R)
 
 
-def loss_grad(flat, dims, D, theta, X, R, V):
-    """Loss of one recorded problem and the flat parameter gradient."""
+def loss_grad(flat, dims, D, theta, X, R, V, bf16=False):
+    """Loss of one recorded problem and the flat parameter gradient (bf16:
+    every layer product of the forward and backward passes on bf16-rounded
+    operands, as the tensor-core path computes them)."""
     params = unflatten(flat, dims)
     N, B = X.shape
     F, base = features(D, theta, R)
-    h, acts = forward(params, F)
+    h, acts = forward(params, F, bf16)
     u = (base * (1.0 + h.astype(np.float64))).reshape(B, N).T
     u = u - X @ (X.T @ u)
     uu = np.sum(u * u, axis=0)
@@ -143,9 +163,9 @@ def loss_grad(flat, dims, D, theta, X, R, V):
     for l in range(len(params) - 1, -1, -1):
         W, b = params[l]
         a = acts[l]
-        grads[l] = (a.T @ gz, gz.sum(axis=0))
+        grads[l] = (_mm(a.T, gz, bf16), gz.sum(axis=0))
         if l > 0:
-            gz = (gz @ W.T) * (acts[l] > 0)
+            gz = _mm(gz, W.T, bf16) * (acts[l] > 0)
     return loss, flatten(grads)
 
 

@@ -13,7 +13,9 @@ from oracle import ops
 def _declared():
     txt = open(os.path.join(ROOT, "include", "ttgpu.h")).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(ttg_[a-z0-9_]+)\s*\(", txt)))
+    # ttg_* entry points and the reference-named by-reference kernels
+    pat = r"\b(ttg_[a-z0-9_]+|dbfun3|djac_gen|djac_apply|dqr)\s*\("
+    return sorted(set(re.findall(pat, txt)))
 
 
 @pytest.fixture(scope="module")

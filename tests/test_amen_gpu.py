@@ -85,3 +85,25 @@ def test_amen_workload_family(ctx):
     assert st["sweeps"] == ref["sweeps"]
     assert abs(st["res"] - ref["res_max"]) <= 1e-3 * ref["res_max"]
     assert tt_rel_diff(nn, rx1, cores, ref["rx"], ref["cores"]) < 1e-6
+
+
+def test_amen_config_size_six_sweeps(ctx):
+    """The AMEn workload at its configured size: d=10, n=64, Laplacian +
+    exp(-|i-c|^2/sigma^2) (rank 3), rhs rank 4, tol 1e-9, ranks up to 128.
+    The oracle needs minutes to converge at these ranks, so both run six
+    sweeps from the same start (ranks reach 26) and the states must agree:
+    same ranks, same sweep count, same largest local residual, same iterate."""
+    import ttgpu
+    from ttgpu.operators import tt_rel_diff as qr_rel_diff
+    d, n, tol, nswp = 10, 64, 1e-9, 6
+    nn, mm, ra, crA = amen_operator(d=d, n=n)
+    _, ry, y = random_tt(d, n, 4, seed=3)
+    _, rx, x0 = random_tt(d, n, 2, seed=7)
+    cores, rx1 = ttgpu.dtt_amen_solve(d, nn, mm, ry, ra, crA, y, x0, rx, tol, rmax=128,
+                                      nswp=nswp, ctx=ctx)
+    st = ctx.stats()
+    ref = oracle_amen(d, nn, ra, crA, ry, y, rx, x0, tol, nswp=nswp)
+    assert rx1 == ref["rx"]
+    assert st["sweeps"] == ref["sweeps"]
+    assert abs(st["res"] - ref["res_max"]) <= 1e-3 * ref["res_max"]
+    assert qr_rel_diff(d, nn, rx1, cores, ref["rx"], ref["cores"]) < 1e-6

@@ -103,3 +103,44 @@ def test_eigb_plain_is_bit_reproducible(ctx):
     assert r0 == r1
     assert np.array_equal(np.asarray(l0), np.asarray(l1))
     assert np.array_equal(np.asarray(c0), np.asarray(c1))
+
+
+def test_eigb_heisen20_matches_primme_sweep(ctx):
+    """The d=20 Heisenberg workload against the sweep whose local eigensolver
+    is the reference's own PRIMME (GD+k pinned, tt_eigb's settings;
+    tests/golden/make_primme_golden.py): same number of sweeps, same ranks,
+    eigenvalues to 1e-10 relative."""
+    import ttgpu
+    f = np.load(os.path.join(GOLDEN, "heisen20_sdv.npz"))
+    g = json.load(open(os.path.join(GOLDEN, "eigb_heisen20_primme.json")))["GD_plusK"]
+    d, B = 20, 5
+    r = [int(v) for v in f["r"]]
+    n = [2] * d
+    _, ry, cr = random_tt(d, 2, 16, last=B, seed=0)
+    lam, _, ry_out = ttgpu.tt_eigb(d, n, n, r, f["cores"], cr, ry, 1e-8, 64, B, nswp=20,
+                                   max_full_size=200, ctx=ctx)
+    assert ctx.stats()["sweeps"] == g["sweeps"]
+    assert list(ry_out) == g["ry"]
+    assert np.allclose(lam, g["lambda"], rtol=1e-10, atol=0)
+
+
+@pytest.mark.parametrize("method", ["plain", "split", "jd64"])
+def test_local_eig_matches_primme(ctx, torch_cuda, method):
+    """Local problems recorded from that PRIMME sweep (the largest, N = 8192,
+    and one of N = 4096), solved from the same start by the library's local
+    eigensolver (ttg_local_eig): PRIMME's eigenvalues to 1e-10 relative."""
+    import ttgpu
+    torch = torch_cuda
+    z = np.load(os.path.join(GOLDEN, "primme_local_heisen20.npz"))
+    for q in range(2):
+        r1, nn, r2, ra1, ra2 = (int(v) for v in z[f"p{q}_dims"])
+        lam_ref, tol = z[f"p{q}_lambda"], float(z[f"p{q}_tol"])
+        B = lam_ref.size
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+        X = dev(z[f"p{q}_X0"])
+        lam, res, nmv = ttgpu.local_eig(r1, nn, r2, ra1, ra2, dev(z[f"p{q}_phi1"]),
+                                        dev(z[f"p{q}_A"]), dev(z[f"p{q}_phi2"]), X, B, tol,
+                                        method=method, ctx=ctx)
+        assert ctx.capped() == 0
+        assert np.max(np.abs(lam - lam_ref) / np.abs(lam_ref)) < 1e-10
+        assert nmv > 0

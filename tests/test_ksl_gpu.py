@@ -271,3 +271,26 @@ def test_tt_ksl_real_ragged_modes_and_rank_cut(ctx):
         c, rr = out["cores"], out["ry"]
     assert ry1 == rr == [1, 2, 3, 2, 1]
     assert _rel(tt_full(4, n, ry1, cores), tt_full(4, n, rr, c)) < 1e-8
+
+
+def test_ksl_config_size_plain_vs_oracle(ctx):
+    """The KSL workload at its configured size: d=16, n=32, A = -(Dirichlet
+    Laplacian) + random rank-4 TT-matrix with N(0, 0.01^2) entries (operator
+    rank 6), x0 a random rank-8 TT vector of norm 1, tau = 1e-3; 10 steps of
+    the PLAIN (FP64) method against 10 oracle steps.  The 2-norm of the
+    difference tensor is taken by QR sweeps (resolves far below 1e-8).  Bar:
+    1e-8 relative, the KSL state tolerance of the reference's Expokit."""
+    import ttgpu
+    from ttgpu.operators import tt_dot, tt_rel_diff
+    d, nn, r, tau, steps = 16, 32, 8, 1e-3, 10
+    n_, m_, ra, crA = ksl_operator(d=d, n=nn, rank=4, std=0.01, seed=1)
+    _, ry, y = random_tt_complex(d, nn, r, seed=2)
+    y = y.copy()
+    y[:ry[1] * nn] /= np.sqrt(tt_dot(d, n_, ry, y, ry, y).real)
+    cores, ry1 = ttgpu.ztt_ksl(d, n_, m_, ra, crA, y, ry, tau, 64, nsteps=steps, ctx=ctx)
+    c, rr = y, list(ry)
+    for _ in range(steps):
+        out = oracle_ksl(d, n_, m_, ra, crA, c, rr, tau, 64)
+        c, rr = out["cores"], out["ry"]
+    assert ry1 == rr
+    assert tt_rel_diff(d, n_, ry1, cores, rr, c) < 1e-8

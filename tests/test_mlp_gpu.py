@@ -2,9 +2,13 @@
 parameter gradients of the hand-written kernels against the oracle, and the
 gain of the trained network on a held-out chain.
 
-Tolerances: FP32 network, so the forward output to 1e-5 relative and the
-flat gradient to 1e-4 relative (atomic accumulation in the weight and bias
-gradients reorders FP32 sums).  The eigenvalues of the preconditioned solve
+Tolerances: with FP32 layer products the forward output to 1e-5 relative and
+the flat gradient to 1e-4 relative (atomic accumulation in the bias
+gradients reorders FP32 sums).  With the BF16 tensor-core products (the
+default) the oracle rounds the same operands to bf16 before every product;
+what remains is FP32 summation order, which now and then moves an
+activation across a bf16 rounding boundary before the next layer (a 2^-8
+change of that element): forward 5e-4, loss 1e-4, gradient 2e-3.  The eigenvalues of the preconditioned solve
 to 1e-10 relative of the plain solve: both meet the same FP64 residual test
 with exact ranks."""
 import numpy as np
@@ -37,38 +41,48 @@ def _params(width, depth, seed):
     return flat, dims
 
 
-def test_mlp_forward_matches_oracle(torch_cuda, ctx):
+TOL = {False: (1e-5, 1e-5, 1e-4), True: (5e-4, 1e-4, 2e-3)}   # forward, loss, gradient
+
+
+@pytest.mark.parametrize("bf16", [True, False])
+@pytest.mark.parametrize("width", [64, 512])
+def test_mlp_forward_matches_oracle(torch_cuda, ctx, bf16, width):
     import ttgpu
     torch = torch_cuda
-    net = ttgpu.LearnedPrec(width=64, depth=3, seed=2, ctx=ctx)
-    assert np.array_equal(net.get_params(), M.init_params(64, 3, 2))
-    flat, dims = _params(64, 3, 2)
+    net = ttgpu.LearnedPrec(width=width, depth=3, seed=2, ctx=ctx)
+    net.set_precision(bf16)
+    assert np.array_equal(net.get_params(), M.init_params(width, 3, 2))
+    flat, dims = _params(width, 3, 2)
     net.set_params(flat)
     P = 5000
     F = np.random.default_rng(3).standard_normal((P, M.NFEAT)).astype(np.float32)
     h = torch.empty(P, dtype=torch.float32, device="cuda")
     net.forward(P, torch.from_numpy(F).cuda(), h)
     ctx.synchronize()
-    ref, _ = M.forward(M.unflatten(flat, dims), F)
+    net.check()
+    ref, _ = M.forward(M.unflatten(flat, dims), F, bf16=bf16)
     got = h.cpu().numpy()
-    assert np.linalg.norm(got - ref) <= 1e-5 * np.linalg.norm(ref)
+    assert np.linalg.norm(got - ref) <= TOL[bf16][0] * np.linalg.norm(ref)
     net.close()
 
 
-@pytest.mark.parametrize("N,B", [(500, 4), (2048, 5)])
-def test_mlp_gradient_matches_oracle(torch_cuda, ctx, N, B):
+@pytest.mark.parametrize("bf16", [True, False])
+@pytest.mark.parametrize("N,B,width", [(500, 4, 64), (2048, 5, 64), (4096, 8, 512)])
+def test_mlp_gradient_matches_oracle(torch_cuda, ctx, N, B, width, bf16):
     import ttgpu
     torch = torch_cuda
-    net = ttgpu.LearnedPrec(width=64, depth=3, seed=4, ctx=ctx)
-    flat, dims = _params(64, 3, 4)
+    net = ttgpu.LearnedPrec(width=width, depth=3, seed=4, ctx=ctx)
+    net.set_precision(bf16)
+    flat, dims = _params(width, 3, 4)
     net.set_params(flat)
     D, theta, X, R, V = _problem(N, B, seed=N)
     t = lambda a: torch.from_numpy(np.asfortranarray(a).ravel(order="F")).cuda()
     loss = net.loss_grad(N, B, t(D), t(theta), t(X), t(R), t(V))
+    net.check()
     g = net.get_grads()
-    loss_ref, g_ref = M.loss_grad(flat, dims, D, theta, X, R, V)
-    assert abs(loss - loss_ref) <= 1e-5 * max(1e-12, abs(loss_ref))
-    assert np.linalg.norm(g - g_ref) <= 1e-4 * np.linalg.norm(g_ref)
+    loss_ref, g_ref = M.loss_grad(flat, dims, D, theta, X, R, V, bf16=bf16)
+    assert abs(loss - loss_ref) <= TOL[bf16][1] * max(1e-12, abs(loss_ref))
+    assert np.linalg.norm(g - g_ref) <= TOL[bf16][2] * np.linalg.norm(g_ref)
     net.close()
 
 

@@ -22,6 +22,15 @@ SHAPES = [
     (8, 32, 8, 8, 32, 8, 6, 6, 1),          # KSL-like
     (32, 64, 24, 32, 64, 24, 3, 3, 1),      # AMEn-like n = 64
     (256, 2, 256, 256, 2, 256, 5, 5, 8),    # the d=100 XXZ local problem (r = 256, B = 8)
+    # single-launch fused path (rx1*m <= 128, rx2 <= 64, ry1 <= 128, n == m,
+    # small core): ragged blocks of c2 and K tiles, boundary cores, m = 4 and
+    # m = 1 with eight K tiles of GEMM3 (narrow-tile plan)
+    (37, 2, 50, 45, 2, 61, 5, 5, 3),
+    (64, 2, 64, 64, 2, 64, 1, 5, 2),        # left boundary core (ra1 = 1)
+    (64, 2, 64, 64, 2, 64, 5, 1, 2),        # right boundary core (ra2 = 1)
+    (32, 4, 16, 40, 4, 16, 2, 3, 2),
+    (64, 1, 64, 100, 1, 64, 8, 8, 4),
+    (60, 2, 33, 128, 2, 20, 3, 4, 9),
 ]
 
 

@@ -230,8 +230,10 @@ struct GmresBufs {
 // Gram-Schmidt applied twice; stops when |residual| / |b| < tol (the
 // Householder GMRES of the reference minimises the same residual over the
 // same Krylov space, ttlocsolve.f90:509-682, tt_linalg.f90:651-845).
+// Returns whether the residual reached tol (false: stopped after iters
+// restarts, which the reference tolerates).
 template <class MV>
-void gmres_cgs2(const MV& mv, i64 N, const double* b, double* x, double tol, int nr, int iters,
+bool gmres_cgs2(const MV& mv, i64 N, const double* b, double* x, double tol, int nr, int iters,
                 const GmresBufs& G, cudaStream_t s) {
   double* H = G.gm;                    // Hessenberg column (first pass)
   double* H2 = G.gm + 64;              // second Gram-Schmidt pass
@@ -258,7 +260,7 @@ void gmres_cgs2(const MV& mv, i64 N, const double* b, double* x, double tol, int
     sync();
     const double beta = std::sqrt(h[0]);
     if (it == 0) nrmb = beta;
-    if (beta == 0.0) break;
+    if (beta == 0.0) return true;
     TTG_CUDA(cudaMemcpyAsync(V, G.w, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
     h[1] = 1.0 / beta;
     TTG_CUDA(cudaMemcpyAsync(red + 8, h + 1, sizeof(double), cudaMemcpyHostToDevice, s));
@@ -309,8 +311,18 @@ void gmres_cgs2(const MV& mv, i64 N, const double* b, double* x, double tol, int
     trsv_kernel<<<1, 1, 0, s>>>(jdone, Rm, ldr, g, y);
     TTG_CHECK_LAUNCH();
     gemm_nn_small(N, 1, jdone, V, N, y, jdone, x, N, 1.0, 1.0, s);
-    if (curres < tol) break;
+    if (curres < tol) return true;
   }
+  return false;
+}
+
+// a local solve that stopped at its iteration cap: counted, or an error when
+// the context asks for strict caps
+void note_capped(ttg_ctx* ctx, const char* who) {
+  ++ctx->stat_capped;
+  if (ctx->strict)
+    throw Error{TTG_ERR_NOCONV, std::string(who) +
+                                    ": local GMRES reached its restart cap before its tolerance"};
 }
 
 }  // namespace
@@ -337,12 +349,15 @@ struct AmenOut {
 
 class AmenSolver {
  public:
-  AmenSolver(ttg_ctx* ctx, const AmenParams& P) : P_(P), s_(ctx->stream) {}
+  AmenSolver(ttg_ctx* ctx, const AmenParams& P) : P_(P), s_(ctx->stream), ctx_(ctx) {
+    ctx->stat_capped = 0;
+  }
   void run(AmenOut& out);
 
  private:
   AmenParams P_;
   cudaStream_t s_;
+  ttg_ctx* ctx_;
   Arena mem_;
   DevTT x_, y_, z_;
   std::vector<double*> A_;
@@ -459,7 +474,8 @@ void AmenSolver::gmres(const LocalDims& L, int k, const double* b, double* x, do
   const double* p1 = pxax_[k];
   const double* p2 = pxax_[k + 1];
   auto mv = [&](const double* in, double* out, int nv) { local_mv(L, p1, p2, k, in, out, nv); };
-  gmres_cgs2(mv, N, b, x, tol, nr, P_.local_iters, GmresBufs{V_, w_, gm_, red_, h_}, s_);
+  if (!gmres_cgs2(mv, N, b, x, tol, nr, P_.local_iters, GmresBufs{V_, w_, gm_, red_, h_}, s_))
+    note_capped(ctx_, "dtt_amen_solve");
 }
 
 
@@ -491,6 +507,7 @@ void AmenSolver::gmres_split(const LocalDims& L, int k, const double* b, double*
     nrr = norm2(ir_r_, N);
   }
   split_matvec_check(s_);
+  if (nrr > tol * nb) note_capped(ctx_, "dtt_amen_solve");
 }
 
 // dtt_trunc dir=+1 with the residual criterion (ttnodeop.f90:227-302)
@@ -1010,12 +1027,15 @@ struct GrowBuf {
 
 class AlsSolver {
  public:
-  AlsSolver(ttg_ctx* ctx, const AlsParams& P) : P_(P), s_(ctx->stream) {}
+  AlsSolver(ttg_ctx* ctx, const AlsParams& P) : P_(P), s_(ctx->stream), ctx_(ctx) {
+    ctx->stat_capped = 0;
+  }
   void run(AmenOut& out);
 
  private:
   AlsParams P_;
   cudaStream_t s_;
+  ttg_ctx* ctx_;
   Arena mem_;
   std::vector<i64> n_, rx_, cap_;
   std::vector<double*> x_, A_, Y_, phiA_, phiy_;
@@ -1286,12 +1306,14 @@ void AlsSolver::run(AmenOut& out) {
           jac_apply_f64(pt, r1, nk_, r2, jacs, in, cand_, nv, s_);
           mv(i, cand_, o, nv);
         };
-        gmres_cgs2(mvf, N, r0_, sol_, tau, nrs, P_.niters, G, s_);
+        if (!gmres_cgs2(mvf, N, r0_, sol_, tau, nrs, P_.niters, G, s_))
+          note_capped(ctx_, "tt_amen_solve");
         jac_apply_f64(pt, r1, nk_, r2, jacs, sol_, candY_, 1, s_);
         TTG_CUDA(cudaMemcpyAsync(sol_, candY_, sizeof(double) * N, cudaMemcpyDeviceToDevice, s_));
       } else {
         auto mvf = [&](const double* in, double* o, int nv) { mv(i, in, o, nv); };
-        gmres_cgs2(mvf, N, r0_, sol_, tau, nrs, P_.niters, G, s_);
+        if (!gmres_cgs2(mvf, N, r0_, sol_, tau, nrs, P_.niters, G, s_))
+          note_capped(ctx_, "tt_amen_solve");
       }
       sub_kernel<<<eb(N), 256, 0, s_>>>(N, x_[i], sol_, x_[i]);
       TTG_CHECK_LAUNCH();

@@ -2,6 +2,7 @@
 // pointers, result access.  Driver entry points (ttg_eigb, ttg_ksl_z,
 // ttg_amen_solve) live beside their drivers.
 #include "ttg_common.cuh"
+#include <algorithm>
 #include <cstring>
 #include <cmath>
 
@@ -360,6 +361,16 @@ int ttg_stats(const ttg_ctx* c, ttg_int* matvecs, ttg_int* sweeps, double* res,
   if (launches) *launches = c->stat_launches;
   return TTG_OK;
 }
+
+int ttg_set_limits(ttg_ctx* c, ttg_int max_matvecs, ttg_int max_expokit_steps, int strict) {
+  if (!c || max_matvecs < 0 || max_expokit_steps < 0) return TTG_ERR_ARG;
+  c->lim_matvecs = (int)std::min<ttg_int>(max_matvecs, 1 << 30);
+  c->lim_expsteps = (int)std::min<ttg_int>(max_expokit_steps, 1 << 30);
+  c->strict = strict ? 1 : 0;
+  return TTG_OK;
+}
+
+ttg_int ttg_capped(const ttg_ctx* c) { return c ? (ttg_int)c->stat_capped : -1; }
 
 /* total kernel launches issued by this library in this process */
 ttg_int ttg_launch_count(void) { return (ttg_int)ttg::g_launches.load(); }

@@ -159,6 +159,12 @@ struct ttg_ctx {
   long long stat_sweeps = 0;
   long long stat_launches = 0;
   double stat_res = 0.0;
+  long long stat_capped = 0;  // local solves of the last driver call that hit a cap
+  // iteration caps (0 = the reference's values) and whether reaching one is
+  // an error (TTG_ERR_NOCONV) instead of being tolerated as the reference does
+  int lim_matvecs = 0;        // local eigensolver matvec budget (maxMatvecs, 500)
+  int lim_expsteps = 0;       // Expokit integration steps per exponential (mxstep, 500)
+  int strict = 0;
   // learned preconditioner: mode bit 0 = precondition the plain Davidson
   // expansions, bit 1 = record training problems from the sweeps
   ttg_mlp* learned = nullptr;
@@ -286,6 +292,13 @@ void split_op_prepare(SplitOp** op, const LocalDims& L, int nvec_max, const doub
                       const double* A, const double* phi2, void* mem, cudaStream_t s);
 void split_op_apply(SplitOp* op, const double* x, double* y, int nvec, cudaStream_t s);
 bool split_op_supported(const LocalDims& L);
+
+// Plain BF16 tensor-core GEMM on FP32 operands, FP32 accumulate (ttg_tc.cu):
+// C[m*scm + n*scn] = sum_k a[m*sam + k*sak] b[n*sbn + k*sbk]; ws holds
+// bf16_gemm_ws(M, N, K) bytes; err is the bounded-wait flag (device int).
+size_t bf16_gemm_ws(int M, int N, int K);
+void bf16_gemm(int M, int N, int K, const float* a, i64 sam, i64 sak, const float* b, i64 sbn,
+               i64 sbk, float* c, i64 scm, i64 scn, void* ws, int* err, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Dense FP64 linear algebra (ttg_linalg.cu)

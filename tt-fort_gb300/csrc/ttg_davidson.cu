@@ -521,6 +521,15 @@ DavidsonStats Davidson::solve(const MatvecFn& mv, const double* X0, double tol, 
     }
     const int kk = k_;
     int tn = orth_block(T_, tt, V_ + N_ * kk);
+    if (tn == 0 && prec) {
+      // Every transformed residual lay in span(V) (near convergence the
+      // correction equation solved on the split operator returns directions
+      // the basis already holds): expand with the FP64 residuals, which are
+      // orthogonal to the Ritz vectors, so the iteration still progresses to
+      // the FP64 tolerance instead of stopping short of it.
+      gather_cols(N_, tt, idx_, R_, T_, s_);
+      tn = orth_block(T_, tt, V_ + N_ * kk);
+    }
     lap.mark(4);
     if (tn == 0) {
       st.converged = false;

@@ -122,7 +122,9 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
   for (int i = 0; i < d; ++i) TTG_REQUIRE(n[i] == P.m[i], "tt_eigb needs square cores (n == m)");
   const double eps2 = P.eps / std::sqrt((double)d);
   const double resid_damp = 10.0;
-  const int max_matvecs = 500;
+  // PRIMME's maxMatvecs (tt_eigb.f90:152,269), or the context's cap
+  const int max_matvecs = ctx->lim_matvecs > 0 ? ctx->lim_matvecs : 500;
+  ctx->stat_capped = 0;
 
   // operator offsets (compute_ps, matrix_util.f90:242-251)
   std::vector<i64> pa(d + 1, 0);
@@ -170,7 +172,8 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
   total += 2 * al(sizeof(double) * dense_max * dense_max) + al(sizeof(double) * 512) + al(256);
   total += al(syev_lowest_scratch((int)std::max<i64>(1, dense_max)));
   total += al(Davidson::bytes(Nmax, B, maxb_cap));
-  if (P.method == TTG_METHOD_SPLIT) total += al(chosen_bytes(Nmax, B));
+  const bool jd = P.method == TTG_METHOD_SPLIT || P.method == TTG_METHOD_JD64;
+  if (jd) total += al(chosen_bytes(Nmax, B));
   const bool learned_prec = P.method == TTG_METHOD_PLAIN && ctx->learned && (ctx->learned_mode & 1);
   const bool record = P.method == TTG_METHOD_PLAIN && (ctx->learned_mode & 2);
   if (learned_prec) total += al(sizeof(double) * Nmax);
@@ -197,7 +200,7 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
   double* dscr = (double*)mem.take<char>(syev_lowest_scratch((int)std::max<i64>(1, dense_max)));
   int* dst = mem.take<int>(64);
   void* dav_mem = mem.take<char>(Davidson::bytes(Nmax, B, maxb_cap));
-  void* jd_mem = P.method == TTG_METHOD_SPLIT ? (void*)mem.take<char>(chosen_bytes(Nmax, B)) : nullptr;
+  void* jd_mem = jd ? (void*)mem.take<char>(chosen_bytes(Nmax, B)) : nullptr;
   double* ldiag = learned_prec ? mem.take<double>(Nmax) : nullptr;
   PinnedBuf hb(4096 + rmaxsvd * 2);
   double* hbuf = hb.p;
@@ -268,6 +271,7 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
       MatvecFn mv = [=](const double* X, double* Y, int nv) { bfun3_f64(L, p1, Ai, p2, X, Y, nv, bfs, s); };
       MatvecFn mvlow;
       if (P.method == TTG_METHOD_SPLIT) split_matvec_factory(L, p1, Ai, p2, B, split_mem, s, &mvlow);
+      if (P.method == TTG_METHOD_JD64) mvlow = mv;   // ablation: the same solver, FP64 products
       if (pt.on) {
         PhaseTimer* ptp = &pt;
         auto wrap = [ptp](MatvecFn inner) {
@@ -283,13 +287,13 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
         if (mvlow) mvlow = wrap(mvlow);
       }
       DavidsonStats st;
-      if (P.method == TTG_METHOD_SPLIT) {
+      if (jd) {
         if (pt.on) pt.dav.s = s;
         int n64 = 0;
         st = chosen_solve(N, B, dav_mem, hbuf, jd_mem, mv, mvlow, cr[i], eps2 / resid_damp,
                           max_matvecs, curcr, lam.data(), s, pt.on ? &pt.dav : nullptr, &n64);
         fp64_mv += n64;
-        split_matvec_check(s);
+        if (P.method == TTG_METHOD_SPLIT) split_matvec_check(s);
       } else {
         const int maxb = (int)std::min<i64>(std::max(4 * B, 32), N);
         const int keep = std::min(B + std::max(1, B / 2), std::max(maxb - B, 1));
@@ -304,6 +308,15 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
       }
       nmv = st.matvecs;
       res = st.res;
+      if (!st.converged) {
+        // the reference tolerates PRIMME's -3 (maxMatvecs reached) and goes
+        // on with the current block (tt_eigb.f90:285-288)
+        ++ctx->stat_capped;
+        if (ctx->strict)
+          throw Error{TTG_ERR_NOCONV, "tt_eigb: local eigensolve at core " + std::to_string(i) +
+                                          " reached the matvec cap (" +
+                                          std::to_string(max_matvecs) + ") before its tolerance"};
+      }
       pt.stop(2);
     }
     double fv = 0.0;
@@ -426,7 +439,9 @@ extern "C" int ttg_eigb(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int
   try {
     TTG_CUDA(cudaSetDevice(ctx->device));
     TTG_REQUIRE(d > 0 && n && m && ra && crA && crY0 && ry && lambda, "null argument");
-    TTG_REQUIRE(method == TTG_METHOD_PLAIN || method == TTG_METHOD_SPLIT, "unknown method");
+    TTG_REQUIRE(method == TTG_METHOD_PLAIN || method == TTG_METHOD_SPLIT ||
+                    method == TTG_METHOD_JD64,
+                "unknown method");
     EigbParams P;
     P.d = (int)d;
     P.n.assign(n, n + d);
@@ -626,5 +641,81 @@ extern "C" int ttg_batch_cores(const ttg_batch* b, ttg_int i, double* out, ttg_i
   const auto& j = b->jobs[i];
   if (j.status != TTG_OK || nelem != (ttg_int)j.out.cores.size()) return TTG_ERR_ARG;
   std::copy(j.out.cores.begin(), j.out.cores.end(), out);
+  return TTG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The local eigensolve of tt_eigb on its own: the call tt_eigb.f90:252-283
+// makes to PRIMME (dprimme with initSize = B, the current block as start,
+// maxMatvecs and eps as given), on device operands.  It lets a caller (or a
+// test) run the library's local solver against the reference's PRIMME on
+// the same local problem.
+// ---------------------------------------------------------------------------
+extern "C" int ttg_local_eig(ttg_ctx* ctx, ttg_int r1, ttg_int n, ttg_int r2, ttg_int ra1,
+                             ttg_int ra2, const double* phi1, const double* A,
+                             const double* phi2, double* X, ttg_int B, double tol,
+                             ttg_int max_matvecs, int method, double* lambda, double* res,
+                             ttg_int* matvecs) {
+  if (!ctx) return TTG_ERR_ARG;
+  try {
+    TTG_CUDA(cudaSetDevice(ctx->device));
+    TTG_REQUIRE(r1 > 0 && n > 0 && r2 > 0 && ra1 > 0 && ra2 > 0, "all sizes must be positive");
+    TTG_REQUIRE(phi1 && A && phi2 && X && lambda, "null argument");
+    TTG_REQUIRE(B >= 1 && B <= 16, "B must be in [1, 16]");
+    TTG_REQUIRE(method == TTG_METHOD_PLAIN || method == TTG_METHOD_SPLIT ||
+                    method == TTG_METHOD_JD64,
+                "unknown method");
+    const i64 N = r1 * n * r2;
+    TTG_REQUIRE(N < (1ll << 31), "local problem too large");
+    TTG_REQUIRE(N >= B, "local problem smaller than the block size");
+    cudaStream_t s = ctx->stream;
+    LocalDims L{r1, n, r2, r1, n, r2, ra1, ra2};
+    const int maxb = (int)std::min<i64>(std::max<i64>(4 * B, 32), N);
+    const bool jd = method != TTG_METHOD_PLAIN;
+    const size_t split_bytes = method == TTG_METHOD_SPLIT ? split_matvec_bytes(L, (int)B) : 0;
+    size_t total = al(bfun3_f64_scratch(L, (int)B)) + al(Davidson::bytes(N, (int)B, maxb)) +
+                   al(sizeof(double) * N * B) + al(split_bytes) + (1 << 16);
+    if (jd) total += al(chosen_bytes(N, (int)B));
+    DevBlock mem;
+    mem.alloc(total);
+    double* bfs = (double*)mem.take<char>(bfun3_f64_scratch(L, (int)B));
+    void* dav_mem = mem.take<char>(Davidson::bytes(N, (int)B, maxb));
+    double* X0 = mem.take<double>(N * B);
+    void* split_mem = split_bytes ? (void*)mem.take<char>(split_bytes) : nullptr;
+    void* jd_mem = jd ? (void*)mem.take<char>(chosen_bytes(N, (int)B)) : nullptr;
+    PinnedBuf hb(4096);
+    TTG_CUDA(cudaMemcpyAsync(X0, X, sizeof(double) * N * B, cudaMemcpyDeviceToDevice, s));
+    MatvecFn mv = [=](const double* x, double* y, int nv) {
+      bfun3_f64(L, phi1, A, phi2, x, y, nv, bfs, s);
+    };
+    const int maxmv = max_matvecs > 0 ? (int)std::min<ttg_int>(max_matvecs, 1 << 30) : 500;
+    std::vector<double> lam(B, 0.0);
+    DavidsonStats st;
+    if (jd) {
+      MatvecFn mvlow = mv;
+      if (method == TTG_METHOD_SPLIT) split_matvec_factory(L, phi1, A, phi2, (int)B, split_mem, s, &mvlow);
+      int n64 = 0;
+      st = chosen_solve(N, (int)B, dav_mem, hb.p, jd_mem, mv, mvlow, X0, tol, maxmv, X,
+                        lam.data(), s, nullptr, &n64);
+      if (method == TTG_METHOD_SPLIT) split_matvec_check(s);
+    } else {
+      const int keep = std::min((int)B + std::max(1, (int)B / 2), std::max(maxb - (int)B, 1));
+      Davidson dav(N, (int)B, maxb, keep, dav_mem, hb.p, s);
+      st = dav.solve(mv, X0, tol, maxmv, X, lam.data());
+    }
+    TTG_CUDA(cudaStreamSynchronize(s));
+    for (int j = 0; j < B; ++j) lambda[j] = lam[j];
+    if (res) *res = st.res;
+    if (matvecs) *matvecs = st.matvecs;
+    ctx->stat_capped = st.converged ? 0 : 1;
+    if (!st.converged && ctx->strict)
+      throw Error{TTG_ERR_NOCONV, "ttg_local_eig: reached the matvec cap before its tolerance"};
+  } catch (const ttg::Error& e) {
+    ctx->last_error = e.msg;
+    return e.code;
+  } catch (const std::exception& e) {
+    ctx->last_error = e.what();
+    return TTG_ERR_ARG;
+  }
   return TTG_OK;
 }

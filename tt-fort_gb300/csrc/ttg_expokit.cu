@@ -603,7 +603,7 @@ static inline double round2(double x) {
 static void zgexpv_dev(ExpWork& w, i64 n, int m, double t, const double2* v, double2* out,
                        double tol, double anorm, const ZMatvecFn& mv, cudaStream_t s,
                        ExpStats* st) {
-  const int ideg = 6, mxstep = 500;
+  const int ideg = 6, mxstep = st && st->mxstep > 0 ? st->mxstep : 500;
   const double delta = 1.2, gamma = 0.9, break_tol = 1.0e-7;
   const double eps = DBL_EPSILON;
   TTG_REQUIRE(m + 2 <= PADE_MAX, "zgexpv: Krylov order too large");
@@ -705,6 +705,14 @@ static void zgexpv_dev(ExpWork& w, i64 n, int m, double t, const double2* v, dou
     if (nstep >= mxstep) break;
   }
   if (st) st->nstep += nstep;
+  if (t_now < t_out) {
+    // stopped at mxstep short of t: Expokit's iflag = 1, which zexp_mv prints
+    // and tolerates (explib.f90:108-111)
+    if (st) ++st->capped;
+    if (st && st->strict)
+      throw Error{TTG_ERR_NOCONV, "zexp_mv: Krylov exponential reached the step cap (" +
+                                      std::to_string(mxstep) + " steps) before t"};
+  }
 }
 
 __global__ void z1x1_kernel(const double2* v, const double2* a, double tau, double2* out) {

@@ -11,6 +11,9 @@ using ZMatvecFn = std::function<void(const double2* X, double2* Y, int t)>;
 
 struct ExpStats {
   long long nmult = 0, nstep = 0, nreject = 0, syncs = 0;
+  int mxstep = 500;          // ZGEXPV's step cap (expokit.f:2506)
+  bool strict = false;       // a capped exponential throws TTG_ERR_NOCONV
+  long long capped = 0;      // exponentials that stopped at the cap short of t
 };
 
 // Workspace for both: n is the largest problem size, m the Krylov order.

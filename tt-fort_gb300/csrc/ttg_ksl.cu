@@ -608,8 +608,12 @@ static void ksl_entry(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_int* 
   P.real_scheme = real;
   long long l0 = g_launches;
   ExpStats est;
+  est.mxstep = ctx->lim_expsteps > 0 ? ctx->lim_expsteps : 500;
+  est.strict = ctx->strict != 0;
+  ctx->stat_capped = 0;
   std::vector<i64> ry_out;
   run_ksl(ctx, P, ctx->zresult_core, ry_out, est);
+  ctx->stat_capped = est.capped;
   for (int k = 0; k <= d; ++k) ry[k] = ry_out[k];
   ctx->result_core.clear();
   if (real) {
@@ -695,8 +699,12 @@ static int diag_ksl_entry(ttg_ctx* ctx, ttg_int d, const ttg_int* n, const ttg_i
   P.diag = true;
   long long l0 = g_launches;
   ExpStats est;
+  est.mxstep = ctx->lim_expsteps > 0 ? ctx->lim_expsteps : 500;
+  est.strict = ctx->strict != 0;
+  ctx->stat_capped = 0;
   std::vector<i64> ry_out;
   run_ksl(ctx, P, ctx->zresult_core, ry_out, est);
+  ctx->stat_capped = est.capped;
   for (int k = 0; k <= d; ++k) ry[k] = ry_out[k];
   ctx->result_core.clear();
   if (real_out) {

@@ -226,6 +226,12 @@ struct ttg_mlp {
   void* work = nullptr;
   size_t work_cap = 0;
   double last_loss = 0.0;
+  // layer products: 1 = BF16 on the tensor cores (tcgen05, FP32 accumulate),
+  // 0 = FP32 on the CUDA cores
+  int bf16 = 1;
+  void* tcws = nullptr;     // bf16 operand tiles and K-split partials (grow-only)
+  size_t tcws_cap = 0;
+  int* tcerr = nullptr;     // bounded-wait flag of the tensor-core products
 };
 
 namespace ttg {
@@ -281,6 +287,29 @@ MlpWork mlp_work(ttg_mlp* M, i64 P, cudaStream_t s) {
   return w;
 }
 
+// c[m*scm + n*scn] = sum_k a[m*sam + k*sak] b[n*sbn + k*sbk] (FP32 in and
+// out), on the tensor cores in BF16 or on the CUDA cores in FP32
+void mlp_gemm(ttg_mlp* M, int Mm, int N, int K, const float* a, i64 sam, i64 sak, const float* b,
+              i64 sbn, i64 sbk, float* c, i64 scm, i64 scn, cudaStream_t s) {
+  if (M->bf16) {
+    const size_t need = bf16_gemm_ws(Mm, N, K);
+    if (need > M->tcws_cap) {
+      if (M->tcws) { cudaStreamSynchronize(s); cudaFree(M->tcws); M->tcws = nullptr; }
+      M->tcws_cap = 0;
+      TTG_CUDA(cudaMalloc(&M->tcws, need));
+      M->tcws_cap = need;
+    }
+    bf16_gemm(Mm, N, K, a, sam, sak, b, sbn, sbk, c, scm, scn, M->tcws, M->tcerr, s);
+    return;
+  }
+  GemmF32 g;
+  g.M = Mm; g.N = N; g.K = K;
+  g.A = a; g.sAm = sam; g.sAk = sak;
+  g.B = b; g.sBk = sbk; g.sBn = sbn;
+  g.C = c; g.sCm = scm; g.sCn = scn;
+  gemm_f32(g, s);
+}
+
 // forward over P points (features in F), layer outputs stored in act; returns h
 const float* mlp_forward(ttg_mlp* M, i64 P, const float* F, float* act, cudaStream_t s) {
   const int L = (int)M->dims.size() - 1;
@@ -288,12 +317,10 @@ const float* mlp_forward(ttg_mlp* M, i64 P, const float* F, float* act, cudaStre
   float* out = act;
   for (int l = 0; l < L; ++l) {
     const int k = M->dims[l], n = M->dims[l + 1];
-    GemmF32 g;   // out (P x n) = in (P x k) W (k x n), row-major
-    g.M = (int)P; g.N = n; g.K = k;
-    g.A = in; g.sAm = k; g.sAk = 1;
-    g.B = M->w + M->woff[l]; g.sBk = n; g.sBn = 1;
-    g.C = out; g.sCm = n; g.sCn = 1;
-    gemm_f32(g, s);
+    // out (P x n) = in (P x k) W (k x n), row-major; computed as
+    // out^T[n_, p] = sum_k W[k, n_] in[p, k] so that the contiguous index of
+    // the output (n_) lies on the tensor-core M side (coalesced stores)
+    mlp_gemm(M, n, (int)P, k, M->w + M->woff[l], 1, n, in, k, 1, out, 1, n, s);
     bias_act_kernel<<<eb(P * n), 256, 0, s>>>(P, n, out, M->w + M->boff[l], l < L - 1);
     TTG_CHECK_LAUNCH();
     in = out;
@@ -318,26 +345,16 @@ void mlp_backward(ttg_mlp* M, i64 P, const float* F, const float* act, float* dz
   float* nxt = dz2;
   for (int l = L - 1; l >= 0; --l) {
     const int k = M->dims[l], n = M->dims[l + 1];
-    {
-      GemmF32 g;   // dW (k x n) = in^T (k x P) cur (P x n)
-      g.M = k; g.N = n; g.K = (int)P;
-      g.A = ain[l]; g.sAm = 1; g.sAk = k;
-      g.B = cur; g.sBk = n; g.sBn = 1;
-      g.C = M->g + M->woff[l]; g.sCm = n; g.sCn = 1;
-      gemm_f32(g, s);
-    }
+    // dW (k x n) = in^T (k x P) cur (P x n): dW[kk, n_] = sum_p cur[p, n_] in[p, kk]
+    mlp_gemm(M, n, k, (int)P, cur, 1, n, ain[l], 1, k, M->g + M->woff[l], 1, n, s);
     {
       dim3 grid((unsigned)ceil_div(n, 128), (unsigned)ceil_div(P, (i64)1024));
       colsum_kernel<<<grid, 128, 0, s>>>(P, n, cur, M->g + M->boff[l]);
       TTG_CHECK_LAUNCH();
     }
     if (l > 0) {
-      GemmF32 g;   // nxt (P x k) = cur (P x n) W^T (n x k)
-      g.M = (int)P; g.N = k; g.K = n;
-      g.A = cur; g.sAm = n; g.sAk = 1;
-      g.B = M->w + M->woff[l]; g.sBk = 1; g.sBn = n;
-      g.C = nxt; g.sCm = k; g.sCn = 1;
-      gemm_f32(g, s);
+      // nxt (P x k) = cur (P x n) W^T (n x k): nxt^T[kk, p] = sum_n_ W[kk, n_] cur[p, n_]
+      mlp_gemm(M, k, (int)P, n, M->w + M->woff[l], n, 1, cur, n, 1, nxt, 1, k, s);
       relu_mask_kernel<<<eb(P * k), 256, 0, s>>>(P * k, nxt, ain[l]);
       TTG_CHECK_LAUNCH();
       std::swap(cur, nxt);
@@ -540,9 +557,10 @@ extern "C" int ttg_mlp_create(ttg_ctx* c, ttg_int width, ttg_int depth, ttg_int 
       off += M->dims[l + 1];
     }
     M->nparams = off;
-    TTG_CUDA(cudaMalloc(&M->w, 4 * off * sizeof(float)));
+    TTG_CUDA(cudaMalloc(&M->w, 4 * off * sizeof(float) + 256));
     M->g = M->w + off; M->m = M->g + off; M->v = M->m + off;
-    TTG_CUDA(cudaMemset(M->w, 0, 4 * off * sizeof(float)));
+    M->tcerr = (int*)(M->v + off);
+    TTG_CUDA(cudaMemset(M->w, 0, 4 * off * sizeof(float) + 256));
     // He-normal weights from the shared splitmix64 stream, zero biases, and a
     // zero output layer: the untrained network is the classical preconditioner
     std::vector<double> z(nw);
@@ -573,7 +591,29 @@ extern "C" int ttg_mlp_destroy(ttg_mlp* M) {
   if (M->ctx->learned == M) { M->ctx->learned = nullptr; M->ctx->learned_mode = 0; }
   if (M->w) cudaFree(M->w);
   if (M->work) cudaFree(M->work);
+  if (M->tcws) cudaFree(M->tcws);
   delete M;
+  return TTG_OK;
+}
+
+extern "C" int ttg_mlp_set_precision(ttg_mlp* M, int bf16) {
+  if (!M) return TTG_ERR_ARG;
+  M->bf16 = bf16 ? 1 : 0;
+  return TTG_OK;
+}
+
+extern "C" int ttg_mlp_check(ttg_mlp* M) {
+  if (!M) return TTG_ERR_ARG;
+  try {
+    TTG_CUDA(cudaSetDevice(M->ctx->device));
+    int h = 0;
+    TTG_CUDA(cudaMemcpyAsync(&h, M->tcerr, sizeof(int), cudaMemcpyDeviceToHost, M->ctx->stream));
+    TTG_CUDA(cudaStreamSynchronize(M->ctx->stream));
+    if (h) throw Error{TTG_ERR_CUDA, "mlp: tensor-core product gave up waiting (mbarrier)"};
+  } catch (const ttg::Error& e) {
+    M->ctx->last_error = e.msg;
+    return e.code;
+  }
   return TTG_OK;
 }
 

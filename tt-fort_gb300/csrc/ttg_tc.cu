@@ -204,20 +204,34 @@ __global__ void split_kernel(const double* __restrict__ src, i64 rv, i64 vs, i64
   }
 }
 
-// C[m, n] (m < M, n < N) = sum_k A[m, k] B[n, k], split-3 on tcgen05.
+// C[m, n] (m < M, n < N) = sum_k A[m, k] B[n, k], split-3 on tcgen05
+// (NPROD = 3: hi hi + hi lo + lo hi) or plain BF16 (NPROD = 1: hi hi only,
+// the lo planes are not read).
 // C[m, n] goes to out[(m / rpv) * vstride + (m % rpv) * rstride + n * cstride].
 // The accumulator row m sits in TMEM lane m % 128, so with rstride == 1 the
 // 32 lanes of a warp store 32 consecutive elements (coalesced).
-template <int BN, int STAGES, class OutT>
+// K split: CTA z of gridDim.z takes the K tiles [z * kchunk, z * kchunk +
+// kchunk) of the ktiles the operands hold and writes its partial product at
+// out + z * zstride (the caller adds the partials in a fixed order).
+template <int BN, int STAGES, class OutT, int NPROD = 3>
 __global__ void __launch_bounds__(NTHREADS, 1)
     split_gemm_kernel(const bf16* __restrict__ Ahi, const bf16* __restrict__ Alo,
                       const bf16* __restrict__ Bhi, const bf16* __restrict__ Blo, int M, int N,
                       int ktiles, OutT* __restrict__ out, i64 rpv, i64 vstride, i64 rstride,
-                      i64 cstride, int* __restrict__ err) {
+                      i64 cstride, int* __restrict__ err, int kchunk = 0, i64 zstride = 0) {
+  static_assert(NPROD == 1 || NPROD == 3, "one or three bf16 products");
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   constexpr uint32_t A_BYTES = TM * TK * 2;
   constexpr uint32_t B_BYTES = BN * TK * 2;
-  constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+  constexpr uint32_t PLANES = NPROD == 3 ? 2 : 1;
+  constexpr uint32_t STAGE_BYTES = PLANES * (A_BYTES + B_BYTES);
+  constexpr uint32_t B_OFF = PLANES * A_BYTES;   // B hi after the A plane(s)
+  const int ktot = ktiles;                        // K tiles the operands hold
+  const int kt0 = kchunk > 0 ? (int)blockIdx.z * kchunk : 0;
+  if (kchunk > 0) {
+    ktiles = min(kchunk, ktot - kt0);
+    out += (i64)blockIdx.z * zstride;
+  }
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   __shared__ __align__(8) uint64_t empty_bar[STAGES];
   __shared__ __align__(8) uint64_t done_bar;
@@ -254,35 +268,40 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       unsigned char* st = base + (size_t)s * STAGE_BYTES;
       uint32_t bar = smem_u32(&full_bar[s]);
       mbar_expect_tx(bar, STAGE_BYTES);
-      size_t ao = ((size_t)mt * ktiles + c) * a_tile;
-      size_t bo = ((size_t)nt * ktiles + c) * b_tile;
+      size_t ao = ((size_t)mt * ktot + kt0 + c) * a_tile;
+      size_t bo = ((size_t)nt * ktot + kt0 + c) * b_tile;
       bulk_g2s(smem_u32(st), Ahi + ao, A_BYTES, bar);
-      bulk_g2s(smem_u32(st + A_BYTES), Alo + ao, A_BYTES, bar);
-      bulk_g2s(smem_u32(st + 2 * A_BYTES), Bhi + bo, B_BYTES, bar);
-      bulk_g2s(smem_u32(st + 2 * A_BYTES + B_BYTES), Blo + bo, B_BYTES, bar);
+      bulk_g2s(smem_u32(st + B_OFF), Bhi + bo, B_BYTES, bar);
+      if constexpr (NPROD == 3) {
+        bulk_g2s(smem_u32(st + A_BYTES), Alo + ao, A_BYTES, bar);
+        bulk_g2s(smem_u32(st + B_OFF + B_BYTES), Blo + bo, B_BYTES, bar);
+      }
     };
-    int issued = 0;
+    int issued = 0, waited = 0;
     for (int c = 0; c < STAGES && c < ktiles; ++c) { issue(c, c); ++issued; }
     bool ok = true;
     for (int c = 0; c < ktiles && ok; ++c) {
       const int s = c % STAGES;
       const uint32_t ph = (uint32_t)((c / STAGES) & 1);
       if (!mbar_wait(smem_u32(&full_bar[s]), ph)) { ok = false; break; }
+      ++waited;
       tc_fence_after();
       unsigned char* st = base + (size_t)s * STAGE_BYTES;
       const uint32_t a_hi = smem_u32(st), a_lo = smem_u32(st + A_BYTES);
-      const uint32_t b_hi = smem_u32(st + 2 * A_BYTES), b_lo = smem_u32(st + 2 * A_BYTES + B_BYTES);
+      const uint32_t b_hi = smem_u32(st + B_OFF), b_lo = smem_u32(st + B_OFF + B_BYTES);
 #pragma unroll
       for (int kk = 0; kk < TK / 16; ++kk) {
         // one 16-wide K slab per MMA
         const uint32_t aoff = kk * (TM * 32), boff = kk * (BN * 32);
         const uint64_t dAh = make_desc(a_hi + aoff, LBO, SBO);
-        const uint64_t dAl = make_desc(a_lo + aoff, LBO, SBO);
         const uint64_t dBh = make_desc(b_hi + boff, LBO, SBO);
-        const uint64_t dBl = make_desc(b_lo + boff, LBO, SBO);
         mma_bf16(taddr, dAh, dBh, idesc, (c > 0 || kk > 0) ? 1u : 0u);
-        mma_bf16(taddr, dAh, dBl, idesc, 1u);
-        mma_bf16(taddr, dAl, dBh, idesc, 1u);
+        if constexpr (NPROD == 3) {
+          const uint64_t dAl = make_desc(a_lo + aoff, LBO, SBO);
+          const uint64_t dBl = make_desc(b_lo + boff, LBO, SBO);
+          mma_bf16(taddr, dAh, dBl, idesc, 1u);
+          mma_bf16(taddr, dAl, dBh, idesc, 1u);
+        }
       }
       mma_commit(smem_u32(&empty_bar[s]));
       const int nc = c + STAGES;
@@ -296,11 +315,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       fail = 1;
       atomicExch(err, 1);
       // let every copy that was issued land before the CTA can exit: the
-      // copies read valid global memory and complete in microseconds, so
-      // these waits end long before their limit; a drain that still gives up
-      // is reported as its own error code (3)
+      // ones not yet waited for (at most one per stage, each in its stage's
+      // current phase) are waited for here.  The copies read valid global
+      // memory and complete in microseconds, so these waits end long before
+      // their limit; a drain that still gives up is reported as code 3
       bool drained = true;
-      for (int c = 0; c < issued; ++c) {
+      for (int c = waited; c < issued; ++c) {
         const int s = c % STAGES;
         drained = mbar_wait(smem_u32(&full_bar[s]), (uint32_t)((c / STAGES) & 1)) && drained;
       }
@@ -430,6 +450,367 @@ __global__ void __launch_bounds__(128)
         if (++a1 == ra1) { a1 = 0; ++i; }
       }
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Fused small local operator: GEMM1, the core contraction and GEMM3 of one
+// (vector, block of c2) in a single CTA, with every intermediate on chip.
+// For local problems whose X_v fits one 128-row tile (rx1*m <= 128, rx2 <= 64,
+// ry1 <= 128) and whose TT-matrix core is small (m*ra2, n*ra1 <= 16, n == m)
+// -- the tt_eigb sizes up to r = 64 -- the four launches of the general path
+// (X split, GEMM1, CORE, GEMM3) and the T1/T2 round trips through memory
+// become one launch:
+//
+//   1. X_v (FP64) is split into bf16 hi/lo straight into shared memory, rows
+//      rho = j + m*b1 (j fastest, so every b1's m rows sit in one tile),
+//      while the Phi2 tile of the CTA (rows kappa = a2 + ra2*c2l for the C
+//      values of c2 the CTA owns) and the first Phi1 tiles land by bulk copy;
+//   2. GEMM1 D1[rho, kappa] = sum_b2 X[rho, b2] Phi2[kappa, b2] on tcgen05
+//      (BF16x3, FP32 in TMEM);
+//   3. D1 goes TMEM -> registers -> shared memory; thread (b1, j) forms
+//      T2[(i = j, c2l), (b1, a1)] = sum_(j', a2) A[a1, i, j', a2] D1[(j', b1), (a2, c2l)]
+//      reading its own and its partners' rows, and writes it split into the
+//      shared-memory B operand of GEMM3 (rows (i, c2l), K = (b1, a1));
+//   4. GEMM3 D3[c1, (i, c2l)] = sum_(b1,a1) Phi1[c1, (b1,a1)] T2[(i,c2l), (b1,a1)]
+//      with the Phi1 tiles streamed through two stages;
+//   5. y[c1 + ry1 (i + n c2)] of vector v is stored from TMEM (lane = c1).
+// ---------------------------------------------------------------------------
+// dynamic shared memory bound of the fused kernel: the 227 KB a CTA may opt
+// into, less the kernel's static shared memory (barriers, 1024-aligned)
+constexpr int FUSED_MAX_SMEM = 225 * 1024;
+
+struct FusedArgs {
+  const double* x;          // x[v*xs + b1 + rx1*(j + m*b2)]
+  double* y;                // y[v*ys + c1 + ry1*(i + n*c2)]
+  const bf16 *p2hi, *p2lo;  // Phi2 tiles (BN1 rows kappa, 64 K = b2), one per block of c2
+  const bf16 *p1hi, *p1lo;  // Phi1 tiles (128 rows c1, K = b1 + rx1*a1), k3tiles of them
+  int rx1, m, rx2, ry1, n, ry2, ra1, ra2;
+  int C;                    // values of c2 per CTA
+  int k3tiles;              // ceil(rx1*ra1 / 64)
+  i64 xs, ys;               // vector strides
+  int* err;
+  // A(a1,i,j,a2) at a[q * NA + p], p = a1 + ra1*i, q = j + m*a2, zero
+  // outside p < n*ra1, q < m*ra2 (NA: the kernel's compile-time bound)
+  float a[256];
+};
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// shared memory plan of fused_small_kernel (bytes from the 1024-aligned base)
+__host__ __device__ constexpr size_t fused_r0(int bn1) {
+  // GEMM1 operands (X and Phi2 tiles, hi and lo) and, after GEMM1, the FP32
+  // copy of D1 with rows of bn1 + 1 floats
+  return (((size_t)2 * TM * TK * 2 + (size_t)2 * bn1 * TK * 2) > (size_t)TM * (bn1 + 1) * 4
+              ? ((size_t)2 * TM * TK * 2 + (size_t)2 * bn1 * TK * 2)
+              : (size_t)TM * (bn1 + 1) * 4 + 1023) & ~(size_t)1023;
+}
+__host__ __device__ constexpr size_t fused_t2(int n3p, int k3tiles) {
+  return (size_t)2 * n3p * TK * 2 * k3tiles;   // hi and lo planes
+}
+constexpr size_t FUSED_P1_STAGE = (size_t)2 * TM * TK * 2;
+__host__ __device__ constexpr size_t fused_smem(int bn1, int n3p, int k3tiles) {
+  return fused_r0(bn1) + fused_t2(n3p, k3tiles) + 2 * FUSED_P1_STAGE + 1024;
+}
+
+template <int BN1, int N3P, int JA, int NA>
+__global__ void __launch_bounds__(NTHREADS, 1) fused_small_kernel(const __grid_constant__ FusedArgs g) {
+  static_assert(JA * NA <= 256, "core coefficients exceed the parameter array");
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar_p2, bar_mma1, bar_mma3;
+  __shared__ __align__(8) uint64_t full3[2], empty3[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int fail;
+
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* sA1 = base;                                  // X tile, hi then lo
+  unsigned char* sB1 = base + 2 * TM * TK * 2;                // Phi2 tile, hi then lo
+  float* sD1 = (float*)base;                                  // after GEMM1
+  unsigned char* sT2 = base + fused_r0(BN1);                  // GEMM3 B operand
+  const size_t t2plane = (size_t)N3P * TK * 2 * g.k3tiles;
+  unsigned char* sP1 = sT2 + 2 * t2plane;                     // two Phi1 stages
+  constexpr int LD1 = BN1 + 1;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nt = blockIdx.x, v = blockIdx.y;
+  const int c20 = nt * g.C;
+  const int ncol = min(g.C, g.ry2 - c20);     // valid c2 of this CTA
+  const int na = g.n * g.ra1;
+
+  if (tid == 0) {
+    mbar_init(smem_u32(&bar_p2), 1);
+    mbar_init(smem_u32(&bar_mma1), 1);
+    mbar_init(smem_u32(&bar_mma3), 1);
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(smem_u32(&full3[s]), 1);
+      mbar_init(smem_u32(&empty3[s]), 1);
+    }
+    fail = 0;
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(smem_u32(&tmem_slot), 256);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t taddr = tmem_slot;
+  constexpr uint32_t B1_BYTES = BN1 * TK * 2, A_BYTES = TM * TK * 2;
+
+  // bulk copies: the Phi2 tile and the first two Phi1 tiles
+  int p1_issued = 0;
+  auto issue_p1 = [&](int c, int s) {
+    unsigned char* st = sP1 + (size_t)s * FUSED_P1_STAGE;
+    const uint32_t bar = smem_u32(&full3[s]);
+    mbar_expect_tx(bar, 2 * A_BYTES);
+    const size_t off = (size_t)c * TM * TK;
+    bulk_g2s(smem_u32(st), g.p1hi + off, A_BYTES, bar);
+    bulk_g2s(smem_u32(st + A_BYTES), g.p1lo + off, A_BYTES, bar);
+  };
+  if (tid == 0) {
+    const uint32_t bar = smem_u32(&bar_p2);
+    mbar_expect_tx(bar, 2 * B1_BYTES);
+    const size_t off = (size_t)nt * BN1 * TK;
+    bulk_g2s(smem_u32(sB1), g.p2hi + off, B1_BYTES, bar);
+    bulk_g2s(smem_u32(sB1 + B1_BYTES), g.p2lo + off, B1_BYTES, bar);
+    for (int c = 0; c < 2 && c < g.k3tiles; ++c) { issue_p1(c, c); ++p1_issued; }
+  }
+
+  // (1) X_v -> sA1, rows rho = j + m*b1, K = b2; one 16-byte core-matrix row
+  // of each plane per item; zero outside rho < rx1*m, b2 < rx2
+  {
+    // thread tid owns row rho = tid; its 64 elements (b2 = 0..63) are loaded
+    // in two batches of 32 independent loads before any conversion, so the
+    // global-memory latency is paid twice, not 64 times
+    const double* __restrict__ xv = g.x + (i64)v * g.xs;
+    const int rho = tid;
+    const int j = rho % g.m, b1 = rho / g.m;
+    const bool row_ok = rho < g.rx1 * g.m;
+    const double* __restrict__ xr = xv + b1 + (i64)g.rx1 * j;
+    const i64 kstride = (i64)g.rx1 * g.m;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      double val[32];
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const int k = half * 32 + q;
+        val[q] = (row_ok && k < g.rx2) ? xr[kstride * k] : 0.0;
+      }
+#pragma unroll
+      for (int gq = 0; gq < 4; ++gq) {
+        __align__(16) bf16 h[8], l[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) split2(val[gq * 8 + q], h[q], l[q]);
+        const uint32_t off = tile_offset(rho, half * 32 + gq * 8, TM);
+        *reinterpret_cast<uint4*>(sA1 + off) = *reinterpret_cast<const uint4*>(h);
+        *reinterpret_cast<uint4*>(sA1 + A_BYTES + off) = *reinterpret_cast<const uint4*>(l);
+      }
+    }
+    // zero the GEMM3 B operand (padding rows and K columns must be zero)
+    uint4* t2 = reinterpret_cast<uint4*>(sT2);
+    const int nz = (int)(2 * t2plane / 16);
+    for (int e = tid; e < nz; e += NTHREADS) t2[e] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  fence_proxy_async();
+  __syncthreads();
+
+  // (2) GEMM1 into TMEM columns [0, BN1)
+  bool p2_ok = true;    // thread 0: the Phi2 copy was waited for
+  if (tid == 0) {
+    if (!mbar_wait(smem_u32(&bar_p2), 0)) {
+      p2_ok = false;
+      fail = 1;
+      atomicExch(g.err, 4);
+    } else {
+      tc_fence_after();
+      constexpr uint32_t idesc = make_idesc(TM, BN1);
+      const uint32_t a_hi = smem_u32(sA1), a_lo = a_hi + A_BYTES;
+      const uint32_t b_hi = smem_u32(sB1), b_lo = b_hi + B1_BYTES;
+#pragma unroll
+      for (int kk = 0; kk < TK / 16; ++kk) {
+        const uint32_t aoff = kk * (TM * 32), boff = kk * (BN1 * 32);
+        const uint64_t dAh = make_desc(a_hi + aoff, LBO, SBO), dAl = make_desc(a_lo + aoff, LBO, SBO);
+        const uint64_t dBh = make_desc(b_hi + boff, LBO, SBO), dBl = make_desc(b_lo + boff, LBO, SBO);
+        mma_bf16(taddr, dAh, dBh, idesc, kk > 0 ? 1u : 0u);
+        mma_bf16(taddr, dAh, dBl, idesc, 1u);
+        mma_bf16(taddr, dAl, dBh, idesc, 1u);
+      }
+    }
+    mma_commit(smem_u32(&bar_mma1));
+  }
+  __syncwarp();
+  if (!mbar_wait(smem_u32(&bar_mma1), 0)) { fail = 1; atomicExch(g.err, 5); }
+  tc_fence_after();
+  __syncthreads();
+  const bool ok1 = fail == 0;
+
+  // (3) D1 -> shared memory (row rho = this thread's TMEM lane), then the
+  // core contraction into the split GEMM3 operand
+  if (ok1) {
+    const int rho = warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN1; c0 += 16) {
+      uint32_t r[16];
+      tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+      tmem_ld_wait();
+#pragma unroll
+      for (int q = 0; q < 16; ++q) sD1[rho * LD1 + c0 + q] = __uint_as_float(r[q]);
+    }
+  }
+  __syncthreads();
+  if (ok1) {
+    // thread (b1, j) forms every output p = (a1, i) of its b1 for the c2
+    // values c2l = j, j + m, ...: the JA inputs of a c2 come from the m rows
+    // of b1 in shared memory, the NA outputs are independent FMA chains with
+    // the core coefficients as compile-time-indexed constants
+    const int rho = tid;
+    const int j = rho % g.m, b1 = rho / g.m;
+    const int ja = g.m * g.ra2, na = g.n * g.ra1;
+    if (b1 < g.rx1) {
+      const float* rows0 = sD1 + (size_t)(g.m * b1) * LD1;
+      int off[JA];
+#pragma unroll
+      for (int q = 0; q < JA; ++q) off[q] = (q % g.m) * LD1 + q / g.m;
+      const uint32_t plane = (uint32_t)t2plane;
+#pragma unroll 1
+      for (int c2l = j; c2l < ncol; c2l += g.m) {
+        const float* rc = rows0 + g.ra2 * c2l;
+        float t[JA];
+#pragma unroll
+        for (int q = 0; q < JA; ++q) t[q] = q < ja ? rc[off[q]] : 0.f;
+#pragma unroll
+        for (int p = 0; p < NA; ++p) {
+          if (p < na) {
+            float acc = 0.f;
+#pragma unroll
+            for (int q = 0; q < JA; ++q) acc = fmaf(g.a[q * NA + p], t[q], acc);
+            const int i = p / g.ra1, a1 = p - i * g.ra1;
+            const int r3 = i + g.n * c2l;
+            const int k3 = b1 + g.rx1 * a1;
+            bf16 h, l;
+            split2f(acc, h, l);
+            const uint32_t o = (uint32_t)(k3 >> 6) * (N3P * TK * 2) + tile_offset(r3, k3 & 63, N3P);
+            *reinterpret_cast<bf16*>(sT2 + o) = h;
+            *reinterpret_cast<bf16*>(sT2 + plane + o) = l;
+          }
+        }
+      }
+    }
+  }
+  fence_proxy_async();
+  __syncthreads();
+
+  // (4) GEMM3 into TMEM columns [BN1, BN1 + N3P), Phi1 tiles through two stages
+  if (tid == 0) {
+    bool ok = ok1;
+    int p1_waited = 0;
+    if (ok) {
+      constexpr uint32_t idesc = make_idesc(TM, N3P);
+      const uint32_t t2hi = smem_u32(sT2), t2lo = t2hi + (uint32_t)t2plane;
+      for (int c = 0; c < g.k3tiles && ok; ++c) {
+        const int s = c & 1;
+        const uint32_t ph = (uint32_t)((c >> 1) & 1);
+        if (!mbar_wait(smem_u32(&full3[s]), ph)) { ok = false; break; }
+        ++p1_waited;
+        tc_fence_after();
+        const uint32_t a_hi = smem_u32(sP1 + (size_t)s * FUSED_P1_STAGE), a_lo = a_hi + A_BYTES;
+        const uint32_t bt = (uint32_t)c * (N3P * TK * 2);
+#pragma unroll
+        for (int kk = 0; kk < TK / 16; ++kk) {
+          const uint32_t aoff = kk * (TM * 32), boff = bt + kk * (N3P * 32);
+          const uint64_t dAh = make_desc(a_hi + aoff, LBO, SBO), dAl = make_desc(a_lo + aoff, LBO, SBO);
+          const uint64_t dBh = make_desc(t2hi + boff, LBO, SBO), dBl = make_desc(t2lo + boff, LBO, SBO);
+          mma_bf16(taddr + BN1, dAh, dBh, idesc, (c > 0 || kk > 0) ? 1u : 0u);
+          mma_bf16(taddr + BN1, dAh, dBl, idesc, 1u);
+          mma_bf16(taddr + BN1, dAl, dBh, idesc, 1u);
+        }
+        mma_commit(smem_u32(&empty3[s]));
+        if (c + 2 < g.k3tiles) {
+          if (!mbar_wait(smem_u32(&empty3[s]), ph)) { ok = false; break; }
+          issue_p1(c + 2, s);
+          ++p1_issued;
+        }
+      }
+    }
+    if (!ok) {
+      fail = 1;
+      atomicExch(g.err, 6);
+    }
+    // every bulk copy this CTA issued lands before it can exit: the copies
+    // not yet waited for (at most one per stage, each in its stage's current
+    // phase) are waited for here.  They read valid global memory and complete
+    // in microseconds; a drain that still gives up is its own code.
+    bool drained = true;
+    if (!p2_ok) drained = mbar_wait(smem_u32(&bar_p2), 0);
+    for (int c = p1_waited; c < p1_issued; ++c)
+      drained = mbar_wait(smem_u32(&full3[c & 1]), (uint32_t)((c >> 1) & 1)) && drained;
+    if (!drained) atomicExch(g.err, 3);
+    mma_commit(smem_u32(&bar_mma3));
+  }
+  __syncwarp();
+  const bool done3 = mbar_wait(smem_u32(&bar_mma3), 0);
+  tc_fence_after();
+  if (!done3) {
+    fail = 1;
+    if (lane == 0) atomicExch(g.err, 2);
+  }
+  __syncthreads();
+
+  // (5) y of vector v: TMEM lane = c1 (coalesced stores along c1); the
+  // condition is CTA-uniform, so every warp's tcgen05.ld is converged
+  if (fail == 0) {
+    const int c1 = warp * 32 + lane;
+    double* yv = g.y + (i64)v * g.ys;
+    const int cols = g.n * ncol;
+#pragma unroll 1
+    for (int c0 = 0; c0 < N3P; c0 += 16) {
+      if (c0 >= cols) break;
+      uint32_t r[16];
+      tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(BN1 + c0), r);
+      tmem_ld_wait();
+      if (c1 < g.ry1) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const int col = c0 + q;
+          if (col < cols) {
+            const int i = col % g.n, c2 = c20 + col / g.n;
+            yv[c1 + (i64)g.ry1 * (i + (i64)g.n * c2)] = (double)__uint_as_float(r[q]);
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(taddr, 256);
+}
+
+// Phi2 rows for the fused kernel: tile t row kappa < ra2*C is (a2, c2) =
+// (kappa % ra2, t*C + kappa / ra2), K = b2; Phi2[b2, a2, c2] at
+// phi2[b2 + rx2*(a2 + ra2*c2)]; other rows, c2 >= ry2 and b2 >= rx2 are zero
+__global__ void split_p2_fused_kernel(const double* __restrict__ phi2, int rx2, int ra2, int ry2,
+                                      int C, int bn1, int ntiles, bf16* __restrict__ hi,
+                                      bf16* __restrict__ lo) {
+  const i64 total = (i64)ntiles * bn1 * (TK / 8);
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total;
+       e += (i64)gridDim.x * blockDim.x) {
+    const int r = (int)(e % ((i64)ntiles * bn1)), k0 = (int)(e / ((i64)ntiles * bn1)) * 8;
+    const int t = r / bn1, kappa = r % bn1;
+    const int a2 = kappa % ra2, c2 = t * C + kappa / ra2;
+    const bool row_ok = kappa < ra2 * C && c2 < ry2;
+    __align__(16) bf16 h[8], l[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      double val = 0.0;
+      if (row_ok && k0 + q < rx2) val = phi2[(k0 + q) + (i64)rx2 * (a2 + (i64)ra2 * c2)];
+      split2(val, h[q], l[q]);
+    }
+    const size_t idx = (size_t)t * bn1 * TK + (tile_offset(kappa, k0, bn1) >> 1);
+    *reinterpret_cast<uint4*>(hi + idx) = *reinterpret_cast<const uint4*>(h);
+    *reinterpret_cast<uint4*>(lo + idx) = *reinterpret_cast<const uint4*>(l);
   }
 }
 
@@ -638,7 +1019,7 @@ static void gemm_launch_bn(const Tiled& A, const Tiled& B, int M, int N, OutT* o
   TTG_CUDA(attr_rc);
   dim3 grid(A.rtiles, B.rtiles);
   kern<<<grid, NTHREADS, smem, s>>>(A.hi, A.lo, B.hi, B.lo, M, N, A.ktiles, out, rpv, vstride,
-                                    rstride, cstride, err);
+                                    rstride, cstride, err, 0, 0);
   TTG_CHECK_LAUNCH();
 }
 
@@ -650,6 +1031,116 @@ static void gemm_launch(const Tiled& A, const Tiled& B, int M, int N, OutT* out,
   if (B.R == 256) gemm_launch_bn<256>(A, B, M, N, out, rpv, vstride, rstride, cstride, err, s);
   else if (B.R == 128) gemm_launch_bn<128>(A, B, M, N, out, rpv, vstride, rstride, cstride, err, s);
   else gemm_launch_bn<64>(A, B, M, N, out, rpv, vstride, rstride, cstride, err, s);
+}
+
+// ---------------------------------------------------------------------------
+// Plain BF16 tensor-core GEMM on FP32 operands (the learned network's layers):
+//   C[m, n] = sum_k A(m, k) B(n, k),  A(m, k) = a[m*sam + k*sak],
+//   B(n, k) = b[n*sbn + k*sbk],  C[m, n] -> c[m*scm + n*scn]   (FP32),
+// each operand rounded once to bf16 into the tcgen05 tile layout, products
+// accumulated in FP32 in TMEM (NPROD = 1 instance of split_gemm_kernel).
+// K is split over CTAs when the output tiles leave SMs idle; the partial
+// products are added in a fixed order (deterministic).
+// ---------------------------------------------------------------------------
+__global__ void tile_f32_kernel(const float* __restrict__ src, i64 sr, i64 sk, int rows, int cols,
+                                int R, int rtiles, int ktiles, bf16* __restrict__ out) {
+  const i64 tr = (i64)rtiles * R, tk8 = (i64)ktiles * (TK / 8);
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tr * tk8;
+       e += (i64)gridDim.x * blockDim.x) {
+    const int r = (int)(e % tr), k0 = (int)(e / tr) * 8;
+    __align__(16) bf16 h[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      float v = 0.f;
+      if (r < rows && k0 + q < cols) v = src[(i64)r * sr + (i64)(k0 + q) * sk];
+      h[q] = __float2bfloat16_rn(v);
+    }
+    *reinterpret_cast<uint4*>(out + tiled_index(r, k0, R, ktiles)) =
+        *reinterpret_cast<const uint4*>(h);
+  }
+}
+
+__global__ void sum_partials_kernel(const float* __restrict__ part, int nz, int M, int N,
+                                    float* __restrict__ c, i64 scm, i64 scn) {
+  const i64 total = (i64)M * N;
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total;
+       e += (i64)gridDim.x * blockDim.x) {
+    float acc = 0.f;
+    for (int z = 0; z < nz; ++z) acc += part[(i64)z * total + e];
+    const int m = (int)(e % M), n = (int)(e / M);
+    c[(i64)m * scm + (i64)n * scn] = acc;
+  }
+}
+
+constexpr int BF_BN = 128, BF_STAGES = 3;
+constexpr size_t BF_SMEM = (size_t)BF_STAGES * ((size_t)TM * TK * 2 + (size_t)BF_BN * TK * 2) + 1024;
+
+struct Bf16Plan {
+  int mt, nt, kt, nz, kchunk;
+  size_t abytes, bbytes, pbytes;
+};
+static Bf16Plan bf16_plan(int M, int N, int K) {
+  Bf16Plan p;
+  p.mt = ceil_div(M, TM);
+  p.nt = ceil_div(N, BF_BN);
+  p.kt = ceil_div(K, TK);
+  const i64 base = (i64)p.mt * p.nt;
+  int z = base >= 2 * 152 ? 1 : (int)std::min<i64>(p.kt, ceil_div((i64)2 * 152, base));
+  p.kchunk = ceil_div(p.kt, std::max(1, z));
+  p.nz = ceil_div(p.kt, p.kchunk);
+  p.abytes = ((size_t)p.mt * TM * p.kt * TK * 2 + 1023) & ~size_t(1023);
+  p.bbytes = ((size_t)p.nt * BF_BN * p.kt * TK * 2 + 1023) & ~size_t(1023);
+  p.pbytes = p.nz > 1 ? (((size_t)p.nz * M * N * 4 + 1023) & ~size_t(1023)) : 0;
+  return p;
+}
+
+size_t bf16_gemm_ws_impl(int M, int N, int K) {
+  const Bf16Plan p = bf16_plan(M, N, K);
+  return p.abytes + p.bbytes + p.pbytes + 1024;
+}
+
+void bf16_gemm_impl(int M, int N, int K, const float* a, i64 sam, i64 sak, const float* b,
+                    i64 sbn, i64 sbk, float* c, i64 scm, i64 scn, void* ws, int* err,
+                    cudaStream_t s) {
+  if (M <= 0 || N <= 0) return;
+  TTG_REQUIRE(K > 0, "bf16 gemm: K must be positive");
+  const Bf16Plan p = bf16_plan(M, N, K);
+  TTG_REQUIRE(p.nt < 65536 && p.nz < 65536, "bf16 gemm: grid too large");
+  char* w = (char*)ws;
+  bf16* at = (bf16*)w;
+  bf16* bt = (bf16*)(w + p.abytes);
+  float* part = p.nz > 1 ? (float*)(w + p.abytes + p.bbytes) : nullptr;
+  {
+    const i64 tot = (i64)p.mt * TM * p.kt * (TK / 8);
+    tile_f32_kernel<<<(int)std::min<i64>(8192, (tot + 255) / 256), 256, 0, s>>>(
+        a, sam, sak, M, K, TM, p.mt, p.kt, at);
+    TTG_CHECK_LAUNCH();
+  }
+  {
+    const i64 tot = (i64)p.nt * BF_BN * p.kt * (TK / 8);
+    tile_f32_kernel<<<(int)std::min<i64>(8192, (tot + 255) / 256), 256, 0, s>>>(
+        b, sbn, sbk, N, K, BF_BN, p.nt, p.kt, bt);
+    TTG_CHECK_LAUNCH();
+  }
+  auto kern = split_gemm_kernel<BF_BN, BF_STAGES, float, 1>;
+  static const cudaError_t attr_rc =
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BF_SMEM);
+  TTG_CUDA(attr_rc);
+  dim3 grid(p.mt, p.nt, p.nz);
+  if (p.nz > 1) {
+    // partial z at part + z*M*N, column-major (m fastest)
+    kern<<<grid, NTHREADS, BF_SMEM, s>>>(at, at, bt, bt, M, N, p.kt, part, 1ll << 40, 0, 1, M,
+                                         err, p.kchunk, (i64)M * N);
+    TTG_CHECK_LAUNCH();
+    const i64 tot = (i64)M * N;
+    sum_partials_kernel<<<(int)std::min<i64>(4096, (tot + 255) / 256), 256, 0, s>>>(
+        part, p.nz, M, N, c, scm, scn);
+    TTG_CHECK_LAUNCH();
+  } else {
+    kern<<<grid, NTHREADS, BF_SMEM, s>>>(at, at, bt, bt, M, N, p.kt, c, 1ll << 40, 0, scm, scn,
+                                         err, 0, 0);
+    TTG_CHECK_LAUNCH();
+  }
 }
 
 // Tile-width autotuner.  The first product of each shape class (tile counts
@@ -742,6 +1233,12 @@ static int tuned_bn(int M, int N, int K, bool out_double, cudaStream_t s) {
 
 }  // namespace tc
 
+size_t bf16_gemm_ws(int M, int N, int K) { return tc::bf16_gemm_ws_impl(M, N, K); }
+void bf16_gemm(int M, int N, int K, const float* a, i64 sam, i64 sak, const float* b, i64 sbn,
+               i64 sbk, float* c, i64 scm, i64 scn, void* ws, int* err, cudaStream_t s) {
+  tc::bf16_gemm_impl(M, N, K, a, sam, sak, b, sbn, sbk, c, scm, scn, ws, err, s);
+}
+
 // prepared split operator of one local problem
 //   GEMM1: A = X (rows (b1,j,v), K b2), B = Phi2 (rows (a2,c2), K b2),
 //          T1 column-major (rows (b1,j,v), ld1 = rx1*m*nvec_max)
@@ -759,7 +1256,48 @@ struct SplitOp {
   float* part;          // K-chunk partials of the tiled CORE kernel (or null)
   int coef_kind;        // 0: tiled CORE kernel; 1..4: small CORE with (JA, NA) bound
   float coef[256];      // A as FP32 in its own column-major order (small CORE)
+  // fused single-launch path (fused_small_kernel) when the shape allows it
+  bool fused = false;
+  int fbn1 = 0, fn3p = 0, fC = 0, fntiles = 0;
+  tc::bf16 *p2f_hi = nullptr, *p2f_lo = nullptr;
 };
+
+// Tile widths of the fused path for a local problem, or false when the shape
+// needs the general four-launch path: X_v in one 128-row tile (rx1*m <= 128,
+// rx2 <= 64), Phi1 in one 128-row tile (ry1 <= 128), a small square core
+// (n == m, m*ra2 and n*ra1 <= 16) and the shared memory plan within 227 KB.
+// The narrow tiles (64 columns of GEMM1, 32 of GEMM3) are taken when the wide
+// ones would leave more than half the SMs without a CTA.  TTG_FUSED=0 turns
+// the fused path off.
+static bool fused_plan(const LocalDims& L, int nvec, int& bn1, int& n3p, int& C, int& ntiles) {
+  static const bool enabled = [] {
+    const char* v = std::getenv("TTG_FUSED");
+    return !(v && v[0] == '0');
+  }();
+  if (!enabled) return false;
+  if (L.n != L.m || 128 % L.m != 0 || L.rx1 * L.m > 128 || L.rx2 > 64 || L.ry1 > 128) return false;
+  if (L.m * L.ra2 > 16 || L.n * L.ra1 > 16) return false;
+  const int k3tiles = ceil_div(L.rx1 * L.ra1, tc::TK);
+  bool feasible[2] = {false, false};
+  int cc[2] = {0, 0};
+  i64 ctas[2] = {0, 0};
+  for (int cand = 0; cand < 2; ++cand) {
+    const int b = cand == 0 ? 128 : 64, n3 = cand == 0 ? 64 : 32;
+    cc[cand] = (int)std::min<i64>(b / L.ra2, n3 / L.n);
+    feasible[cand] = cc[cand] >= 1 &&
+                     tc::fused_smem(b, n3, k3tiles) <= (size_t)tc::FUSED_MAX_SMEM;
+    if (feasible[cand]) ctas[cand] = (i64)nvec * ceil_div(L.ry2, cc[cand]);
+  }
+  int pick = -1;
+  if (feasible[0] && (2 * ctas[0] >= 152 || !feasible[1])) pick = 0;
+  else if (feasible[1]) pick = 1;
+  if (pick < 0) return false;
+  bn1 = pick == 0 ? 128 : 64;
+  n3p = pick == 0 ? 64 : 32;
+  C = cc[pick];
+  ntiles = ceil_div(L.ry2, C);
+  return true;
+}
 
 // Sizing (op == nullptr) takes the widest tile padding so that the bytes
 // bound every tile width the autotuner may pick at layout time.
@@ -789,6 +1327,20 @@ static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* 
   }
   part = (part + 1023) & ~size_t(1023);
   tot += part;
+  // permuted Phi2 tiles of the fused path (the larger of its two tile plans)
+  size_t p2f = 0;
+  {
+    int b, n3, c, nt;
+    if (fused_plan(L, nvec_max, b, n3, c, nt)) {
+      for (int bb : {128, 64}) {
+        const int cb = (int)std::min<i64>(bb / L.ra2, (bb == 128 ? 64 : 32) / L.n);
+        if (cb < 1) continue;
+        const size_t e = (size_t)ceil_div(L.ry2, cb) * bb * tc::TK;
+        p2f = std::max(p2f, 2 * ((e * sizeof(tc::bf16) + 1023) & ~size_t(1023)));
+      }
+    }
+  }
+  tot += p2f;
   if (op && base) {
     char* p = base;
     op->L = L;
@@ -802,6 +1354,14 @@ static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* 
     op->ld1 = ld1;
     op->err = (int*)p; p += 1024;
     op->part = part ? (float*)p : nullptr; p += part;
+    op->fused = p2f > 0 && fused_plan(L, nvec_max, op->fbn1, op->fn3p, op->fC, op->fntiles);
+    if (op->fused) {
+      const size_t e = (size_t)op->fntiles * op->fbn1 * tc::TK;
+      const size_t b = (e * sizeof(tc::bf16) + 1023) & ~size_t(1023);
+      op->p2f_hi = (tc::bf16*)p;
+      op->p2f_lo = (tc::bf16*)(p + b);
+    }
+    p += p2f;
   }
   return tot;
 }
@@ -833,15 +1393,26 @@ void split_op_prepare(SplitOp* op, const LocalDims& L, int nvec_max, const doubl
     TTG_CUDA(cudaStreamSynchronize(s));
     for (int e = 0; e < ja * na; ++e) op->coef[e] = (float)ah[e];
   }
-  // Phi2 element (n=(a2,c2), k=b2) at phi2[b2 + rx2*n]
-  tc::split_into(phi2, 1ll << 40, 0, L.rx2, 1, op->P2, s);
   // Phi1 element (c1, k=(b1,a1)) at phi1[c1 + ry1*k]
   tc::split_into(phi1, 1ll << 40, 0, 1, L.ry1, op->P1, s);
+  TTG_CUDA(cudaMemsetAsync(op->err, 0, sizeof(int), s));
+  if (op->fused) {
+    // fused path: Phi2 rows (a2, c2) grouped per block of C values of c2
+    TTG_REQUIRE(op->coef_kind > 0, "fused split matvec: core too large");
+    const i64 total = (i64)op->fntiles * op->fbn1 * (tc::TK / 8);
+    const int blocks = (int)std::min<i64>(4096, (total + 255) / 256);
+    tc::split_p2_fused_kernel<<<blocks, 256, 0, s>>>(phi2, (int)L.rx2, (int)L.ra2, (int)L.ry2,
+                                                      op->fC, op->fbn1, op->fntiles, op->p2f_hi,
+                                                      op->p2f_lo);
+    TTG_CHECK_LAUNCH();
+    return;
+  }
+  // Phi2 element (n=(a2,c2), k=b2) at phi2[b2 + rx2*n]
+  tc::split_into(phi2, 1ll << 40, 0, L.rx2, 1, op->P2, s);
   // T2 padding (K columns the CORE kernel never writes) must be zero: padded
   // K columns meet zero columns of Phi1, and 0 * garbage could be NaN
   TTG_CUDA(cudaMemsetAsync(op->T2.hi, 0, op->T2.elems() * sizeof(tc::bf16), s));
   TTG_CUDA(cudaMemsetAsync(op->T2.lo, 0, op->T2.elems() * sizeof(tc::bf16), s));
-  TTG_CUDA(cudaMemsetAsync(op->err, 0, sizeof(int), s));
 }
 
 static void core_apply(SplitOp* op, int nvec, cudaStream_t s) {
@@ -895,9 +1466,60 @@ static void core_apply(SplitOp* op, int nvec, cudaStream_t s) {
   TTG_CHECK_LAUNCH();
 }
 
+template <int BN1, int N3P, int JA, int NA>
+static void fused_launch(const tc::FusedArgs& a, int ntiles, int nvec, cudaStream_t s) {
+  auto kern = tc::fused_small_kernel<BN1, N3P, JA, NA>;
+  const size_t smem = tc::fused_smem(BN1, N3P, a.k3tiles);
+  static const cudaError_t attr_rc = cudaFuncSetAttribute(
+      kern, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::FUSED_MAX_SMEM);
+  TTG_CUDA(attr_rc);
+  TTG_REQUIRE(smem <= (size_t)tc::FUSED_MAX_SMEM, "fused split matvec: shared memory plan");
+  kern<<<dim3(ntiles, nvec), tc::NTHREADS, smem, s>>>(a);
+  TTG_CHECK_LAUNCH();
+}
+
+static void fused_apply(SplitOp* op, const double* x, double* y, int nvec, cudaStream_t s) {
+  const LocalDims& L = op->L;
+  TTG_REQUIRE(nvec < 65536, "fused split matvec: too many vectors");
+  tc::FusedArgs a;
+  a.x = x; a.y = y;
+  a.p2hi = op->p2f_hi; a.p2lo = op->p2f_lo;
+  a.p1hi = op->P1.hi; a.p1lo = op->P1.lo;
+  a.rx1 = (int)L.rx1; a.m = (int)L.m; a.rx2 = (int)L.rx2; a.ry1 = (int)L.ry1;
+  a.n = (int)L.n; a.ry2 = (int)L.ry2; a.ra1 = (int)L.ra1; a.ra2 = (int)L.ra2;
+  a.C = op->fC;
+  a.k3tiles = op->P1.ktiles;
+  a.xs = L.xsize(); a.ys = L.ysize();
+  a.err = op->err;
+  const int na = (int)(L.n * L.ra1), ja = (int)(L.m * L.ra2);
+  // coefficients at a[q * NA + p] for the kernel's bound NA
+  auto fill = [&](int NA) {
+    for (int e = 0; e < 256; ++e) a.a[e] = 0.f;
+    for (int q = 0; q < ja; ++q)
+      for (int p = 0; p < na; ++p) a.a[q * NA + p] = op->coef[(size_t)q * na + p];
+  };
+#define TTG_FUSED(JA_, NA_)                                                       \
+  do {                                                                            \
+    fill(NA_);                                                                    \
+    if (op->fbn1 == 128) fused_launch<128, 64, JA_, NA_>(a, op->fntiles, nvec, s); \
+    else fused_launch<64, 32, JA_, NA_>(a, op->fntiles, nvec, s);                 \
+  } while (0)
+  switch (op->coef_kind) {
+    case 1: TTG_FUSED(4, 4); break;
+    case 2: TTG_FUSED(8, 8); break;
+    case 3: TTG_FUSED(10, 10); break;
+    default: TTG_FUSED(16, 16); break;
+  }
+#undef TTG_FUSED
+}
+
 void split_op_apply(SplitOp* op, const double* x, double* y, int nvec, cudaStream_t s) {
   const LocalDims& L = op->L;
   TTG_REQUIRE(nvec >= 1 && nvec <= op->nvec_max, "split matvec: nvec out of range");
+  if (op->fused) {
+    fused_apply(op, x, y, nvec, s);
+    return;
+  }
   const int M1 = (int)(L.rx1 * L.m * nvec), N1 = (int)(L.ra2 * L.ry2);
   const int M3 = (int)L.ry1, N3 = (int)(L.n * L.ry2 * nvec);
   // X_v element (row (b1,j), k=b2) at x[v*xsize + row + rx1*m*b2]

@@ -25,8 +25,9 @@ LIB_PATH = os.path.join(_HERE, "libttgpu.so")
 
 TTG_OK = 0
 TTG_ERR_ARG = -1
+TTG_ERR_NOCONV = -4
 TTG_ERR_UNSUPPORTED = -7
-METHOD = {"plain": 0, "split": 1}
+METHOD = {"plain": 0, "split": 1, "jd64": 2}
 
 _i64 = C.c_int64
 _i64p = C.POINTER(C.c_int64)
@@ -58,6 +59,8 @@ def lib():
         L.ttg_djac_size.argtypes = [C.c_char, _i64, _i64, _i64]
         L.ttg_mlp_nparams.restype = _i64
         L.ttg_mlp_nparams.argtypes = [C.c_void_p]
+        L.ttg_capped.restype = _i64
+        L.ttg_capped.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -77,7 +80,9 @@ EXPORTED = [
     "ttg_mlp_train_recorded", "ttg_batch_create", "ttg_batch_destroy", "ttg_batch_add_eigb",
     "ttg_batch_run", "ttg_batch_result", "ttg_batch_cores", "ttg_djac_size", "ttg_djac_gen",
     "ttg_djac_apply", "ttg_mvk4", "ttg_sdv_write", "ttg_sdv_read", "ttg_diag_ksl_z",
-    "ttg_diag_ksl_d", "ttg_ksl_d",
+    "ttg_diag_ksl_d", "ttg_ksl_d", "ttg_set_limits", "ttg_capped",
+    "ttg_local_eig", "dbfun3", "djac_gen", "djac_apply", "dqr", "ttg_fshim_status",
+    "ttg_mlp_set_precision", "ttg_mlp_check",
 ]
 
 
@@ -118,6 +123,20 @@ class Context:
         res = C.c_double()
         lib().ttg_stats(self._h, C.byref(mv), C.byref(sw), C.byref(res), C.byref(la))
         return {"matvecs": mv.value, "sweeps": sw.value, "res": res.value, "launches": la.value}
+
+    def set_limits(self, max_matvecs=0, max_expokit_steps=0, strict=False):
+        """Iteration caps of the local solvers for the next driver calls (0 =
+        the reference's 500 / 500).  strict=True turns a capped local solve
+        into TTGError(TTG_ERR_NOCONV); otherwise it is tolerated and counted,
+        as the reference tolerates PRIMME's -3 and Expokit's iflag = 1."""
+        if max_matvecs < 0 or max_expokit_steps < 0:
+            raise ValueError("caps must be >= 0")
+        self.check(lib().ttg_set_limits(self._h, _i64(max_matvecs), _i64(max_expokit_steps),
+                                        C.c_int(1 if strict else 0)))
+
+    def capped(self):
+        """Local solves of the last driver call that stopped at a cap."""
+        return int(lib().ttg_capped(self._h))
 
     def close(self):
         if self._h:
@@ -431,6 +450,27 @@ def dbfun3(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1, A, phi2, x, y, nvec=1, spli
     ctx.check(f(ctx.handle, *_dims(*dims), *ptrs, _i64(nvec)))
 
 
+def local_eig(r1, n, r2, ra1, ra2, phi1, A, phi2, X, B, tol, max_matvecs=500, method="plain",
+              ctx=None):
+    """Lowest B eigenpairs of the local operator y = Phi1 A Phi2 x (the
+    dprimme call of tt_eigb, tt_eigb.f90:252-283) on device tensors: X
+    (N x B) holds the start block and receives the Ritz vectors.  Returns
+    (lambda, res, matvecs)."""
+    N = int(r1) * int(n) * int(r2)
+    dims = (r1, n, r2, r1, n, r2, ra1, ra2)
+    ptrs = _bfun3_ptrs(dims, phi1, A, phi2, X, X, B, "float64")
+    ctx = _kctx(ctx)
+    lam = np.zeros(int(B))
+    res = C.c_double()
+    nmv = _i64()
+    ctx.check(lib().ttg_local_eig(ctx.handle, *_dims(r1, n, r2, ra1, ra2), ptrs[0], ptrs[1],
+                                  ptrs[2], ptrs[3], _i64(B), C.c_double(tol), _i64(max_matvecs),
+                                  C.c_int(METHOD[method]), _p(lam), C.byref(res),
+                                  C.byref(nmv)))
+    assert N >= B
+    return lam, res.value, nmv.value
+
+
 def djac_size(ptype, rx1, n, rx2):
     """Doubles of the block-Jacobi preconditioner (djac_gen, tt_linalg.f90:363)."""
     return int(lib().ttg_djac_size(ptype.encode(), rx1, n, rx2))
@@ -631,6 +671,14 @@ class LearnedPrec:
 
     def adam_step(self, lr):
         self.ctx.check(lib().ttg_mlp_adam_step(self._h, C.c_double(lr)))
+
+    def set_precision(self, bf16=True):
+        """Layer products in BF16 on the tensor cores (default) or FP32."""
+        self.ctx.check(lib().ttg_mlp_set_precision(self._h, C.c_int(1 if bf16 else 0)))
+
+    def check(self):
+        """Raise if a tensor-core product of the network gave up waiting."""
+        self.ctx.check(lib().ttg_mlp_check(self._h))
 
     def train_recorded(self, rec_ctx, steps, lr=1e-4, seed=0):
         l0, l1 = C.c_double(), C.c_double()
