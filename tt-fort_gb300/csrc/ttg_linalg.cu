@@ -17,6 +17,7 @@
 #include "ttg_common.cuh"
 #include <cooperative_groups.h>
 #include <cfloat>
+#include <cstdlib>
 
 namespace cg = cooperative_groups;
 
@@ -526,6 +527,8 @@ static int svd_coop_blocks() {
 // can co-schedule them, else the portable 8; 0 when clusters are unusable
 static int svd_cluster_ctas() {
   static const int n = [] {
+    const char* env = std::getenv("TTG_SVD_CLUSTER");
+    if (env && env[0] == '0') return 0;   // TTG_SVD_CLUSTER=0: grid sweeps only
     if (cudaFuncSetAttribute(svd_sweep_cluster_kernel,
                              cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
       (void)cudaGetLastError();
