@@ -420,85 +420,6 @@ __global__ void __launch_bounds__(SVD_CT) svd_sweep_kernel(int p, int q, T* M, T
   if (blockIdx.x == 0 && tid == 0 && status) *status = sweep;
 }
 
-// The same sweeps for narrow blocks (q <= SVDC_MAXQ) on one thread block
-// cluster instead of the whole grid: one warp per column pair (lanes split
-// the rows, dot products by warp shuffles, every lane computes the same
-// rotation) and a cluster barrier between rounds, which costs a fraction of
-// a grid barrier.  M and V stay in global memory (L2); the release/acquire
-// cluster barrier orders the rounds' writes across the cluster's CTAs.  The
-// pair order, the rotation formula, the thresholds and the stopping rule
-// (a sweep without a counted rotation) are those of svd_sweep_kernel.
-constexpr int SVDC_NT = 256;          // eight warps per CTA
-constexpr int SVDC_MAXQ = 256;        // at most 128 pairs: one per warp of 16 CTAs
-__global__ void __launch_bounds__(SVDC_NT) svd_sweep_cluster_kernel(int p, int q, double* M,
-                                                                     double* V, int* status,
-                                                                     int init_v, double tol,
-                                                                     double tol_count,
-                                                                     int max_sweeps) {
-  cg::cluster_group cl = cg::this_cluster();
-  __shared__ int cnt;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nwarp_cl = (int)cl.num_blocks() * (SVDC_NT / 32);
-  const int gw = (int)cl.block_rank() * (SVDC_NT / 32) + warp;
-  const int K = (q + 1) & ~1;
-  const int npairs = K / 2;
-  if (!init_v)
-    for (i64 e = (i64)cl.block_rank() * SVDC_NT + tid; e < (i64)q * q;
-         e += (i64)cl.num_blocks() * SVDC_NT)
-      V[e] = (e % q == e / q) ? 1.0 : 0.0;
-  if (tid == 0) cnt = 0;
-  cl.sync();
-  int sweep = 0;
-  for (sweep = 0; sweep < max_sweeps; ++sweep) {
-    int mine = 0;   // counted rotations of this warp in this sweep
-    for (int r = 0; r < K - 1; ++r) {
-      for (int pi = gw; pi < npairs; pi += nwarp_cl) {
-        int a, b;
-        rr_pair(K, r, pi, a, b);
-        if (a >= q || b >= q) continue;
-        double* ca = M + (i64)p * a;
-        double* cb = M + (i64)p * b;
-        double al = 0.0, be = 0.0, ga = 0.0;
-        for (int i = lane; i < p; i += 32) {
-          const double x = ca[i], y = cb[i];
-          al = fma(x, x, al); be = fma(y, y, be); ga = fma(x, y, ga);
-        }
-        al = warp_sum_t(al); be = warp_sum_t(be); ga = warp_sum_t(ga);
-        const double nab = sqrt(al * be);
-        if (!((ga != 0.0) && (fabs(ga) > tol * nab))) continue;
-        const double zeta = (be - al) / (2.0 * ga);
-        const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        const double c = 1.0 / sqrt(1.0 + t * t);
-        const double sn = c * t;
-        if (fabs(ga) > tol_count * nab) ++mine;
-        for (int i = lane; i < p; i += 32) {
-          const double x = ca[i], y = cb[i];
-          ca[i] = c * x - sn * y;
-          cb[i] = sn * x + c * y;
-        }
-        double* va = V + (i64)q * a;
-        double* vb = V + (i64)q * b;
-        for (int i = lane; i < q; i += 32) {
-          const double x = va[i], y = vb[i];
-          va[i] = c * x - sn * y;
-          vb[i] = sn * x + c * y;
-        }
-      }
-      cl.sync();
-    }
-    // rotations counted by the whole cluster in this sweep
-    if (lane == 0 && mine) atomicAdd(&cnt, mine);
-    cl.sync();
-    int total = 0;
-    for (unsigned rk = 0; rk < cl.num_blocks(); ++rk) total += *cl.map_shared_rank(&cnt, rk);
-    cl.sync();
-    if (tid == 0) cnt = 0;
-    cl.sync();
-    if (total == 0) break;
-  }
-  if (cl.block_rank() == 0 && tid == 0 && status) *status = sweep;
-}
-
 __global__ void d2f_kernel(i64 n, const double* __restrict__ a, float* __restrict__ b) {
   for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x)
     b[e] = (float)a[e];
@@ -523,57 +444,9 @@ static int svd_coop_blocks() {
   return max_coop;
 }
 
-// CTAs of the cluster for narrow sweeps: 16 (non-portable) when the device
-// can co-schedule them, else the portable 8; 0 when clusters are unusable
-static int svd_cluster_ctas() {
-  static const int n = [] {
-    const char* env = std::getenv("TTG_SVD_CLUSTER");
-    if (env && env[0] == '0') return 0;   // TTG_SVD_CLUSTER=0: grid sweeps only
-    if (cudaFuncSetAttribute(svd_sweep_cluster_kernel,
-                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
-      (void)cudaGetLastError();
-      return kMaxCluster;
-    }
-    for (int c : {16, 8}) {
-      cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3(c);
-      cfg.blockDim = dim3(SVDC_NT);
-      cudaLaunchAttribute at[1];
-      at[0].id = cudaLaunchAttributeClusterDimension;
-      at[0].val.clusterDim.x = c;
-      at[0].val.clusterDim.y = 1;
-      at[0].val.clusterDim.z = 1;
-      cfg.attrs = at;
-      cfg.numAttrs = 1;
-      int nclusters = 0;
-      if (cudaOccupancyMaxActiveClusters(&nclusters, svd_sweep_cluster_kernel, &cfg) ==
-              cudaSuccess &&
-          nclusters >= 1)
-        return c;
-      (void)cudaGetLastError();
-    }
-    return 0;
-  }();
-  return n;
-}
-
 template <class T>
 static void svd_sweeps(int p, int q, T* M, T* V, int* counters, int* status, int init_v, T tol,
                        T tol_count, int max_sweeps, cudaStream_t s) {
-  if constexpr (sizeof(T) == 8) {
-    const int ncl = q <= SVDC_MAXQ ? svd_cluster_ctas() : 0;
-    if (ncl > 0) {
-      // narrow blocks: one cluster, a cluster barrier per round; as many
-      // CTAs as pairs need (eight warps each)
-      const int npairs = ((q + 1) & ~1) / 2;
-      int ctas = std::min(ncl, std::max(1, ceil_div(npairs, SVDC_NT / 32)));
-      if (ctas > kMaxCluster) ctas = 16;   // 9..16 CTAs: the non-portable size
-      launch_clustered(svd_sweep_cluster_kernel, dim3(ctas), dim3(SVDC_NT), dim3(ctas, 1, 1),
-                       0, s, p, q, (double*)M, (double*)V, status, init_v, (double)tol,
-                       (double)tol_count, max_sweeps);
-      return;
-    }
-  }
   int blocks = std::max(1, std::min((q + 1) / 2, svd_coop_blocks<T>()));
   void* args[] = {&p, &q, &M, &V, &counters, &status, &init_v, &tol, &tol_count, &max_sweeps};
   TTG_CUDA(cudaLaunchCooperativeKernel((void*)svd_sweep_kernel<T>, dim3(blocks), dim3(SVD_CT),
