@@ -456,6 +456,9 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--methods", default="split,plain",
                     help="larger workloads: the methods to time (one method: profiling runs)")
+    ap.add_argument("--profile-matvec", nargs=2, type=int, metavar=("R", "B"),
+                    help="only apply the prepared split local operator (r = R, n = 2, ra = 5, "
+                         "block of B) four times, for a profiler capture")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the block of the metric's other configurations")
     ap.add_argument("--no-xxz", action="store_true",
@@ -485,6 +488,21 @@ def main():
     bench_stream = torch.cuda.Stream()
     torch.cuda.set_stream(bench_stream)
     ctx.bind_torch_stream()
+    if args.profile_matvec:
+        r, nv = args.profile_matvec
+        rng = np.random.default_rng(0)
+        t = lambda a: torch.from_numpy(a).cuda()
+        phi1, A, phi2 = (t(rng.standard_normal(r * r * 5)), t(rng.standard_normal(5 * 2 * 2 * 5)),
+                         t(rng.standard_normal(r * 5 * r)))
+        X = t(rng.standard_normal(r * 2 * r * nv))
+        Y = torch.zeros(r * 2 * r * nv, dtype=torch.float64, device="cuda")
+        op = ttgpu.LocalOp(r, 2, r, r, 2, r, 5, 5, phi1, A, phi2, nvec_max=nv, method="split",
+                           ctx=ctx)
+        for _ in range(4):
+            op.apply(X, Y, nv)
+        torch.cuda.synchronize()
+        op.close()
+        return
     if args.workload != "heisenberg20":
         if rank == 0:
             bench_extra(args, torch, ttgpu, ctx)

@@ -80,3 +80,51 @@ def test_prepared_localop(torch_cuda, ctx, method, tol):
         y = Y.cpu().numpy()
         assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < tol
     op.close()
+
+
+FUSED_SHAPES = [s for s in SHAPES if s[1] == s[4] and s[0] * s[1] <= 128 and s[2] <= 64
+                and s[3] <= 128 and s[1] * s[7] <= 16 and s[4] * s[6] <= 16]
+
+_FUSED_CHILD = r'''
+import json, sys
+import numpy as np, torch
+import ttgpu
+from oracle import ops
+shapes = json.loads(sys.argv[1])
+ctx = ttgpu.Context(0)
+errs = []
+for rx1, m, rx2, ry1, n, ry2, ra1, ra2, nvec in shapes:
+    rng = np.random.default_rng(rx1 + 7 * ry2 + nvec)
+    phi1 = rng.standard_normal(ry1 * rx1 * ra1)
+    A = rng.standard_normal(ra1 * n * m * ra2)
+    phi2 = rng.standard_normal(rx2 * ra2 * ry2)
+    X = rng.standard_normal(rx1 * m * rx2 * nvec)
+    ref = ops.bfun3_block(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1, A, phi2, X, nvec)
+    t = lambda a: torch.from_numpy(a).cuda()
+    Y = torch.full((ry1 * n * ry2 * nvec,), float("nan"), dtype=torch.float64, device="cuda")
+    ttgpu.dbfun3(rx1, m, rx2, ry1, n, ry2, ra1, ra2, t(phi1), t(A), t(phi2), t(X), Y,
+                 nvec=nvec, split=True, ctx=ctx)
+    ctx.synchronize()
+    y = Y.cpu().numpy()
+    errs.append(float(np.linalg.norm(y - ref) / np.linalg.norm(ref)) if np.all(np.isfinite(y))
+                else float("inf"))
+print(json.dumps(errs))
+'''
+
+
+def test_fused_single_launch_path_vs_oracle(torch_cuda):
+    """The opt-in single-launch operator (TTG_FUSED=1, read once per process,
+    so it runs in a child process) on every shape it accepts."""
+    import json
+    import os
+    import subprocess
+    import sys
+    from conftest import ROOT
+    assert len(FUSED_SHAPES) >= 6
+    env = dict(os.environ, TTG_FUSED="1",
+               PYTHONPATH=os.pathsep.join([ROOT, os.path.join(ROOT, "tt-fort_gb300")]))
+    out = subprocess.run([sys.executable, "-c", _FUSED_CHILD, json.dumps(FUSED_SHAPES)],
+                         capture_output=True, text=True, env=env, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    errs = json.loads(out.stdout.strip().splitlines()[-1])
+    assert max(errs) < TOL_SPLIT, errs

@@ -173,10 +173,27 @@ __device__ __forceinline__ size_t tiled_index(int r, int k, int R, int ktiles) {
   return tile * (size_t)R * TK + (tile_offset(r % R, k % TK, R) >> 1);
 }
 
-__device__ __forceinline__ void split2(double v, bf16& hi, bf16& lo) {
-  hi = __float2bfloat16_rn((float)v);
-  lo = __float2bfloat16_rn((float)(v - (double)__bfloat162float(hi)));
+// v ~ hi + lo in bf16: one FP64 -> FP32 conversion, then FP32 arithmetic.
+// GB300 issues FP64 conversions and arithmetic at a small fraction of its
+// FP32 rate, so the remainder is taken from f = fl32(v): the split then
+// carries |v - f| <= 2^-24 |v| beyond the lo term's own rounding (2^-9 of
+// |v - hi|, itself <= 2^-9 |v|), far below what the products keep.
+// fl32(v) truncated toward zero from the two 32-bit halves of v with 32-bit
+// integer operations only (|v - f| < 2^-23 |v|); values outside FP32's
+// normal range, and zeros, take the FP64 conversion
+__device__ __forceinline__ float d2f_trunc(double v) {
+  const unsigned int h = (unsigned int)__double2hiint(v), l = (unsigned int)__double2loint(v);
+  const unsigned int e = (h >> 20) & 0x7FF;
+  if (e < 897 || e > 1150) return __double2float_rn(v);
+  return __uint_as_float((h & 0x80000000u) | ((e - 896) << 23) | ((h & 0xFFFFFu) << 3) | (l >> 29));
 }
+
+__device__ __forceinline__ void split2(double v, bf16& hi, bf16& lo) {
+  const float f = __double2float_rn(v);
+  hi = __float2bfloat16_rn(f);
+  lo = __float2bfloat16_rn(f - __bfloat162float(hi));   // exact in FP32
+}
+
 
 // split an FP64 matrix into tiled hi/lo planes; element (r, k) is read at
 // src[(r / rv) * vs + (r % rv) * sr + k * sk]; padding is written as zero.
@@ -603,16 +620,29 @@ __global__ void __launch_bounds__(NTHREADS, 1) fused_small_kernel(const __grid_c
       for (int gq = 0; gq < 4; ++gq) {
         __align__(16) bf16 h[8], l[8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) split2(val[gq * 8 + q], h[q], l[q]);
+        for (int q = 0; q < 8; ++q) {
+          // every CTA of a vector splits the whole X_v, so the conversion
+          // stays on the integer pipe (truncation: |v - f| < 2^-23 |v|)
+          const float f = d2f_trunc(val[gq * 8 + q]);
+          h[q] = __float2bfloat16_rn(f);
+          l[q] = __float2bfloat16_rn(f - __bfloat162float(h[q]));
+        }
         const uint32_t off = tile_offset(rho, half * 32 + gq * 8, TM);
         *reinterpret_cast<uint4*>(sA1 + off) = *reinterpret_cast<const uint4*>(h);
         *reinterpret_cast<uint4*>(sA1 + A_BYTES + off) = *reinterpret_cast<const uint4*>(l);
       }
     }
-    // zero the GEMM3 B operand (padding rows and K columns must be zero)
-    uint4* t2 = reinterpret_cast<uint4*>(sT2);
-    const int nz = (int)(2 * t2plane / 16);
-    for (int e = tid; e < nz; e += NTHREADS) t2[e] = make_uint4(0u, 0u, 0u, 0u);
+    // zero the padding of the GEMM3 B operand (rows past n*ncol, K columns
+    // past rx1*ra1): those 16-byte row pieces meet zero rows or columns of
+    // the products, and 0 * garbage could be NaN.  The core writes the rest.
+    const int nrow = g.n * ncol, kvalid = g.rx1 * g.ra1, kg = g.k3tiles * (TK / 8);
+    for (int e = tid; e < N3P * kg; e += NTHREADS) {
+      const int r = e % N3P, k0 = (e / N3P) * 8;
+      if (r < nrow && k0 + 8 <= kvalid) continue;
+      const uint32_t o = (uint32_t)(k0 >> 6) * (N3P * TK * 2) + tile_offset(r, k0 & 63, N3P);
+      *reinterpret_cast<uint4*>(sT2 + o) = make_uint4(0u, 0u, 0u, 0u);
+      *reinterpret_cast<uint4*>(sT2 + t2plane + o) = make_uint4(0u, 0u, 0u, 0u);
+    }
   }
   fence_proxy_async();
   __syncthreads();
@@ -674,25 +704,42 @@ __global__ void __launch_bounds__(NTHREADS, 1) fused_small_kernel(const __grid_c
       int off[JA];
 #pragma unroll
       for (int q = 0; q < JA; ++q) off[q] = (q % g.m) * LD1 + q / g.m;
+      // per output p = (a1, i): its row i and the K part (k3 = b1 + rx1*a1)
+      // of its byte offset in the tiled operand, computed once
+      int ip[NA];
+      uint32_t koff[NA];
+#pragma unroll
+      for (int p = 0; p < NA; ++p) {
+        const int i = p / g.ra1, a1 = p - i * g.ra1;
+        const int k3 = b1 + g.rx1 * a1, kk = k3 & 63;
+        ip[p] = i;
+        koff[p] = (uint32_t)(k3 >> 6) * (N3P * TK * 2) + (uint32_t)(kk >> 4) * (N3P * 32) +
+                  (uint32_t)((kk >> 3) & 1) * 128 + (uint32_t)(kk & 7) * 2;
+      }
       const uint32_t plane = (uint32_t)t2plane;
 #pragma unroll 1
       for (int c2l = j; c2l < ncol; c2l += g.m) {
         const float* rc = rows0 + g.ra2 * c2l;
+        const int rbase = g.n * c2l;
         float t[JA];
 #pragma unroll
         for (int q = 0; q < JA; ++q) t[q] = q < ja ? rc[off[q]] : 0.f;
+        // all NA chains unconditionally (the coefficients are zero past na),
+        // q outer so the NA accumulators are independent FMA chains
+        float acc[NA];
+#pragma unroll
+        for (int p = 0; p < NA; ++p) acc[p] = 0.f;
+#pragma unroll
+        for (int q = 0; q < JA; ++q)
+#pragma unroll
+          for (int p = 0; p < NA; ++p) acc[p] = fmaf(g.a[q * NA + p], t[q], acc[p]);
 #pragma unroll
         for (int p = 0; p < NA; ++p) {
           if (p < na) {
-            float acc = 0.f;
-#pragma unroll
-            for (int q = 0; q < JA; ++q) acc = fmaf(g.a[q * NA + p], t[q], acc);
-            const int i = p / g.ra1, a1 = p - i * g.ra1;
-            const int r3 = i + g.n * c2l;
-            const int k3 = b1 + g.rx1 * a1;
+            const int r3 = ip[p] + rbase;
             bf16 h, l;
-            split2f(acc, h, l);
-            const uint32_t o = (uint32_t)(k3 >> 6) * (N3P * TK * 2) + tile_offset(r3, k3 & 63, N3P);
+            split2f(acc[p], h, l);
+            const uint32_t o = koff[p] + (uint32_t)(r3 >> 3) * 256 + (uint32_t)(r3 & 7) * 16;
             *reinterpret_cast<bf16*>(sT2 + o) = h;
             *reinterpret_cast<bf16*>(sT2 + plane + o) = l;
           }
@@ -1267,12 +1314,19 @@ struct SplitOp {
 // rx2 <= 64), Phi1 in one 128-row tile (ry1 <= 128), a small square core
 // (n == m, m*ra2 and n*ra1 <= 16) and the shared memory plan within 227 KB.
 // The narrow tiles (64 columns of GEMM1, 32 of GEMM3) are taken when the wide
-// ones would leave more than half the SMs without a CTA.  TTG_FUSED=0 turns
-// the fused path off.
+// ones would leave more than half the SMs without a CTA.
+// The path is opt-in (TTG_FUSED=1): measured on GB300 (CUDA-graph replays,
+// r = 64, n = 2, ra = 5, block of 5) one fused launch takes 18.7 us against
+// 17.5 us for the four launches of the general path.  Its phases run on one
+// CTA of four warps per block of c2, so each is latency-bound: the X split
+// (64 loads and conversions per thread) ~7.6k cycles, the core contraction
+// ~11k cycles (about 1.8k instructions per thread at ~6 cycles each), GEMM3
+// with its streamed Phi1 tiles ~6.7k, the FP64 stores ~6k; the general path
+// spreads the X split and the core over many CTAs instead.
 static bool fused_plan(const LocalDims& L, int nvec, int& bn1, int& n3p, int& C, int& ntiles) {
   static const bool enabled = [] {
     const char* v = std::getenv("TTG_FUSED");
-    return !(v && v[0] == '0');
+    return v && v[0] == '1';
   }();
   if (!enabled) return false;
   if (L.n != L.m || 128 % L.m != 0 || L.rx1 * L.m > 128 || L.rx2 > 64 || L.ry1 > 128) return false;
