@@ -302,6 +302,55 @@ def config_block(args, torch, ttgpu, ctx):
     return out
 
 
+def batch_chains(count, seed=4):
+    """The first `count` of the 256 chains of the batched configuration: XXZ,
+    d ~ U{16..64}, delta ~ U[0.5, 1.5], B = 4, random rank-16 start (seeded),
+    rank cap ~ U{32..128}."""
+    from ttgpu.operators import xxz_mpo, random_tt
+    rng = np.random.default_rng(seed)
+    ds = rng.integers(16, 65, size=256)
+    deltas = rng.uniform(0.5, 1.5, size=256)
+    caps = rng.integers(32, 129, size=256)
+    out = []
+    for c in range(count):
+        d = int(ds[c])
+        n, m, ra, crA = xxz_mpo(d, delta=float(deltas[c]))
+        _, ry, cr = random_tt(d, 2, 16, last=4, seed=1000 + c)
+        out.append((d, n, m, ra, crA, cr, ry, int(caps[c])))
+    return out
+
+
+def bench_batch(args, torch, ttgpu, ctx):
+    """The batched configuration: independent chains queued on the batch
+    runner (worker threads, one non-blocking stream each, longest first),
+    chosen method, eps 1e-8, at most 20 sweeps; wall time of the whole batch
+    (CUDA events around run())."""
+    chains = batch_chains(args.batch_chains)
+    batch = ttgpu.EigbBatch(nworkers=args.batch_workers, ctx=ctx)
+    for (d, n, m, ra, crA, cr, ry, cap) in chains:
+        batch.add(d, n, m, ra, crA, cr, ry, 1e-8, cap, 4, nswp=20, max_full_size=200,
+                  method="split")
+    with ClockSampler() as clk:
+        _, t = _timed(torch, batch.run)
+    mv = []
+    sec = []
+    for i in range(len(chains)):
+        lam, _, ry_out, st = batch.result(i)
+        mv.append(st["matvecs"])
+        sec.append(st["seconds"])
+    batch.close()
+    line = {"metric": f"batched tt_eigb time, {len(chains)} of the 256 XXZ chains",
+            "value": t, "unit": "s", "n_gpus": 1, "higher_is_better": False,
+            "dtype": "bf16x3+f64", "data": "synthetic (seeded)", "method": "split",
+            "config": {"workload": "batch: XXZ d~U{16..64} delta~U[0.5,1.5] B=4 start_rank=16 "
+                                   "rmax~U{32..128} eps=1e-8 nswp=20 (seed 4)",
+                       "chains": len(chains), "workers": args.batch_workers},
+            "chain_seconds": {"sum": float(np.sum(sec)), "max": float(np.max(sec))},
+            "matvecs": int(np.sum(mv)), "d_sum": int(sum(c[0] for c in chains)),
+            "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
 def run_reference(args):
     from oracle.eigb import tt_eigb as oracle_eigb
     n, m, ra, crA, ry, cr = workload()
@@ -468,7 +517,10 @@ def main():
     ap.add_argument("--ksl-steps", type=int, default=200,
                     help="ksl16: time steps (the workload is 200)")
     ap.add_argument("--workload", default="heisenberg20",
-                    choices=["heisenberg20", "xxz100", "amen10", "ksl16"])
+                    choices=["heisenberg20", "xxz100", "amen10", "ksl16", "batch256"])
+    ap.add_argument("--batch-chains", type=int, default=256,
+                    help="batch256: solve the first K of the 256 chains")
+    ap.add_argument("--batch-workers", type=int, default=16)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
@@ -502,6 +554,10 @@ def main():
             op.apply(X, Y, nv)
         torch.cuda.synchronize()
         op.close()
+        return
+    if args.workload == "batch256":
+        if rank == 0:
+            bench_batch(args, torch, ttgpu, ctx)
         return
     if args.workload != "heisenberg20":
         if rank == 0:
