@@ -7,7 +7,8 @@ block with ranks 16 (seed 0), ranks capped at 64, eps=1e-8, max_full_size=200,
 swept to convergence.  Metric: wall time of one full solve (lower is better).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--method plain|split] [--workload heisenberg20|xxz100|amen10|ksl16]
+                  [--method plain|split]
+                  [--workload heisenberg20|xxz100|amen10|ksl16|batch256|matvec]
 
 The default workload (heisenberg20) is the metric's.  Two larger workloads
 are measured the same way, one timed run per method after a warm-up solve:
@@ -17,7 +18,9 @@ problems r^2 n = 131k), two sweeps; amen10 = the ttamen AMEn solve of
 rank 4, tol 1e-9, ranks up to 128, 20 sweeps; ksl16 = ztt_ksl, 200 steps of
 tau=1e-3 of dx/dt = A x, A = -(Dirichlet Laplacian, d=16, n=32) + a random
 rank-4 TT-matrix with N(0, 0.01^2) entries, x0 a random rank-8 TT vector of
-norm 1, with the split state's relative error against the FP64 state.
+norm 1, with the split state's relative error against the FP64 state;
+batch256 = the batched chains (see batch_chains); matvec = the split and plain
+local matvecs alone at r=64 (block 5) and r=256 (block 8).
 
 GPU arm: times K solves through the C-ABI with CUDA events on the library's
 stream (value), the same solves end to end from pinned host buffers (e2e),
@@ -320,6 +323,24 @@ def batch_chains(count, seed=4):
     return out
 
 
+def bench_matvec(args, torch, ttgpu, ctx):
+    """Split and plain local matvecs (prepared operators, CUDA-graph replays)
+    at the d=20 Heisenberg local size (r=64, block 5) and the d=100 XXZ one
+    (r=256, block 8); one JSON line."""
+    peaks, src = measured_peaks()
+    out = {"metric": "local matvec TFLOP/s (algorithmic)", "peak_bf16_tflops": peaks["bf16_tflops"],
+           "peak_source": src, "shapes": {}}
+    for r, nv in ((64, 5), (256, 8)):
+        row = {}
+        for meth in ("split", "plain"):
+            fl, dt = matvec_roofline(torch, ctx, split=meth == "split", r=r, nvec=nv)
+            row[meth] = {"us": dt * 1e6, "tflops": fl / dt / 1e12}
+        fl = row["split"]["tflops"]
+        row["split"]["bf16_issued_frac"] = 3 * fl / peaks["bf16_tflops"]
+        out["shapes"]["r%d_b%d" % (r, nv)] = row
+    print(json.dumps(out))
+
+
 def bench_batch(args, torch, ttgpu, ctx):
     """The batched configuration: independent chains queued on the batch
     runner (worker threads, one non-blocking stream each, longest first),
@@ -517,7 +538,7 @@ def main():
     ap.add_argument("--ksl-steps", type=int, default=200,
                     help="ksl16: time steps (the workload is 200)")
     ap.add_argument("--workload", default="heisenberg20",
-                    choices=["heisenberg20", "xxz100", "amen10", "ksl16", "batch256"])
+                    choices=["heisenberg20", "xxz100", "amen10", "ksl16", "batch256", "matvec"])
     ap.add_argument("--batch-chains", type=int, default=256,
                     help="batch256: solve the first K of the 256 chains")
     ap.add_argument("--batch-workers", type=int, default=16)
@@ -554,6 +575,10 @@ def main():
             op.apply(X, Y, nv)
         torch.cuda.synchronize()
         op.close()
+        return
+    if args.workload == "matvec":
+        if rank == 0:
+            bench_matvec(args, torch, ttgpu, ctx)
         return
     if args.workload == "batch256":
         if rank == 0:

@@ -128,3 +128,30 @@ def test_fused_single_launch_path_vs_oracle(torch_cuda):
     assert out.returncode == 0, out.stderr[-2000:]
     errs = json.loads(out.stdout.strip().splitlines()[-1])
     assert max(errs) < TOL_SPLIT, errs
+
+
+# products with several output tiles per CTA of the persistent GEMM (both
+# TMEM accumulators reused, ragged K and tile edges), run at each fixed tile
+# width in a child process (TTG_SPLIT_BN is read once per process)
+WIDE_SHAPES = [
+    (256, 2, 256, 256, 2, 256, 5, 5, 8),
+    (256, 2, 200, 250, 2, 190, 5, 5, 7),
+    (130, 2, 70, 130, 2, 70, 5, 5, 3),
+    (7, 3, 11, 5, 2, 9, 2, 3, 2),
+]
+
+
+@pytest.mark.parametrize("bn", ["64", "128", "256"])
+def test_split_gemm_each_tile_width_vs_oracle(torch_cuda, bn):
+    import json
+    import os
+    import subprocess
+    import sys
+    from conftest import ROOT
+    env = dict(os.environ, TTG_SPLIT_BN=bn,
+               PYTHONPATH=os.pathsep.join([ROOT, os.path.join(ROOT, "tt-fort_gb300")]))
+    out = subprocess.run([sys.executable, "-c", _FUSED_CHILD, json.dumps(WIDE_SHAPES)],
+                         capture_output=True, text=True, env=env, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    errs = json.loads(out.stdout.strip().splitlines()[-1])
+    assert max(errs) < TOL_SPLIT, errs

@@ -10,6 +10,14 @@ namespace ttg {
 
 std::atomic<long long> g_launches{0};
 
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("TTG_PDL");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+
 void Workspace::reserve(size_t bytes) {
   bytes = (bytes + 255) & ~size_t(255);
   if (bytes <= cap) return;

@@ -25,6 +25,8 @@ namespace ttg {
 // out[j] = sum_i U[i,j] V[i,j]   (out pre-zeroed)
 __global__ void col_dots_kernel(i64 N, const double* __restrict__ U, const double* __restrict__ V,
                                 double* __restrict__ out) {
+  pdl_trigger();
+  pdl_wait();
   const int j = blockIdx.y;
   double acc = 0.0;
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += (i64)gridDim.x * blockDim.x)
@@ -45,8 +47,7 @@ __global__ void col_dots_kernel(i64 N, const double* __restrict__ U, const doubl
 static void col_dots(i64 N, int t, const double* U, const double* V, double* out, cudaStream_t s) {
   TTG_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * t, s));
   int bx = (int)std::max<i64>(1, std::min<i64>(128, (N + 2047) / 2048));
-  col_dots_kernel<<<dim3(bx, t), 256, 0, s>>>(N, U, V, out);
-  TTG_CHECK_LAUNCH();
+  launch_pdl(col_dots_kernel, dim3(bx, t), dim3(256), 0, s, N, U, V, out);
 }
 
 // q[:, j] -= theta_j p[:, j]; block 0 also clears the step's accumulators
@@ -54,6 +55,8 @@ static void col_dots(i64 N, int t, const double* U, const double* V, double* out
 __global__ void shift_kernel(i64 N, int t, const double* __restrict__ theta,
                              const double* __restrict__ p, double* __restrict__ q,
                              double* __restrict__ pq, double* __restrict__ rr_new) {
+  pdl_trigger();
+  pdl_wait();
   if (blockIdx.x == 0 && threadIdx.x < t) {
     pq[threadIdx.x] = 0.0;
     rr_new[threadIdx.x] = 0.0;
@@ -73,6 +76,8 @@ __global__ void __launch_bounds__(128) proj_dot_kernel(i64 N, int t, int nb,
                                                        double* __restrict__ pq) {
   __shared__ double Cs[PD_MAXT * PD_MAXT];
   __shared__ double red[4][PD_MAXT];
+  pdl_trigger();
+  pdl_wait();
   for (int e = threadIdx.x; e < nb * t; e += blockDim.x) Cs[e] = C[e];
   __syncthreads();
   double acc[PD_MAXT];
@@ -116,6 +121,8 @@ __global__ void cg_update_kernel(i64 N, const double* __restrict__ rr, const dou
                                  const double* __restrict__ p, const double* __restrict__ q,
                                  double* __restrict__ x, double* __restrict__ r,
                                  double* __restrict__ rr_new) {
+  pdl_trigger();
+  pdl_wait();
   const int j = blockIdx.y;
   const bool active = pq[j] > 0.0 && rr[j] > tol2 * rr0[j];
   const double alpha = active ? rr[j] / pq[j] : 0.0;
@@ -148,6 +155,8 @@ __global__ void cg_dir_kernel(i64 N, int t, const double* __restrict__ rr,
                               const double* __restrict__ rr_new, const double* __restrict__ pq,
                               const double* __restrict__ rr0, double tol2,
                               const double* __restrict__ r, double* __restrict__ p) {
+  pdl_trigger();
+  pdl_wait();
   for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < N * t; e += (i64)gridDim.x * blockDim.x) {
     const int j = (int)(e / N);
     const bool active = pq[j] > 0.0 && rr[j] > tol2 * rr0[j];
@@ -262,23 +271,25 @@ struct JdCg {
     int pb = (int)std::max<i64>(1, std::min<i64>(1024, (N + 127) / 128));
     for (int it = 0; it < iters; ++it) {
       low(p, q, t);                                   // q = A~ p
-      shift_kernel<<<eb, 256, 0, s>>>(N, t, theta, p, q, pq, rr_new);   // q -= theta p
-      TTG_CHECK_LAUNCH();
+      launch_pdl(shift_kernel, dim3(eb), dim3(256), 0, s, N, t, theta, (const double*)p, q, pq,
+                 rr_new);                               // q -= theta p
       if (fused) {
         // q = P q with pq = p^T q in the same pass
         double* c = sc + 6 * 64;
         gemm_tn_small(nb, t, N, X, N, q, N, c, nb, 1.0, 0.0, s);
-        proj_dot_kernel<<<pb, 128, 0, s>>>(N, t, nb, X, c, p, q, pq);
-        TTG_CHECK_LAUNCH();
+        launch_pdl(proj_dot_kernel, dim3(pb), dim3(128), 0, s, N, t, nb, X, (const double*)c,
+                   (const double*)p, q, pq);
       } else {
         project(q, t, X, nb);                         // q = P q
         col_dots(N, t, p, q, pq, s);
         TTG_CUDA(cudaMemsetAsync(rr_new, 0, sizeof(double) * t, s));
       }
-      cg_update_kernel<<<dim3(bx, t), 256, 0, s>>>(N, rr, pq, rr0, tol2, p, q, x, r, rr_new);
-      TTG_CHECK_LAUNCH();
-      cg_dir_kernel<<<eb, 256, 0, s>>>(N, t, rr, rr_new, pq, rr0, tol2, r, p);
-      TTG_CHECK_LAUNCH();
+      launch_pdl(cg_update_kernel, dim3(bx, t), dim3(256), 0, s, N, (const double*)rr,
+                 (const double*)pq, (const double*)rr0, tol2, (const double*)p, (const double*)q, x,
+                 r, rr_new);
+      launch_pdl(cg_dir_kernel, dim3(eb), dim3(256), 0, s, N, t, (const double*)rr,
+                 (const double*)rr_new, (const double*)pq, (const double*)rr0, tol2,
+                 (const double*)r, p);
       std::swap(rr, rr_new);
     }
     // keep the correction orthogonal to X (rounding of the split products)
@@ -290,14 +301,15 @@ struct JdCg {
 };
 
 __global__ void neg_kernel(i64 n, double* v) {
+  pdl_trigger();
+  pdl_wait();
   for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x)
     v[e] = -v[e];
 }
 
 void JdCg::scale_cols_neg(double* v, int t) {
   int eb = (int)std::min<i64>(4096, (N * t + 255) / 256);
-  neg_kernel<<<eb, 256, 0, s>>>(N * t, v);
-  TTG_CHECK_LAUNCH();
+  launch_pdl(neg_kernel, dim3(eb), dim3(256), 0, s, N * t, v);
 }
 
 size_t chosen_bytes(i64 N, int B) { return JdCg::bytes(N, B); }

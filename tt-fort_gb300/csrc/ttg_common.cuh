@@ -89,24 +89,64 @@ __device__ __forceinline__ double cluster_sum(double v) {
   return out;
 }
 
-// launch kernel k on grid/block with a cluster of cx x cy x cz CTAs
+// -------------------------------------------------------------------------
+// Programmatic dependent launch.  A kernel launched with launch_pdl may start
+// while the kernel before it in the stream is still running: its CTAs run
+// their prologue (index set-up, barrier initialisation, tensor memory
+// allocation), then every thread calls pdl_wait(), which returns once the
+// preceding grid has completed and its memory is visible.  Every kernel
+// launched this way calls pdl_wait() before its first global load or store,
+// in every thread, so the completion order of the stream is kept transitively
+// (a kernel completes only after the one before it).  pdl_trigger() lets the
+// next kernel's CTAs be scheduled before this one finishes.  Kernels launched
+// without the attribute (or when TTG_PDL=0) see both as no-ops.
+// -------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+bool pdl_enabled();
+
+// launch kernel k on grid/block with a cluster of cx x cy x cz CTAs (cluster.x
+// == 0: no cluster attribute), optionally as a programmatic dependent launch
 template <class... KArgs, class... Args>
-void launch_clustered(void (*k)(KArgs...), dim3 grid, dim3 block, dim3 cluster, size_t smem,
-                      cudaStream_t s, Args&&... args) {
+void launch_ex(void (*k)(KArgs...), dim3 grid, dim3 block, dim3 cluster, bool pdl, size_t smem,
+               cudaStream_t s, Args&&... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = cluster.x;
-  at[0].val.clusterDim.y = cluster.y;
-  at[0].val.clusterDim.z = cluster.z;
+  cudaLaunchAttribute at[2];
+  int na = 0;
+  if (cluster.x > 0) {
+    at[na].id = cudaLaunchAttributeClusterDimension;
+    at[na].val.clusterDim.x = cluster.x;
+    at[na].val.clusterDim.y = cluster.y;
+    at[na].val.clusterDim.z = cluster.z;
+    ++na;
+  }
+  if (pdl && pdl_enabled()) {
+    at[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[na].val.programmaticStreamSerializationAllowed = 1;
+    ++na;
+  }
   cfg.attrs = at;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = na;
   TTG_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...));
   TTG_CHECK_LAUNCH();
+}
+
+template <class... KArgs, class... Args>
+void launch_clustered(void (*k)(KArgs...), dim3 grid, dim3 block, dim3 cluster, size_t smem,
+                      cudaStream_t s, Args&&... args) {
+  launch_ex(k, grid, block, cluster, false, smem, s, std::forward<Args>(args)...);
+}
+
+template <class... KArgs, class... Args>
+void launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                Args&&... args) {
+  launch_ex(k, grid, block, dim3(0, 1, 1), true, smem, s, std::forward<Args>(args)...);
 }
 
 // -------------------------------------------------------------------------

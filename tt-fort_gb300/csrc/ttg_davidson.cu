@@ -24,6 +24,8 @@ __global__ void tn_small_kernel(int M, int N, i64 K, const double* __restrict__ 
                                 const double* __restrict__ B, i64 ldb, double* __restrict__ C,
                                 int ldc, double alpha, double beta, i64 kchunk) {
   namespace cgr = cooperative_groups;
+  pdl_trigger();
+  pdl_wait();
   const int m = blockIdx.x;
   const i64 k0 = blockIdx.y * kchunk, k1 = min(K, k0 + kchunk);
   double acc[TS_MAXN];
@@ -74,8 +76,8 @@ void gemm_tn_small(int M, int N, i64 K, const double* A, i64 lda, const double* 
   i64 nk = std::max<i64>(1, std::min<i64>((304 + M - 1) / M, (K + 255) / 256));
   nk = std::min<i64>(nk, kMaxCluster);
   i64 kchunk = std::max<i64>(1, (K + nk - 1) / nk);
-  launch_clustered(tn_small_kernel, dim3(M, (unsigned)nk), dim3(256), dim3(1, (unsigned)nk, 1),
-                   0, s, M, N, K, A, lda, B, ldb, C, ldc, alpha, beta, kchunk);
+  launch_ex(tn_small_kernel, dim3(M, (unsigned)nk), dim3(256), dim3(1, (unsigned)nk, 1), true, 0, s,
+            M, N, K, A, lda, B, ldb, C, ldc, alpha, beta, kchunk);
 }
 
 // C (R x N, ldc) = alpha * A (R x K, lda) * B (K x N, ldb) + beta * C, with
@@ -84,6 +86,8 @@ __global__ void nn_small_kernel(i64 R, int N, int K, const double* __restrict__ 
                                 const double* __restrict__ B, int ldb, double* __restrict__ C,
                                 i64 ldc, double alpha, double beta) {
   __shared__ double Bs[128 * TS_MAXN];
+  pdl_trigger();
+  pdl_wait();
   for (int e = threadIdx.x; e < K * N; e += blockDim.x) Bs[e] = B[(e % K) + (i64)ldb * (e / K)];
   __syncthreads();
   for (i64 r = blockIdx.x * (i64)blockDim.x + threadIdx.x; r < R; r += (i64)gridDim.x * blockDim.x) {
@@ -110,8 +114,8 @@ void gemm_nn_small(i64 R, int N, int K, const double* A, i64 lda, const double* 
   if (R <= 0 || N <= 0) return;
   TTG_REQUIRE(N <= TS_MAXN && K <= 128, "gemm_nn_small: N > 16 or K > 128");
   int blocks = (int)std::min<i64>(2048, (R + 127) / 128);
-  nn_small_kernel<<<blocks, 128, 0, s>>>(R, N, K, A, lda, B, ldb, C, ldc, alpha, beta);
-  TTG_CHECK_LAUNCH();
+  launch_pdl(nn_small_kernel, dim3(blocks), dim3(128), 0, s, R, N, K, A, lda, B, ldb, C, ldc, alpha,
+             beta);
 }
 
 // R[:, j] = AX[:, j] - theta_j X[:, j];  rn2[j] = ||R[:, j]||^2.  Grid (bx, nb),
@@ -120,6 +124,8 @@ void gemm_nn_small(i64 R, int N, int K, const double* A, i64 lda, const double* 
 __global__ void residual_kernel(i64 N, const double* __restrict__ AX, const double* __restrict__ X,
                                 const double* __restrict__ theta, double* __restrict__ R,
                                 double* __restrict__ rn2) {
+  pdl_trigger();
+  pdl_wait();
   const int j = blockIdx.y;
   const double th = theta[j];
   double acc = 0.0;
@@ -135,11 +141,13 @@ __global__ void residual_kernel(i64 N, const double* __restrict__ AX, const doub
 void residual_cols(i64 N, int nb, const double* AX, const double* X, const double* theta,
                    double* R, double* rn2, cudaStream_t s) {
   int bx = (int)std::max<i64>(1, std::min<i64>(kMaxCluster, (N + 1023) / 1024));
-  launch_clustered(residual_kernel, dim3(bx, nb), dim3(256), dim3(bx, 1, 1), 0, s, N, AX, X,
-                   theta, R, rn2);
+  launch_ex(residual_kernel, dim3(bx, nb), dim3(256), dim3(bx, 1, 1), true, 0, s, N, AX, X, theta,
+            R, rn2);
 }
 
 __global__ void gather_cols_kernel(i64 N, int t, const int* idx, const double* src, double* dst) {
+  pdl_trigger();
+  pdl_wait();
   for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < N * t; e += (i64)gridDim.x * blockDim.x) {
     i64 i = e % N;
     int c = (int)(e / N);
@@ -149,8 +157,7 @@ __global__ void gather_cols_kernel(i64 N, int t, const int* idx, const double* s
 
 void gather_cols(i64 N, int t, const int* idx, const double* src, double* dst, cudaStream_t s) {
   int blocks = (int)std::min<i64>(4096, (N * t + 255) / 256);
-  gather_cols_kernel<<<blocks, 256, 0, s>>>(N, t, idx, src, dst);
-  TTG_CHECK_LAUNCH();
+  launch_pdl(gather_cols_kernel, dim3(blocks), dim3(256), 0, s, N, t, idx, src, dst);
 }
 
 // Cholesky with dropping of dependent columns (oracle.davidson.chol_drop).

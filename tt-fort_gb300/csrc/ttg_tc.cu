@@ -203,6 +203,8 @@ __device__ __forceinline__ void split2(double v, bf16& hi, bf16& lo) {
 __global__ void split_kernel(const double* __restrict__ src, i64 rv, i64 vs, i64 sr, i64 sk,
                              int rows, int cols, int R, int rtiles, int ktiles,
                              bf16* __restrict__ hi, bf16* __restrict__ lo) {
+  pdl_trigger();
+  pdl_wait();
   const i64 tr = (i64)rtiles * R, tk8 = (i64)ktiles * (TK / 8);
   for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tr * tk8;
        e += (i64)gridDim.x * blockDim.x) {
@@ -372,6 +374,263 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 0) tmem_dealloc(taddr, BN);
 }
 
+// ---------------------------------------------------------------------------
+// Persistent, warp-specialised form of the same product (same operand tile
+// layout, same output addressing, same K split).  One CTA per SM walks the
+// output tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...; tile t is
+// (mt, nt, z) with mt fastest.  Six warps:
+//   warp 0 (one lane)  bulk copies of the A/B stages into a STAGES-deep ring,
+//                      running ahead across tile boundaries;
+//   warp 1 (one lane)  tcgen05.mma issue; owns the tensor memory, two FP32
+//                      accumulators of BN columns, used alternately by
+//                      consecutive tiles of the CTA;
+//   warps 2-5          epilogue: warp w reads TMEM lanes 32*(w%4).. with
+//                      tcgen05.ld and stores them, while the MMAs of the
+//                      next tile run on the other accumulator.
+// Ring barriers: full[s] (copies landed), empty[s] (MMAs that read the stage
+// done, tcgen05.commit); accumulator barriers: acc_full[a] (tile's MMAs done,
+// tcgen05.commit) and acc_empty[a] (the four epilogue warps have read it).
+// Every wait is bounded and also gives up once another role has failed; a
+// failing CTA records the code in *err, waits (bounded) for the copies and
+// MMAs it issued and frees its tensor memory.
+// ---------------------------------------------------------------------------
+constexpr int WS_THREADS = 192;
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_wait_f(uint32_t bar, uint32_t parity, volatile int* fail) {
+  for (long long i = 0; i < WAIT_LIMIT; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 63) == 63 && *fail) return false;
+  }
+  return false;
+}
+
+template <int BN, int NPROD>
+__host__ __device__ constexpr int ws_stages() {
+  // as many stages as fit in ~192 KB of shared memory (at most 8)
+  return (192 * 1024) / ((NPROD == 3 ? 2 : 1) * (TM * TK * 2 + BN * TK * 2)) > 8
+             ? 8
+             : (192 * 1024) / ((NPROD == 3 ? 2 : 1) * (TM * TK * 2 + BN * TK * 2));
+}
+template <int BN, int NPROD>
+__host__ __device__ constexpr size_t ws_smem() {
+  return (size_t)ws_stages<BN, NPROD>() * (NPROD == 3 ? 2 : 1) * (TM * TK * 2 + BN * TK * 2) + 1024;
+}
+
+template <int BN, class OutT, int NPROD = 3>
+__global__ void __launch_bounds__(WS_THREADS, 1)
+    split_gemm_ws_kernel(const bf16* __restrict__ Ahi, const bf16* __restrict__ Alo,
+                         const bf16* __restrict__ Bhi, const bf16* __restrict__ Blo, int M, int N,
+                         int ktot, int mtiles, int ntiles, int nz, OutT* __restrict__ out,
+                         i64 rpv, i64 vstride, i64 rstride, i64 cstride, int* __restrict__ err,
+                         int kchunk, i64 zstride) {
+  static_assert(NPROD == 1 || NPROD == 3, "one or three bf16 products");
+  static_assert(BN == 64 || BN == 128 || BN == 256, "tile width");
+  constexpr int STAGES = ws_stages<BN, NPROD>();
+  constexpr uint32_t A_BYTES = TM * TK * 2;
+  constexpr uint32_t B_BYTES = BN * TK * 2;
+  constexpr uint32_t PLANES = NPROD == 3 ? 2 : 1;
+  constexpr uint32_t STAGE_BYTES = PLANES * (A_BYTES + B_BYTES);
+  constexpr uint32_t B_OFF = PLANES * A_BYTES;
+  constexpr uint32_t TMEM_COLS = 2 * BN;   // 128, 256 or 512: a power of two
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[STAGES];
+  __shared__ __align__(8) uint64_t acc_full[2];
+  __shared__ __align__(8) uint64_t acc_empty[2];
+  __shared__ __align__(8) uint64_t done_bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int fail_s;
+  volatile int* fail = &fail_s;
+
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int per_z = mtiles * ntiles, total = per_z * nz;
+
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(smem_u32(&full_bar[s]), 1);
+      mbar_init(smem_u32(&empty_bar[s]), 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(smem_u32(&acc_full[a]), 1);
+      mbar_init(smem_u32(&acc_empty[a]), 4);
+    }
+    mbar_init(smem_u32(&done_bar), 1);
+    fail_s = 0;
+    fence_mbar_init();
+  }
+  if (warp == 1) {
+    tmem_alloc(smem_u32(&tmem_slot), TMEM_COLS);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t taddr = tmem_slot;
+  // the prologue above may overlap the kernel before this one
+  pdl_wait();
+  pdl_trigger();
+
+  // K tiles [k0, k0 + kn) of tile t
+  auto krange = [&](int t, int& k0, int& kn) {
+    if (kchunk > 0) {
+      k0 = (t / per_z) * kchunk;
+      kn = min(kchunk, ktot - k0);
+    } else {
+      k0 = 0;
+      kn = ktot;
+    }
+  };
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- producer ----
+      const size_t a_tile = (size_t)TM * TK, b_tile = (size_t)BN * TK;
+      int it = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
+        const int r = t % per_z, mt = r % mtiles, nt = r / mtiles;
+        int k0, kn;
+        krange(t, k0, kn);
+        for (int c = 0; c < kn; ++c, ++it) {
+          const int s = it % STAGES;
+          if (it >= STAGES &&
+              !mbar_wait_f(smem_u32(&empty_bar[s]), (uint32_t)((it / STAGES - 1) & 1), fail)) {
+            ok = false;
+            break;
+          }
+          unsigned char* st = base + (size_t)s * STAGE_BYTES;
+          const uint32_t bar = smem_u32(&full_bar[s]);
+          mbar_expect_tx(bar, STAGE_BYTES);
+          const size_t ao = ((size_t)mt * ktot + k0 + c) * a_tile;
+          const size_t bo = ((size_t)nt * ktot + k0 + c) * b_tile;
+          bulk_g2s(smem_u32(st), Ahi + ao, A_BYTES, bar);
+          bulk_g2s(smem_u32(st + B_OFF), Bhi + bo, B_BYTES, bar);
+          if constexpr (NPROD == 3) {
+            bulk_g2s(smem_u32(st + A_BYTES), Alo + ao, A_BYTES, bar);
+            bulk_g2s(smem_u32(st + B_OFF + B_BYTES), Blo + bo, B_BYTES, bar);
+          }
+        }
+      }
+      if (!ok) {
+        *fail = 1;
+        atomicExch(err, 1);
+      }
+      if (!ok || *fail) {
+        // the last fill of each stage may not have been consumed: let it land
+        bool drained = true;
+        for (int s = 0; s < STAGES; ++s) {
+          const int last = it - 1 - ((it - 1 - s) % STAGES + STAGES) % STAGES;
+          if (last >= 0 && last < it)
+            drained = mbar_wait(smem_u32(&full_bar[s]), (uint32_t)((last / STAGES) & 1)) && drained;
+        }
+        if (!drained) atomicExch(err, 3);
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issue ----
+      constexpr uint32_t idesc = make_idesc(TM, BN);
+      int it = 0, lt = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < total && ok; t += gridDim.x, ++lt) {
+        const int acc = lt & 1, use = lt >> 1;
+        if (use > 0 && !mbar_wait_f(smem_u32(&acc_empty[acc]), (uint32_t)((use - 1) & 1), fail)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t d = taddr + (uint32_t)(acc * BN);
+        int k0, kn;
+        krange(t, k0, kn);
+        for (int c = 0; c < kn; ++c, ++it) {
+          const int s = it % STAGES;
+          if (!mbar_wait_f(smem_u32(&full_bar[s]), (uint32_t)((it / STAGES) & 1), fail)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          unsigned char* st = base + (size_t)s * STAGE_BYTES;
+          const uint32_t a_hi = smem_u32(st), a_lo = smem_u32(st + A_BYTES);
+          const uint32_t b_hi = smem_u32(st + B_OFF), b_lo = smem_u32(st + B_OFF + B_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < TK / 16; ++kk) {
+            const uint32_t aoff = kk * (TM * 32), boff = kk * (BN * 32);
+            const uint64_t dAh = make_desc(a_hi + aoff, LBO, SBO);
+            const uint64_t dBh = make_desc(b_hi + boff, LBO, SBO);
+            mma_bf16(d, dAh, dBh, idesc, (c > 0 || kk > 0) ? 1u : 0u);
+            if constexpr (NPROD == 3) {
+              mma_bf16(d, dAh, make_desc(b_lo + boff, LBO, SBO), idesc, 1u);
+              mma_bf16(d, make_desc(a_lo + aoff, LBO, SBO), dBh, idesc, 1u);
+            }
+          }
+          mma_commit(smem_u32(&empty_bar[s]));
+        }
+        if (!ok) break;
+        mma_commit(smem_u32(&acc_full[acc]));
+      }
+      if (!ok) {
+        *fail = 1;
+        atomicExch(err, 1);
+      }
+      // every MMA this thread issued has completed once done_bar flips
+      mma_commit(smem_u32(&done_bar));
+      if (!mbar_wait(smem_u32(&done_bar), 0)) atomicExch(err, 2);
+    }
+    __syncwarp();
+  } else {
+    // ---- epilogue ----
+    const int q = warp & 3;   // TMEM lane quadrant this warp may read
+    int lt = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x, ++lt) {
+      const int acc = lt & 1, use = lt >> 1;
+      const bool got = __all_sync(0xffffffffu,
+                                  mbar_wait_f(smem_u32(&acc_full[acc]), (uint32_t)(use & 1), fail));
+      if (!got) {
+        if (lane == 0) {
+          *fail = 1;
+          atomicExch(err, 1);
+        }
+        break;
+      }
+      tc_fence_after();
+      const int r = t % per_z, mt = r % mtiles, nt = r / mtiles;
+      OutT* o = out + (i64)(t / per_z) * zstride;
+      const int row = mt * TM + q * 32 + lane;
+      OutT* orow = o + (row / rpv) * vstride + (row % rpv) * rstride;
+      const int n0 = nt * BN;
+      const uint32_t tbase = taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN);
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        uint32_t v[16];
+        tmem_ld16(tbase + (uint32_t)c0, v);
+        tmem_ld_wait();
+        if (c0 + 16 >= BN) {
+          // the whole accumulator is in registers: hand it back to the MMAs
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(smem_u32(&acc_empty[acc]));
+        }
+        if (row < M) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int n = n0 + c0 + j;
+            if (n < N) orow[(i64)n * cstride] = (OutT)__uint_as_float(v[j]);
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) tmem_dealloc(taddr, TMEM_COLS);
+}
+
 // CORE: T2[(i,c2,v),(b1,a1)] = sum_(j,a2) A[(a1,i),(j,a2)] T1[(b1,j,v),(a2,c2)]
 // T1 is column-major with leading dimension ld1 over the rows (b1,j,v), so
 // b1 is contiguous; the result is written split and tiled as the B operand of
@@ -401,6 +660,8 @@ __global__ void __launch_bounds__(128)
     core_small_kernel(const float* __restrict__ T1, i64 ld1, const CoreCoef<JA, NA> A, int rx1,
                       int m, int ra2, int n, int ra1, int ry2, int nvec, int lgR3, int ktiles3,
                       bf16* __restrict__ hi, bf16* __restrict__ lo) {
+  pdl_trigger();
+  pdl_wait();
   const int ja = m * ra2, na = n * ra1;
   const int nb = rx1 / B1;
   const i64 total = (i64)nb * ry2 * nvec;
@@ -877,6 +1138,8 @@ __global__ void __launch_bounds__(256)
                       float* __restrict__ part) {
   __shared__ float Ts[CT_Q][CT_R + 4];
   __shared__ float As[CT_Q][CT_P + 4];
+  pdl_trigger();
+  pdl_wait();
   __shared__ i64 rbase[CT_R];
   const int ja = m * ra2, na = n * ra1;
   const i64 rows = (i64)rx1 * ry2 * nvec;
@@ -965,6 +1228,8 @@ __global__ void __launch_bounds__(256)
 __global__ void core_finish_kernel(const float* __restrict__ part, int nz, i64 rows, int na,
                                    int rx1, int n, int ra1, int lgR3, int ktiles3,
                                    bf16* __restrict__ hi, bf16* __restrict__ lo) {
+  pdl_trigger();
+  pdl_wait();
   const i64 total = rows * na;
   for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total;
        e += (i64)gridDim.x * blockDim.x) {
@@ -1008,6 +1273,14 @@ static int num_sms() {
   return nsm;
 }
 
+static bool use_ws() {
+  static const bool on = [] {
+    const char* v = std::getenv("TTG_GEMM_WS");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+
 constexpr int stages_for(int bn) { return bn == 256 ? 2 : (bn == 128 ? 3 : 2); }
 constexpr size_t smem_for(int bn) {
   return (size_t)stages_for(bn) * ((size_t)2 * TM * TK * 2 + (size_t)2 * bn * TK * 2) + 1024;
@@ -1022,7 +1295,7 @@ static int pick_bn(int M, int N, int K) {
   int best = 64;
   double best_cost = 1e300;
   for (int bn : {256, 128, 64}) {
-    const int per_sm = (int)std::max<size_t>(1, 228 * 1024 / (smem_for(bn) + 1024));
+    const int per_sm = use_ws() ? 1 : (int)std::max<size_t>(1, 228 * 1024 / (smem_for(bn) + 1024));
     const long long ctas = (long long)mt * ceil_div(N, bn);
     const long long waves = (ctas + (long long)nsm * per_sm - 1) / ((long long)nsm * per_sm);
     const double cost = (double)waves * (kt * (bn / 64.0 + 1.0) + bn / 64.0 + 2.0);
@@ -1050,14 +1323,36 @@ static void split_into(const double* src, i64 rv, i64 vs, i64 sr, i64 sk, const 
                        cudaStream_t s) {
   i64 total = (i64)t.rtiles * t.R * t.ktiles * (TK / 8);
   int blocks = (int)std::min<i64>(8192, (total + 255) / 256);
-  split_kernel<<<blocks, 256, 0, s>>>(src, rv, vs, sr, sk, t.rows, t.cols, t.R, t.rtiles,
-                                      t.ktiles, t.hi, t.lo);
-  TTG_CHECK_LAUNCH();
+  launch_pdl(split_kernel, dim3(blocks), dim3(256), 0, s, src, rv, vs, sr, sk, t.rows, t.cols, t.R,
+             t.rtiles, t.ktiles, t.hi, t.lo);
+}
+
+// persistent launch: one CTA per SM, at most one per output tile
+template <int BN, class OutT, int NPROD>
+static void ws_launch(const bf16* Ahi, const bf16* Alo, const bf16* Bhi, const bf16* Blo, int M,
+                      int N, int ktot, int mtiles, int ntiles, int nz, OutT* out, i64 rpv,
+                      i64 vstride, i64 rstride, i64 cstride, int* err, int kchunk, i64 zstride,
+                      cudaStream_t s) {
+  constexpr size_t smem = ws_smem<BN, NPROD>();
+  auto kern = split_gemm_ws_kernel<BN, OutT, NPROD>;
+  static const cudaError_t attr_rc =
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  TTG_CUDA(attr_rc);
+  const i64 total = (i64)mtiles * ntiles * nz;
+  TTG_REQUIRE(total < (1ll << 31), "split gemm: too many tiles");
+  const int grid = (int)std::min<i64>(total, num_sms());
+  launch_pdl(kern, dim3(grid), dim3(WS_THREADS), smem, s, Ahi, Alo, Bhi, Blo, M, N, ktot, mtiles,
+             ntiles, nz, out, rpv, vstride, rstride, cstride, err, kchunk, zstride);
 }
 
 template <int BN, class OutT>
 static void gemm_launch_bn(const Tiled& A, const Tiled& B, int M, int N, OutT* out, i64 rpv,
                            i64 vstride, i64 rstride, i64 cstride, int* err, cudaStream_t s) {
+  if (use_ws()) {
+    ws_launch<BN, OutT, 3>(A.hi, A.lo, B.hi, B.lo, M, N, A.ktiles, A.rtiles, B.rtiles, 1, out, rpv,
+                           vstride, rstride, cstride, err, 0, 0, s);
+    return;
+  }
   constexpr int STAGES = stages_for(BN);
   constexpr size_t smem = smem_for(BN) + SMEM_PAD;
   auto kern = split_gemm_kernel<BN, STAGES, OutT>;
@@ -1169,6 +1464,20 @@ void bf16_gemm_impl(int M, int N, int K, const float* a, i64 sam, i64 sak, const
         b, sbn, sbk, N, K, BF_BN, p.nt, p.kt, bt);
     TTG_CHECK_LAUNCH();
   }
+  if (use_ws()) {
+    if (p.nz > 1) {
+      ws_launch<BF_BN, float, 1>(at, at, bt, bt, M, N, p.kt, p.mt, p.nt, p.nz, part, 1ll << 40, 0,
+                                 1, M, err, p.kchunk, (i64)M * N, s);
+      const i64 tot = (i64)M * N;
+      sum_partials_kernel<<<(int)std::min<i64>(4096, (tot + 255) / 256), 256, 0, s>>>(
+          part, p.nz, M, N, c, scm, scn);
+      TTG_CHECK_LAUNCH();
+    } else {
+      ws_launch<BF_BN, float, 1>(at, at, bt, bt, M, N, p.kt, p.mt, p.nt, 1, c, 1ll << 40, 0, scm,
+                                 scn, err, 0, 0, s);
+    }
+    return;
+  }
   auto kern = split_gemm_kernel<BF_BN, BF_STAGES, float, 1>;
   static const cudaError_t attr_rc =
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BF_SMEM);
@@ -1196,7 +1505,7 @@ void bf16_gemm_impl(int M, int N, int K, const float* a, i64 sam, i64 sak, const
 // warm-up, with CUDA events on the caller's stream, and keeps the fastest;
 // later products of the class reuse it.  The cost model above is the choice
 // while a stream is being captured into a graph and when TTG_AUTOTUNE=0;
-// TTG_AUTOTUNE=2 prints each choice.
+// TTG_AUTOTUNE=2 prints each choice; TTG_SPLIT_BN fixes the width instead.
 struct TuneKey {
   int mt, nt, kt, dbl;
   bool operator<(const TuneKey& o) const {
@@ -1231,6 +1540,13 @@ static int tuned_bn(int M, int N, int K, bool out_double, cudaStream_t s) {
     const char* v = std::getenv("TTG_AUTOTUNE");
     return !(v && v[0] == '0');
   }();
+  // TTG_SPLIT_BN=64|128|256 fixes the tile width of every split product
+  static const int forced = [] {
+    const char* v = std::getenv("TTG_SPLIT_BN");
+    const int b = v ? std::atoi(v) : 0;
+    return (b == 64 || b == 128 || b == 256) ? b : 0;
+  }();
+  if (forced) return forced;
   const int model = pick_bn(M, N, K);
   if (!enabled) return model;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1484,14 +1800,10 @@ static void core_apply(SplitOp* op, int nvec, cudaStream_t s) {
     for (int q = 0; q < JA; ++q)                                                                \
       for (int p = 0; p < NA; ++p)                                                              \
         cc.a[q * NA + p] = (q < ja && p < na) ? op->coef[(size_t)q * na + p] : 0.f;            \
-    if (wide)                                                                                   \
-      tc::core_small_kernel<JA, NA, 8><<<blocks, 128, 0, s>>>(                                 \
-          op->T1, op->ld1, cc, (int)L.rx1, (int)L.m, (int)L.ra2, (int)L.n, (int)L.ra1,         \
-          (int)L.ry2, nvec, lgR3, T2.ktiles, T2.hi, T2.lo);                                    \
-    else                                                                                        \
-      tc::core_small_kernel<JA, NA, 1><<<blocks, 128, 0, s>>>(                                 \
-          op->T1, op->ld1, cc, (int)L.rx1, (int)L.m, (int)L.ra2, (int)L.n, (int)L.ra1,         \
-          (int)L.ry2, nvec, lgR3, T2.ktiles, T2.hi, T2.lo);                                    \
+    launch_pdl(wide ? tc::core_small_kernel<JA, NA, 8> : tc::core_small_kernel<JA, NA, 1>,       \
+               dim3(blocks), dim3(128), 0, s, (const float*)op->T1, op->ld1, cc, (int)L.rx1,    \
+               (int)L.m, (int)L.ra2, (int)L.n, (int)L.ra1, (int)L.ry2, nvec, lgR3, T2.ktiles,   \
+               T2.hi, T2.lo);                                                                   \
   } while (0)
     switch (op->coef_kind) {
       case 1: TTG_CORE_SMALL(4, 4); break;
@@ -1507,17 +1819,16 @@ static void core_apply(SplitOp* op, int nvec, cudaStream_t s) {
     if (nz > 1 && !op->part) nz = 1, qchunk = ja;
     float* part = nz > 1 ? op->part : nullptr;
     dim3 grid((unsigned)ceil_div(rows, (i64)tc::CT_R), (unsigned)ceil_div(na, tc::CT_P), nz);
-    tc::core_tiled_kernel<<<grid, 256, 0, s>>>(op->T1, op->ld1, op->A, (int)L.rx1, (int)L.m,
-                                              (int)L.ra2, (int)L.n, (int)L.ra1, (int)L.ry2, nvec,
-                                              lgR3, T2.ktiles, T2.hi, T2.lo, qchunk, part);
+    launch_pdl(tc::core_tiled_kernel, grid, dim3(256), 0, s, (const float*)op->T1, op->ld1, op->A,
+               (int)L.rx1, (int)L.m, (int)L.ra2, (int)L.n, (int)L.ra1, (int)L.ry2, nvec, lgR3,
+               T2.ktiles, T2.hi, T2.lo, qchunk, part);
     if (part) {
-      TTG_CHECK_LAUNCH();
       const i64 tot = rows * na;
-      tc::core_finish_kernel<<<(int)std::min<i64>(4096, ceil_div(tot, (i64)256)), 256, 0, s>>>(
-          part, nz, rows, na, (int)L.rx1, (int)L.n, (int)L.ra1, lgR3, T2.ktiles, T2.hi, T2.lo);
+      launch_pdl(tc::core_finish_kernel, dim3((unsigned)std::min<i64>(4096, ceil_div(tot, (i64)256))),
+                 dim3(256), 0, s, (const float*)part, nz, rows, na, (int)L.rx1, (int)L.n,
+                 (int)L.ra1, lgR3, T2.ktiles, T2.hi, T2.lo);
     }
   }
-  TTG_CHECK_LAUNCH();
 }
 
 template <int BN1, int N3P, int JA, int NA>
