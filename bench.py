@@ -8,7 +8,7 @@ swept to convergence.  Metric: wall time of one full solve (lower is better).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--method plain|split]
-                  [--workload heisenberg20|xxz100|amen10|ksl16|batch256|matvec]
+                  [--workload heisenberg20|xxz100|amen10|ksl16|batch256|matvec|svd]
 
 The default workload (heisenberg20) is the metric's.  Two larger workloads
 are measured the same way, one timed run per method after a warm-up solve:
@@ -20,7 +20,8 @@ tau=1e-3 of dx/dt = A x, A = -(Dirichlet Laplacian, d=16, n=32) + a random
 rank-4 TT-matrix with N(0, 0.01^2) entries, x0 a random rank-8 TT vector of
 norm 1, with the split state's relative error against the FP64 state;
 batch256 = the batched chains (see batch_chains); matvec = the split and plain
-local matvecs alone at r=64 (block 5) and r=256 (block 8).
+local matvecs alone at r=64 (block 5) and r=256 (block 8); svd = the
+truncation SVD alone at the two workloads' block shapes.
 
 GPU arm: times K solves through the C-ABI with CUDA events on the library's
 stream (value), the same solves end to end from pinned host buffers (e2e),
@@ -341,6 +342,37 @@ def bench_matvec(args, torch, ttgpu, ctx):
     print(json.dumps(out))
 
 
+def bench_svd(args, torch, ttgpu, ctx):
+    """The truncation SVD alone (ttg_dgesvd: QR with column sorting, one-sided
+    Jacobi on R^T) on graded matrices of the sweeps' shapes: 320 x 128 (the
+    d=20 Heisenberg block, B ry x n ry = 5*64 x 2*64) and 2048 x 512 (the d=100
+    XXZ block, 8*256 x 2*256); mean of 5 calls after a warm-up, CUDA events."""
+    out = {"metric": "truncation SVD time (ms)", "shapes": {}}
+    for p, q in ((320, 128), (2048, 512)):
+        rng = np.random.default_rng(p + q)
+        r = min(p, q)
+        U0 = np.linalg.qr(rng.standard_normal((p, r)))[0]
+        V0 = np.linalg.qr(rng.standard_normal((q, r)))[0]
+        M = (U0 * np.logspace(0, -13, r)) @ V0.T
+        Md = torch.from_numpy(np.asfortranarray(M).ravel(order="F")).cuda()
+        U = torch.zeros(p * r, dtype=torch.float64, device="cuda")
+        sv = torch.zeros(r, dtype=torch.float64, device="cuda")
+        Vt = torch.zeros(r * q, dtype=torch.float64, device="cuda")
+        ttgpu.dgesvd(p, q, Md, U, sv, Vt, ctx=ctx)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            ttgpu.dgesvd(p, q, Md, U, sv, Vt, ctx=ctx)
+        e1.record()
+        torch.cuda.synchronize()
+        s_ref = np.linalg.svd(M, compute_uv=False)
+        out["shapes"]["%dx%d" % (p, q)] = {
+            "ms": e0.elapsed_time(e1) / 5,
+            "sigma_maxabs_err": float(np.abs(sv.cpu().numpy() - s_ref).max())}
+    print(json.dumps(out))
+
+
 def bench_batch(args, torch, ttgpu, ctx):
     """The batched configuration: independent chains queued on the batch
     runner (worker threads, one non-blocking stream each, longest first),
@@ -538,7 +570,8 @@ def main():
     ap.add_argument("--ksl-steps", type=int, default=200,
                     help="ksl16: time steps (the workload is 200)")
     ap.add_argument("--workload", default="heisenberg20",
-                    choices=["heisenberg20", "xxz100", "amen10", "ksl16", "batch256", "matvec"])
+                    choices=["heisenberg20", "xxz100", "amen10", "ksl16", "batch256", "matvec",
+                             "svd"])
     ap.add_argument("--batch-chains", type=int, default=256,
                     help="batch256: solve the first K of the 256 chains")
     ap.add_argument("--batch-workers", type=int, default=16)
@@ -579,6 +612,10 @@ def main():
     if args.workload == "matvec":
         if rank == 0:
             bench_matvec(args, torch, ttgpu, ctx)
+        return
+    if args.workload == "svd":
+        if rank == 0:
+            bench_svd(args, torch, ttgpu, ctx)
         return
     if args.workload == "batch256":
         if rank == 0:
