@@ -228,54 +228,3 @@ def test_dgesvd_jacobi(torch_cuda, ctx, pq):
         if gap > 1e-3 * s_ref[0]:
             assert abs(abs(Uh[:, j] @ Ur[:, j]) - 1) < 1e-10
 
-
-_SVD_CHILD = r"""
-import json, sys
-import numpy as np, torch
-import ttgpu
-from oracle import ops
-ctx = ttgpu.Context(0)
-out = []
-for p, q in json.loads(sys.argv[1]):
-    rng = np.random.default_rng(p * q + 1)
-    r = min(p, q)
-    U0 = np.linalg.qr(rng.standard_normal((p, r)))[0]
-    V0 = np.linalg.qr(rng.standard_normal((q, r)))[0]
-    M = (U0 * np.logspace(0, -13, r)) @ V0.T
-    t = torch.from_numpy(ops.flat(M)).cuda()
-    U = torch.zeros(p * r, dtype=torch.float64, device="cuda")
-    s = torch.zeros(r, dtype=torch.float64, device="cuda")
-    Vt = torch.zeros(r * q, dtype=torch.float64, device="cuda")
-    ttgpu.dgesvd(p, q, t, U, s, Vt, ctx=ctx)
-    ctx.synchronize()
-    out.append([s.cpu().numpy().tolist(), U.cpu().numpy().tolist(), Vt.cpu().numpy().tolist()])
-print(json.dumps(out))
-"""
-
-
-def test_svd_flow_rounds_match_barrier_rounds(torch_cuda):
-    """The barrier-free Jacobi rounds (column versions, default) against the
-    grid-barrier rounds (TTG_SVD_FLOW=0, read once per process, so each runs
-    in a child process): same pair order and arithmetic, so the factors agree
-    to rounding (1e-13 relative), on the QR-preconditioned path (square R^T,
-    odd column count with a dummy column), the FP32 pre-sweep path with rows
-    beyond the register cache, and the plain path."""
-    import json
-    import os
-    import subprocess
-    import sys
-    from conftest import ROOT
-    shapes = [(320, 128), (301, 41), (3000, 12), (2000, 5), (7, 3)]
-    res = {}
-    for mode in ("0", "1"):
-        env = dict(os.environ, TTG_SVD_FLOW=mode,
-                   PYTHONPATH=os.pathsep.join([ROOT, os.path.join(ROOT, "tt-fort_gb300")]))
-        out = subprocess.run([sys.executable, "-c", _SVD_CHILD, json.dumps(shapes)],
-                             capture_output=True, text=True, env=env, timeout=600)
-        assert out.returncode == 0, out.stderr[-2000:]
-        res[mode] = json.loads(out.stdout.strip().splitlines()[-1])
-    for (p, q), a, b in zip(shapes, res["0"], res["1"]):
-        for x, y in zip(a, b):
-            x, y = np.asarray(x), np.asarray(y)
-            assert np.all(np.isfinite(y)), (p, q)
-            assert np.abs(x - y).max() <= 1e-13 * max(1.0, np.abs(x).max()), (p, q)

@@ -420,170 +420,6 @@ __global__ void __launch_bounds__(SVD_CT) svd_sweep_kernel(int p, int q, T* M, T
   if (blockIdx.x == 0 && tid == 0 && status) *status = sweep;
 }
 
-// The same sweeps without a grid barrier between rounds.  Every column
-// carries a version (ver[c] = rounds completed on it); the CTA that owns pair
-// (a, b) of global round g waits until ver[a] and ver[b] reach g, rotates, and
-// publishes both at g + 1 (release store after the CTA's writes, acquire load
-// before its reads).  Each column is in exactly one pair per round, so a
-// pair depends only on the two pairs of the round before that held its
-// columns: rounds overlap across the GPU and a round costs a flag hand-off
-// instead of a grid-wide barrier.  Pair order, per-pair arithmetic,
-// thresholds and the stopping rule (a sweep without a counted rotation,
-// decided at a grid barrier per sweep) are those of svd_sweep_kernel, so the
-// results are the same.  All CTAs are co-resident (cooperative launch) and
-// every CTA takes its pairs in round order, so the waits form no cycle; each
-// is still bounded (about a second), and a wait that gives up sets
-// counters[2]: every CTA then leaves its rounds for the sweep's barrier, the
-// kernel writes *status = -1 and NaN into column 0 of M, so the singular
-// values the caller reads are NaN.
-constexpr long long SVD_FLOW_WAIT = 1ll << 20;
-constexpr int SVD_RC = 8;   // column rows kept in registers per thread
-
-__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_gpu(int* p, int v) {
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-template <class T>
-__global__ void __launch_bounds__(SVD_CT) svd_flow_kernel(int p, int q, T* M, T* V,
-                                                          int* counters, int* ver, int* status,
-                                                          int init_v, T tol, T tol_count,
-                                                          int max_sweeps) {
-  cg::grid_group grid = cg::this_grid();
-  __shared__ T red[3][SVD_CT / 32];
-  __shared__ T csn[2];
-  __shared__ int act, stop;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int K = (q + 1) & ~1;
-  const int npairs = K / 2;
-  volatile int* abort_flag = counters + 2;
-  if (!init_v)
-    for (i64 e = blockIdx.x * (i64)SVD_CT + tid; e < (i64)q * q; e += (i64)gridDim.x * SVD_CT)
-      V[e] = (e % q == e / q) ? T(1) : T(0);
-  for (int c = blockIdx.x * SVD_CT + tid; c < K; c += gridDim.x * SVD_CT) ver[c] = 0;
-  if (blockIdx.x == 0 && tid == 0) { counters[0] = 0; counters[1] = 0; counters[2] = 0; }
-  grid.sync();
-  int sweep = 0;
-  for (sweep = 0; sweep < max_sweeps; ++sweep) {
-    int* cnt = counters + (sweep & 1);
-    bool broken = false;
-    for (int r = 0; r < K - 1 && !broken; ++r) {
-      const int g = sweep * (K - 1) + r;
-      for (int pi = blockIdx.x; pi < npairs; pi += gridDim.x) {
-        int a, b;
-        rr_pair(K, r, pi, a, b);
-        if (tid == 0) {
-          int ok = 0;
-          for (long long it = 0; it < SVD_FLOW_WAIT; ++it) {
-            if (ld_acquire_gpu(ver + a) >= g && ld_acquire_gpu(ver + b) >= g) { ok = 1; break; }
-            if ((it & 255) == 255 && *abort_flag) break;
-          }
-          if (!ok) *abort_flag = 1;
-          stop = !ok;
-        }
-        __syncthreads();
-        if (stop) { broken = true; break; }
-        if (a < q && b < q) {
-          T* ca = M + (i64)p * a;
-          T* cb = M + (i64)p * b;
-          T* va = V + (i64)q * a;
-          T* vb = V + (i64)q * b;
-          // the pair's rows, read once from L2 (never a stale L1 line)
-          T xr[SVD_RC], yr[SVD_RC], ur[SVD_RC], wr[SVD_RC];
-#pragma unroll
-          for (int k = 0; k < SVD_RC; ++k) {
-            const int i = tid + k * SVD_CT;
-            xr[k] = i < p ? __ldcg(ca + i) : T(0);
-            yr[k] = i < p ? __ldcg(cb + i) : T(0);
-            ur[k] = i < q ? __ldcg(va + i) : T(0);
-            wr[k] = i < q ? __ldcg(vb + i) : T(0);
-          }
-          T al = 0, be = 0, ga = 0;
-#pragma unroll
-          for (int k = 0; k < SVD_RC; ++k) {
-            if (tid + k * SVD_CT < p) {
-              al = fma(xr[k], xr[k], al); be = fma(yr[k], yr[k], be); ga = fma(xr[k], yr[k], ga);
-            }
-          }
-          for (int i = tid + SVD_RC * SVD_CT; i < p; i += SVD_CT) {
-            const T x = __ldcg(ca + i), y = __ldcg(cb + i);
-            al = fma(x, x, al); be = fma(y, y, be); ga = fma(x, y, ga);
-          }
-          al = warp_sum_t(al); be = warp_sum_t(be); ga = warp_sum_t(ga);
-          if (lane == 0) { red[0][warp] = al; red[1][warp] = be; red[2][warp] = ga; }
-          __syncthreads();
-          if (tid == 0) {
-            T A = 0, Bv = 0, G = 0;
-            for (int w = 0; w < SVD_CT / 32; ++w) { A += red[0][w]; Bv += red[1][w]; G += red[2][w]; }
-            const T nab = sqrt(A * Bv);
-            int go = (G != T(0)) && (fabs(G) > tol * nab);
-            if (go) {
-              const T zeta = (Bv - A) / (T(2) * G);
-              const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-              const T c = T(1) / sqrt(T(1) + t * t);
-              csn[0] = c;
-              csn[1] = c * t;
-              if (fabs(G) > tol_count * nab) atomicAdd(cnt, 1);
-            }
-            act = go;
-          }
-          __syncthreads();
-          if (act) {
-            const T c = csn[0], sn = csn[1];
-#pragma unroll
-            for (int k = 0; k < SVD_RC; ++k) {
-              const int i = tid + k * SVD_CT;
-              if (i < p) {
-                ca[i] = c * xr[k] - sn * yr[k];
-                cb[i] = sn * xr[k] + c * yr[k];
-              }
-              if (i < q) {
-                va[i] = c * ur[k] - sn * wr[k];
-                vb[i] = sn * ur[k] + c * wr[k];
-              }
-            }
-            for (int i = tid + SVD_RC * SVD_CT; i < p; i += SVD_CT) {
-              const T x = __ldcg(ca + i), y = __ldcg(cb + i);
-              ca[i] = c * x - sn * y;
-              cb[i] = sn * x + c * y;
-            }
-            for (int i = tid + SVD_RC * SVD_CT; i < q; i += SVD_CT) {
-              const T x = __ldcg(va + i), y = __ldcg(vb + i);
-              va[i] = c * x - sn * y;
-              vb[i] = sn * x + c * y;
-            }
-          }
-        }
-        // publish: every thread's writes, then the release of both versions
-        __syncthreads();
-        if (tid == 0) {
-          __threadfence();
-          st_release_gpu(ver + a, g + 1);
-          st_release_gpu(ver + b, g + 1);
-        }
-      }
-    }
-    grid.sync();
-    const int aborted = *abort_flag;
-    int done = aborted || (*((volatile int*)cnt) == 0);
-    grid.sync();
-    if (blockIdx.x == 0 && tid == 0) counters[(sweep + 1) & 1] = 0;
-    grid.sync();
-    if (aborted) {
-      if (blockIdx.x == 0)
-        for (int i = tid; i < p; i += SVD_CT) M[i] = T(NAN);
-      sweep = -1;
-      break;
-    }
-    if (done) break;
-  }
-  if (blockIdx.x == 0 && tid == 0 && status) *status = sweep;
-}
-
 __global__ void d2f_kernel(i64 n, const double* __restrict__ a, float* __restrict__ b) {
   for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x)
     b[e] = (float)a[e];
@@ -602,37 +438,19 @@ static int svd_coop_blocks() {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, svd_sweep_kernel<T>, SVD_CT, 0) !=
             cudaSuccess)
       return 0;
-    int per2 = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, svd_flow_kernel<T>, SVD_CT, 0) !=
-        cudaSuccess)
-      return 0;
-    return nsm * std::min(per, per2);
+    return nsm * per;
   }();
   TTG_REQUIRE(max_coop > 0, "svd: occupancy query failed");
   return max_coop;
 }
 
-// counters: 4 ints, then the column versions of the barrier-free sweeps
-// (q + 1 ints); TTG_SVD_FLOW=0 selects the grid-barrier rounds instead
 template <class T>
 static void svd_sweeps(int p, int q, T* M, T* V, int* counters, int* status, int init_v, T tol,
                        T tol_count, int max_sweeps, cudaStream_t s) {
-  static const bool flow = [] {
-    const char* v = std::getenv("TTG_SVD_FLOW");
-    return !(v && v[0] == '0');
-  }();
   int blocks = std::max(1, std::min((q + 1) / 2, svd_coop_blocks<T>()));
-  if (flow) {
-    int* ver = counters + 4;
-    void* args[] = {&p, &q, &M, &V, &counters, &ver, &status, &init_v, &tol, &tol_count,
-                    &max_sweeps};
-    TTG_CUDA(cudaLaunchCooperativeKernel((void*)svd_flow_kernel<T>, dim3(blocks), dim3(SVD_CT),
-                                         args, 0, s));
-  } else {
-    void* args[] = {&p, &q, &M, &V, &counters, &status, &init_v, &tol, &tol_count, &max_sweeps};
-    TTG_CUDA(cudaLaunchCooperativeKernel((void*)svd_sweep_kernel<T>, dim3(blocks), dim3(SVD_CT),
-                                         args, 0, s));
-  }
+  void* args[] = {&p, &q, &M, &V, &counters, &status, &init_v, &tol, &tol_count, &max_sweeps};
+  TTG_CUDA(cudaLaunchCooperativeKernel((void*)svd_sweep_kernel<T>, dim3(blocks), dim3(SVD_CT),
+                                       args, 0, s));
   ++g_launches;
 }
 
@@ -1003,16 +821,12 @@ static size_t svd_qr_work(size_t p, size_t q) {
          coop + 64;
 }
 
-// counters (4 ints) and the column versions (up to q + 1 ints), in doubles
-static size_t svd_flag_doubles(size_t q) { return 64 + (q + 8) / 2; }
-
 size_t svd_scratch(int p, int q) {
   // working copy of M (max(p,q) x min(p,q)), V (min^2), norms, ranks, counters, Ut,
   // for the FP32 pre-sweeps two min^2 and one max x min temporaries, and the
   // workspace of the QR-preconditioned path
   size_t pp = std::max(p, q), qq = std::min(p, q);
-  return (pp * qq + qq * qq + 2 * qq + svd_flag_doubles(qq)) * sizeof(double) +
-         pp * qq * sizeof(double) +
+  return (pp * qq + qq * qq + 2 * qq + 64) * sizeof(double) + pp * qq * sizeof(double) +
          (2 * qq * qq + pp * qq) * sizeof(double) + svd_qr_work(pp, qq) * sizeof(double);
 }
 
@@ -1205,8 +1019,8 @@ void svd_jacobi(int p, int q, const double* M, double* U, double* sigma, double*
   double* V = Mw + (size_t)std::max(p, q) * r;            // r x r
   double* nrm = V + (size_t)r * r;                        // r
   int* rank = (int*)(nrm + r);                            // r ints (<= r doubles)
-  int* counters = (int*)(nrm + 2 * r);                    // counters and column versions
-  double* T = nrm + 2 * r + svd_flag_doubles(r);          // max x min (for p < q)
+  int* counters = (int*)(nrm + 2 * r);                    // 2 ints
+  double* T = nrm + 2 * r + 64;                           // max x min (for p < q)
   double* tmp = T + (size_t)std::max(p, q) * r;           // 2 min^2 + max x min
   double* qrw = tmp + 2 * (size_t)r * r + (size_t)std::max(p, q) * r;   // svd_qr_work
   if (p >= q) {
