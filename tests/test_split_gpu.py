@@ -31,6 +31,10 @@ SHAPES = [
     (32, 4, 16, 40, 4, 16, 2, 3, 2),
     (64, 1, 64, 100, 1, 64, 8, 8, 4),
     (60, 2, 33, 128, 2, 20, 3, 4, 9),
+    # core-contracted path (rx1 % 8 == 0, n*m <= 4) with ragged other sizes
+    (40, 2, 24, 48, 2, 56, 3, 4, 3),
+    (8, 1, 5, 7, 2, 6, 1, 5, 2),
+    (24, 2, 8, 16, 2, 8, 5, 1, 2),
 ]
 
 

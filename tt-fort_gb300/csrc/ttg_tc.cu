@@ -223,6 +223,42 @@ __global__ void split_kernel(const double* __restrict__ src, i64 rv, i64 vs, i64
   }
 }
 
+// The TT-matrix core contracted into Phi2 once per local problem:
+//   Q[mq, kq] = sum_a2 A(a1,i,j,a2) Phi2(b2,a2,c2),
+//   mq = (i + n*c2) + n*ry2*a1, kq = j + m*b2,
+// in FP64, then split and tiled as a 128-row A operand.  With Q the local
+// operator's first product gives its core-contracted intermediate directly:
+// T2[(i,c2,v),(b1,a1)] = sum_kq Q[(i,c2,a1), kq] X_v[b1, kq].  One thread per
+// (row, 8-wide K group) as in split_kernel; padding is written as zero.
+__global__ void build_q_kernel(const double* __restrict__ A, const double* __restrict__ phi2,
+                               int m, int rx2, int n, int ry2, int ra1, int ra2, int rtiles,
+                               int ktiles, bf16* __restrict__ hi, bf16* __restrict__ lo) {
+  const int nry2 = n * ry2, MQ = nry2 * ra1, KQ = m * rx2;
+  const i64 tr = (i64)rtiles * TM, tk8 = (i64)ktiles * (TK / 8);
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tr * tk8;
+       e += (i64)gridDim.x * blockDim.x) {
+    const int r = (int)(e % tr), k0 = (int)(e / tr) * 8;
+    const int ic2 = r % nry2, a1 = r / nry2, i = ic2 % n, c2 = ic2 / n;
+    __align__(16) bf16 h[8], l[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int kq = k0 + q;
+      double v = 0.0;
+      if (r < MQ && kq < KQ) {
+        const int j = kq % m, b2 = kq / m;
+        const double* a = A + a1 + (i64)ra1 * (i + (i64)n * j);   // a2 stride ra1*n*m
+        const double* p2 = phi2 + b2 + (i64)rx2 * ra2 * c2;      // a2 stride rx2
+        for (int a2 = 0; a2 < ra2; ++a2)
+          v = fma(a[(i64)ra1 * n * m * a2], p2[(i64)rx2 * a2], v);
+      }
+      split2(v, h[q], l[q]);
+    }
+    const size_t idx = tiled_index(r, k0, TM, ktiles);
+    *reinterpret_cast<uint4*>(hi + idx) = *reinterpret_cast<const uint4*>(h);
+    *reinterpret_cast<uint4*>(lo + idx) = *reinterpret_cast<const uint4*>(l);
+  }
+}
+
 // C[m, n] (m < M, n < N) = sum_k A[m, k] B[n, k], split-3 on tcgen05
 // (NPROD = 3: hi hi + hi lo + lo hi) or plain BF16 (NPROD = 1: hi hi only,
 // the lo planes are not read).
@@ -374,6 +410,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 0) tmem_dealloc(taddr, BN);
 }
 
+__device__ __forceinline__ size_t tiled_index_pow2(int r, int k, int lgR, int ktiles) {
+  const size_t tile = (size_t)(r >> lgR) * ktiles + (k >> 6);
+  return (tile << (lgR + 6)) + (tile_offset(r & ((1 << lgR) - 1), k & (TK - 1), 1 << lgR) >> 1);
+}
+__device__ __forceinline__ void split2f(float v, bf16& hi, bf16& lo) {
+  hi = __float2bfloat16_rn(v);
+  lo = __float2bfloat16_rn(v - __bfloat162float(hi));   // v - hi is exact in FP32
+}
+
 // ---------------------------------------------------------------------------
 // Persistent, warp-specialised form of the same product (same operand tile
 // layout, same output addressing, same K split).  One CTA per SM walks the
@@ -419,13 +464,25 @@ __host__ __device__ constexpr size_t ws_smem() {
   return (size_t)ws_stages<BN, NPROD>() * (NPROD == 3 ? 2 : 1) * (TM * TK * 2 + BN * TK * 2) + 1024;
 }
 
-template <int BN, class OutT, int NPROD = 3>
+// Epilogue that writes the product, split into bf16 hi/lo, straight into the
+// tiled B operand of the local operator's last product (EPI = 1): product row
+// mq = (i + n*c2) + n*ry2*a1, column nx = b1 + rx1*v go to operand row
+// i + n*c2 + n*ry2*v, K index b1 + rx1*a1.  rx1 is a multiple of 8, so the
+// eight columns of a 16-byte core-matrix row are eight consecutive b1 of one
+// v: each thread stores them as one 16-byte vector per plane.
+struct EpiT2 {
+  int rx1 = 8, nry2 = 1, lgR3 = 6, ktiles3 = 1;
+  bf16* hi = nullptr;
+  bf16* lo = nullptr;
+};
+
+template <int BN, class OutT, int NPROD = 3, int EPI = 0>
 __global__ void __launch_bounds__(WS_THREADS, 1)
     split_gemm_ws_kernel(const bf16* __restrict__ Ahi, const bf16* __restrict__ Alo,
                          const bf16* __restrict__ Bhi, const bf16* __restrict__ Blo, int M, int N,
                          int ktot, int mtiles, int ntiles, int nz, OutT* __restrict__ out,
                          i64 rpv, i64 vstride, i64 rstride, i64 cstride, int* __restrict__ err,
-                         int kchunk, i64 zstride) {
+                         int kchunk, i64 zstride, const EpiT2 ep) {
   static_assert(NPROD == 1 || NPROD == 3, "one or three bf16 products");
   static_assert(BN == 64 || BN == 128 || BN == 256, "tile width");
   constexpr int STAGES = ws_stages<BN, NPROD>();
@@ -599,11 +656,43 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
       }
       tc_fence_after();
       const int r = t % per_z, mt = r % mtiles, nt = r / mtiles;
-      OutT* o = out + (i64)(t / per_z) * zstride;
       const int row = mt * TM + q * 32 + lane;
-      OutT* orow = o + (row / rpv) * vstride + (row % rpv) * rstride;
       const int n0 = nt * BN;
       const uint32_t tbase = taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN);
+      if constexpr (EPI == 1) {
+        // operand row base (i + n*c2) and K base rx1*a1 of this product row
+        const int ic2 = row % ep.nry2, kb = ep.rx1 * (row / ep.nry2);
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+          uint32_t v[16];
+          tmem_ld16(tbase + (uint32_t)c0, v);
+          tmem_ld_wait();
+          if (c0 + 16 >= BN) {
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&acc_empty[acc]));
+          }
+          if (row < M) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const int nx = n0 + c0 + 8 * h;   // multiple of 8: eight b1 of one v
+              if (nx < N) {
+                const int vv = nx / ep.rx1, b1 = nx - vv * ep.rx1;
+                const size_t idx =
+                    tiled_index_pow2(ic2 + ep.nry2 * vv, b1 + kb, ep.lgR3, ep.ktiles3);
+                __align__(16) bf16 hh[8], ll[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) split2f(__uint_as_float(v[8 * h + e]), hh[e], ll[e]);
+                *reinterpret_cast<uint4*>(ep.hi + idx) = *reinterpret_cast<const uint4*>(hh);
+                *reinterpret_cast<uint4*>(ep.lo + idx) = *reinterpret_cast<const uint4*>(ll);
+              }
+            }
+          }
+        }
+        continue;
+      }
+      OutT* o = out + (i64)(t / per_z) * zstride;
+      OutT* orow = o + (row / rpv) * vstride + (row % rpv) * rstride;
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 16) {
         uint32_t v[16];
@@ -635,15 +724,6 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
 // T1 is column-major with leading dimension ld1 over the rows (b1,j,v), so
 // b1 is contiguous; the result is written split and tiled as the B operand of
 // GEMM3 (rows (i,c2,v), K (b1,a1), tile rows 1 << lgR3).
-
-__device__ __forceinline__ size_t tiled_index_pow2(int r, int k, int lgR, int ktiles) {
-  const size_t tile = (size_t)(r >> lgR) * ktiles + (k >> 6);
-  return (tile << (lgR + 6)) + (tile_offset(r & ((1 << lgR) - 1), k & (TK - 1), 1 << lgR) >> 1);
-}
-__device__ __forceinline__ void split2f(float v, bf16& hi, bf16& lo) {
-  hi = __float2bfloat16_rn(v);
-  lo = __float2bfloat16_rn(v - __bfloat162float(hi));   // v - hi is exact in FP32
-}
 
 // the TT-matrix core as a kernel parameter: a[q * NA + p] = A(a1,i,j,a2) with
 // q = j + m*a2 and p = a1 + ra1*i, so every FMA reads it from the constant bank
@@ -1328,13 +1408,13 @@ static void split_into(const double* src, i64 rv, i64 vs, i64 sr, i64 sk, const 
 }
 
 // persistent launch: one CTA per SM, at most one per output tile
-template <int BN, class OutT, int NPROD>
+template <int BN, class OutT, int NPROD, int EPI = 0>
 static void ws_launch(const bf16* Ahi, const bf16* Alo, const bf16* Bhi, const bf16* Blo, int M,
                       int N, int ktot, int mtiles, int ntiles, int nz, OutT* out, i64 rpv,
                       i64 vstride, i64 rstride, i64 cstride, int* err, int kchunk, i64 zstride,
-                      cudaStream_t s) {
+                      cudaStream_t s, const EpiT2& ep = EpiT2()) {
   constexpr size_t smem = ws_smem<BN, NPROD>();
-  auto kern = split_gemm_ws_kernel<BN, OutT, NPROD>;
+  auto kern = split_gemm_ws_kernel<BN, OutT, NPROD, EPI>;
   static const cudaError_t attr_rc =
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   TTG_CUDA(attr_rc);
@@ -1342,7 +1422,7 @@ static void ws_launch(const bf16* Ahi, const bf16* Alo, const bf16* Bhi, const b
   TTG_REQUIRE(total < (1ll << 31), "split gemm: too many tiles");
   const int grid = (int)std::min<i64>(total, num_sms());
   launch_pdl(kern, dim3(grid), dim3(WS_THREADS), smem, s, Ahi, Alo, Bhi, Blo, M, N, ktot, mtiles,
-             ntiles, nz, out, rpv, vstride, rstride, cstride, err, kchunk, zstride);
+             ntiles, nz, out, rpv, vstride, rstride, cstride, err, kchunk, zstride, ep);
 }
 
 template <int BN, class OutT>
@@ -1373,6 +1453,24 @@ static void gemm_launch(const Tiled& A, const Tiled& B, int M, int N, OutT* out,
   if (B.R == 256) gemm_launch_bn<256>(A, B, M, N, out, rpv, vstride, rstride, cstride, err, s);
   else if (B.R == 128) gemm_launch_bn<128>(A, B, M, N, out, rpv, vstride, rstride, cstride, err, s);
   else gemm_launch_bn<64>(A, B, M, N, out, rpv, vstride, rstride, cstride, err, s);
+}
+
+// product whose epilogue writes the split T2 operand (EPI = 1)
+static void gemm_launch_t2(const Tiled& A, const Tiled& B, int M, int N, const EpiT2& ep, int* err,
+                           cudaStream_t s) {
+  TTG_REQUIRE(A.ktiles == B.ktiles, "split gemm: K tiles differ");
+  TTG_REQUIRE(A.R == TM, "split gemm: A tiles must have 128 rows");
+  TTG_REQUIRE(ep.rx1 % 8 == 0 && N % 8 == 0, "split gemm: T2 epilogue needs rx1 % 8 == 0");
+  float* none = nullptr;
+  if (B.R == 256)
+    ws_launch<256, float, 3, 1>(A.hi, A.lo, B.hi, B.lo, M, N, A.ktiles, A.rtiles, B.rtiles, 1, none,
+                                1ll << 40, 0, 1, 0, err, 0, 0, s, ep);
+  else if (B.R == 128)
+    ws_launch<128, float, 3, 1>(A.hi, A.lo, B.hi, B.lo, M, N, A.ktiles, A.rtiles, B.rtiles, 1, none,
+                                1ll << 40, 0, 1, 0, err, 0, 0, s, ep);
+  else
+    ws_launch<64, float, 3, 1>(A.hi, A.lo, B.hi, B.lo, M, N, A.ktiles, A.rtiles, B.rtiles, 1, none,
+                               1ll << 40, 0, 1, 0, err, 0, 0, s, ep);
 }
 
 // ---------------------------------------------------------------------------
@@ -1619,6 +1717,11 @@ struct SplitOp {
   float* part;          // K-chunk partials of the tiled CORE kernel (or null)
   int coef_kind;        // 0: tiled CORE kernel; 1..4: small CORE with (JA, NA) bound
   float coef[256];      // A as FP32 in its own column-major order (small CORE)
+  // core-contracted path: Q = A x Phi2 built at prepare, one product writes
+  // the last product's operand (no T1, no CORE launch); X tiled as its B
+  // operand (rows (b1,v), K (j,b2))
+  bool pre = false;
+  tc::Tiled Q;
   // fused single-launch path (fused_small_kernel) when the shape allows it
   bool fused = false;
   int fbn1 = 0, fn3p = 0, fC = 0, fntiles = 0;
@@ -1669,10 +1772,54 @@ static bool fused_plan(const LocalDims& L, int nvec, int& bn1, int& n3p, int& C,
   return true;
 }
 
+// The core-contracted path for small mode sizes (n*m <= 4: spin chains),
+// where contracting A into Phi2 costs the first product only n*ra1/ra2 times
+// its FLOPs but saves the FP32 intermediate T1 (written and read back once per
+// apply) and the CUDA-core CORE launch; rx1 a multiple of 8 for the 16-byte
+// epilogue stores.  TTG_SPLIT_PRE=0 keeps the four-launch path.
+static bool pre_plan(const LocalDims& L) {
+  static const bool enabled = [] {
+    const char* v = std::getenv("TTG_SPLIT_PRE");
+    return !(v && v[0] == '0');
+  }();
+  return enabled && tc::use_ws() && L.rx1 % 8 == 0 && L.n * L.m <= 4;
+}
+
 // Sizing (op == nullptr) takes the widest tile padding so that the bytes
 // bound every tile width the autotuner may pick at layout time.
 static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* base,
                            cudaStream_t s = nullptr) {
+  {
+    int b_, n_, c_, t_;
+    if (!fused_plan(L, nvec_max, b_, n_, c_, t_) && pre_plan(L)) {
+      const int MQ = (int)(L.n * L.ry2 * L.ra1), KQ = (int)(L.m * L.rx2);
+      const int NX = (int)(L.rx1 * nvec_max);
+      const int M3 = (int)L.ry1, N3 = (int)(L.n * L.ry2 * nvec_max), K3 = (int)(L.rx1 * L.ra1);
+      const bool sizing = !(op && base);
+      const int bnq = sizing ? 256 : tc::tuned_bn(MQ, NX, KQ, false, s);
+      const int bn3 = sizing ? 256 : tc::tuned_bn(M3, N3, K3, true, s);
+      size_t tot = tc::tiled_bytes(MQ, KQ, tc::TM) + tc::tiled_bytes(NX, KQ, bnq) +
+                   tc::tiled_bytes(M3, K3, tc::TM) + tc::tiled_bytes(N3, K3, bn3) + 1024 +
+                   sizeof(SplitOp) + 1024;
+      if (op && base) {
+        char* p = base;
+        op->L = L;
+        op->nvec_max = nvec_max;
+        op->bn1 = bnq; op->bn3 = bn3;
+        op->pre = true;
+        op->fused = false;
+        op->Q = tc::make_tiled(MQ, KQ, tc::TM, p);
+        op->X = tc::make_tiled(NX, KQ, bnq, p);
+        op->P1 = tc::make_tiled(M3, K3, tc::TM, p);
+        op->T2 = tc::make_tiled(N3, K3, bn3, p);
+        op->T1 = nullptr;
+        op->ld1 = 0;
+        op->err = (int*)p; p += 1024;
+        op->part = nullptr;
+      }
+      return tot;
+    }
+  }
   const int M1 = (int)(L.rx1 * L.m * nvec_max), N1 = (int)(L.ra2 * L.ry2), K1 = (int)L.rx2;
   const int M3 = (int)L.ry1, N3 = (int)(L.n * L.ry2 * nvec_max), K3 = (int)(L.rx1 * L.ra1);
   const bool sizing = !(op && base);
@@ -1716,6 +1863,7 @@ static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* 
     op->L = L;
     op->nvec_max = nvec_max;
     op->bn1 = bn1; op->bn3 = bn3;
+    op->pre = false;
     op->X = tc::make_tiled(M1, K1, tc::TM, p);
     op->P2 = tc::make_tiled(N1, K1, bn1, p);
     op->P1 = tc::make_tiled(M3, K3, tc::TM, p);
@@ -1750,6 +1898,19 @@ void split_op_prepare(SplitOp* op, const LocalDims& L, int nvec_max, const doubl
                       const double* A, const double* phi2, void* mem, cudaStream_t s) {
   split_layout(L, nvec_max, op, (char*)mem, s);
   op->A = A;
+  if (op->pre) {
+    const i64 total = (i64)op->Q.rtiles * tc::TM * op->Q.ktiles * (tc::TK / 8);
+    tc::build_q_kernel<<<(int)std::min<i64>(8192, (total + 255) / 256), 256, 0, s>>>(
+        A, phi2, (int)L.m, (int)L.rx2, (int)L.n, (int)L.ry2, (int)L.ra1, (int)L.ra2,
+        op->Q.rtiles, op->Q.ktiles, op->Q.hi, op->Q.lo);
+    TTG_CHECK_LAUNCH();
+    tc::split_into(phi1, 1ll << 40, 0, 1, L.ry1, op->P1, s);
+    TTG_CUDA(cudaMemsetAsync(op->err, 0, sizeof(int), s));
+    // K columns of T2 beyond rx1*ra1 must be zero (they meet Phi1's zero padding)
+    TTG_CUDA(cudaMemsetAsync(op->T2.hi, 0, op->T2.elems() * sizeof(tc::bf16), s));
+    TTG_CUDA(cudaMemsetAsync(op->T2.lo, 0, op->T2.elems() * sizeof(tc::bf16), s));
+    return;
+  }
   // small TT-matrix cores travel as a kernel parameter of the CORE kernel
   const int ja = (int)(L.m * L.ra2), na = (int)(L.n * L.ra1);
   op->coef_kind = 0;
@@ -1883,6 +2044,27 @@ void split_op_apply(SplitOp* op, const double* x, double* y, int nvec, cudaStrea
   TTG_REQUIRE(nvec >= 1 && nvec <= op->nvec_max, "split matvec: nvec out of range");
   if (op->fused) {
     fused_apply(op, x, y, nvec, s);
+    return;
+  }
+  if (op->pre) {
+    // X_v element (row (b1,v), k=(j,b2)) at x[v*xsize + b1 + rx1*k]
+    const int NX = (int)(L.rx1 * nvec), MQ = (int)(L.n * L.ry2 * L.ra1);
+    tc::Tiled X = op->X;
+    X.rows = NX;
+    X.rtiles = ceil_div(NX, X.R);
+    tc::split_into(x, L.rx1, L.xsize(), 1, L.rx1, X, s);
+    tc::Tiled T2b = op->T2;
+    const int N3 = (int)(L.n * L.ry2 * nvec);
+    T2b.rtiles = ceil_div(N3, T2b.R);
+    tc::EpiT2 ep;
+    ep.rx1 = (int)L.rx1;
+    ep.nry2 = (int)(L.n * L.ry2);
+    ep.lgR3 = T2b.R == 256 ? 8 : (T2b.R == 128 ? 7 : 6);
+    ep.ktiles3 = T2b.ktiles;
+    ep.hi = T2b.hi;
+    ep.lo = T2b.lo;
+    tc::gemm_launch_t2(op->Q, X, MQ, NX, ep, op->err, s);
+    tc::gemm_launch<double>(op->P1, T2b, (int)L.ry1, N3, y, 1ll << 40, 0, 1, L.ry1, op->err, s);
     return;
   }
   const int M1 = (int)(L.rx1 * L.m * nvec), N1 = (int)(L.ra2 * L.ry2);
