@@ -135,10 +135,11 @@ def fp64_peak_tflops(torch):
 
 
 # DRAM bytes (read + write) of one split block matvec at r=64, n=2, ra=5, 5
-# vectors: the sum over its four launches (split X, GEMM1, CORE, GEMM3) in one
-# ncu capture (profiles/split_matvec_r64_b5_traffic.md), cold L2 per launch
-SPLIT_MV_TRAFFIC = 339200 + 270592 + 843008 + 1008640
-SPLIT_MV_TRAFFIC_NOTE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum summed over the four "
+# vectors: the sum over its three launches (split X, the core-contracted first
+# product, the last product) in one ncu capture
+# (profiles/split_matvec_r64_b5_traffic.md), cold L2 per launch
+SPLIT_MV_TRAFFIC = 337920 + 517632 + 1012992
+SPLIT_MV_TRAFFIC_NOTE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum summed over the three "
                          "launches of one apply, cold L2 (profiles/split_matvec_r64_b5_traffic.md)")
 
 

@@ -103,8 +103,6 @@ struct PhaseTimer {
     fprintf(stderr, "[ttg profile]   fp64 matvecs %lld of %lld\n", fp64_mv_report, all_mv_report);
   }
   long long fp64_mv_report = 0, all_mv_report = 0;
-  void dummy() {
-  }
 };
 
 static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {

@@ -1,15 +1,22 @@
 // Split-precision (BF16x3) tensor-core local operator for sm_103a.
 //
-// y = Phi1 * A * Phi2 * x  (dbfun3, ttals.f90:9-32) as two tcgen05 GEMMs and a
-// CUDA-core contraction with the TT-matrix core:
+// y = Phi1 * A * Phi2 * x  (dbfun3, ttals.f90:9-32).  Two forms:
 //
+// Core-contracted (small mode sizes, n*m <= 4, rx1 % 8 == 0: the spin chains
+// of tt_eigb): the TT-matrix core is folded into Phi2 once per local problem,
+//   Q      Q[(i,c2,a1), (j,b2)] = sum_a2 A(a1,i,j,a2) Phi2(b2,a2,c2)   (FP64)
+//   GEMM1  T2[(i,c2,v), (b1,a1)] = sum_(j,b2) Q[(i,c2,a1),(j,b2)] X_v[b1,(j,b2)]
+//          M = n*ry2*ra1, N = rx1*nvec, K = m*rx2; the epilogue writes T2 split
+//          and tiled as the B operand of GEMM3 (no FP32 intermediate)
+//   GEMM3  Y[c1, (i,c2,v)]       = sum_(b1,a1) Phi1[c1,(b1,a1)] T2[(i,c2,v),(b1,a1)]
+//          M = ry1, N = n*ry2*nvec, K = rx1*ra1
+// General (any mode size): two tcgen05 GEMMs around a CUDA-core contraction,
 //   GEMM1  T1[(b1,j,v), (a2,c2)] = sum_b2 X_v[(b1,j), b2] Phi2[b2, (a2,c2)]
 //          M = rx1*m*nvec (all vectors of the block stacked), N = ra2*ry2, K = rx2
 //   CORE   T2[(i,c2,v), (b1,a1)] = sum_(j,a2) A[(a1,i),(j,a2)] T1[(b1,j,v),(a2,c2)]
-//   GEMM3  Y[c1, (i,c2,v)]       = sum_(b1,a1) Phi1[c1,(b1,a1)] T2[(i,c2,v),(b1,a1)]
-//          M = ry1, N = n*ry2*nvec, K = rx1*ra1
+//   GEMM3  as above.
 //
-// Both GEMMs put the index that is contiguous in their output (b1 in T1, c1
+// The GEMMs put the index that is contiguous in their output (b1 in T1, c1
 // in y) on the MMA M side, i.e. on TMEM lanes, so the epilogue stores of a
 // warp are coalesced.
 // Every FP64 operand a is split as a_hi = bf16(a), a_lo = bf16(a - a_hi) and a
@@ -18,15 +25,17 @@
 // are stored in global memory already in the tcgen05 K-major, no-swizzle
 // canonical layout, tile by tile (128 or BN rows x 64 K-elements, core
 // matrices of 8 rows x 16 bytes), so each pipeline stage is a handful of
-// contiguous cp.async.bulk copies completing on an mbarrier.  One thread
-// issues the MMAs (3 per 16-wide K step), tcgen05.commit releases the smem
-// stage, and four epilogue warps read the FP32 accumulator with tcgen05.ld.
-// Phi1 and Phi2 are split once per local problem (split_op_prepare); X is
+// contiguous cp.async.bulk copies completing on an mbarrier.  The products
+// run in a persistent warp-specialised kernel (split_gemm_ws_kernel: one
+// copy thread, one MMA thread issuing 3 MMAs per 16-wide K step, eight
+// epilogue warps reading a double-buffered FP32 accumulator with tcgen05.ld);
+// split_gemm_kernel is the one-tile-per-CTA form (TTG_GEMM_WS=0).
+// Phi1, Phi2 (or Q) are split once per local problem (split_op_prepare); X is
 // split per call.
 //
 // Every mbarrier wait is bounded: on timeout the kernel records an error
-// code, waits (bounded) for the MMAs it issued, frees its tensor memory and
-// returns; the host turns the code into TTG_ERR_CUDA.
+// code, waits (bounded) for the copies and MMAs it issued, frees its tensor
+// memory and returns; the host turns the code into TTG_ERR_CUDA.
 #include "ttg_davidson.cuh"
 #include <cuda_bf16.h>
 #include <cstdlib>
@@ -423,23 +432,29 @@ __device__ __forceinline__ void split2f(float v, bf16& hi, bf16& lo) {
 // Persistent, warp-specialised form of the same product (same operand tile
 // layout, same output addressing, same K split).  One CTA per SM walks the
 // output tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...; tile t is
-// (mt, nt, z) with mt fastest.  Six warps:
+// (mt, nt, z) with mt fastest.  Ten warps:
 //   warp 0 (one lane)  bulk copies of the A/B stages into a STAGES-deep ring,
 //                      running ahead across tile boundaries;
 //   warp 1 (one lane)  tcgen05.mma issue; owns the tensor memory, two FP32
 //                      accumulators of BN columns, used alternately by
 //                      consecutive tiles of the CTA;
-//   warps 2-5          epilogue: warp w reads TMEM lanes 32*(w%4).. with
-//                      tcgen05.ld and stores them, while the MMAs of the
-//                      next tile run on the other accumulator.
+//   warps 2-9          epilogue: warp w reads TMEM lanes 32*(w%4).. of one
+//                      half of the columns ((w-2)/4) with tcgen05.ld and
+//                      stores them, while the MMAs of the next tile run on
+//                      the other accumulator (eight storing warps per SM:
+//                      four cannot keep enough stores in flight).
 // Ring barriers: full[s] (copies landed), empty[s] (MMAs that read the stage
 // done, tcgen05.commit); accumulator barriers: acc_full[a] (tile's MMAs done,
-// tcgen05.commit) and acc_empty[a] (the four epilogue warps have read it).
+// tcgen05.commit) and acc_empty[a] (the eight epilogue warps have read it).
 // Every wait is bounded and also gives up once another role has failed; a
 // failing CTA records the code in *err, waits (bounded) for the copies and
 // MMAs it issued and frees its tensor memory.
 // ---------------------------------------------------------------------------
-constexpr int WS_THREADS = 192;
+#ifndef TTG_WS_EPI_WARPS
+#define TTG_WS_EPI_WARPS 8
+#endif
+constexpr int WS_EPI_WARPS = TTG_WS_EPI_WARPS;   // 4, 8 or 16
+constexpr int WS_THREADS = 64 + 32 * WS_EPI_WARPS;
 
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
@@ -513,7 +528,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
     }
     for (int a = 0; a < 2; ++a) {
       mbar_init(smem_u32(&acc_full[a]), 1);
-      mbar_init(smem_u32(&acc_empty[a]), 4);
+      mbar_init(smem_u32(&acc_empty[a]), WS_EPI_WARPS);
     }
     mbar_init(smem_u32(&done_bar), 1);
     fail_s = 0;
@@ -642,6 +657,9 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
   } else {
     // ---- epilogue ----
     const int q = warp & 3;   // TMEM lane quadrant this warp may read
+    constexpr int CW = BN / (WS_EPI_WARPS / 4);   // columns per epilogue warp
+    static_assert(CW % 16 == 0, "epilogue column share");
+    const int cb = ((warp - 2) >> 2) * CW, ce = cb + CW;   // its columns
     int lt = 0;
     for (int t = blockIdx.x; t < total; t += gridDim.x, ++lt) {
       const int acc = lt & 1, use = lt >> 1;
@@ -663,11 +681,11 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
         // operand row base (i + n*c2) and K base rx1*a1 of this product row
         const int ic2 = row % ep.nry2, kb = ep.rx1 * (row / ep.nry2);
 #pragma unroll 1
-        for (int c0 = 0; c0 < BN; c0 += 16) {
+        for (int c0 = cb; c0 < ce; c0 += 16) {
           uint32_t v[16];
           tmem_ld16(tbase + (uint32_t)c0, v);
           tmem_ld_wait();
-          if (c0 + 16 >= BN) {
+          if (c0 + 16 >= ce) {
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(smem_u32(&acc_empty[acc]));
@@ -694,12 +712,12 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
       OutT* o = out + (i64)(t / per_z) * zstride;
       OutT* orow = o + (row / rpv) * vstride + (row % rpv) * rstride;
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 16) {
+      for (int c0 = cb; c0 < ce; c0 += 16) {
         uint32_t v[16];
         tmem_ld16(tbase + (uint32_t)c0, v);
         tmem_ld_wait();
-        if (c0 + 16 >= BN) {
-          // the whole accumulator is in registers: hand it back to the MMAs
+        if (c0 + 16 >= ce) {
+          // this warp's share of the accumulator is in registers: hand it back
           tc_fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(smem_u32(&acc_empty[acc]));
