@@ -377,17 +377,28 @@ __global__ void __launch_bounds__(SVD_CT) svd_sweep_kernel(int p, int q, T* M, T
         if (tid == 0) {
           T A = 0, Bv = 0, G = 0;
           for (int w = 0; w < SVD_CT / 32; ++w) { A += red[0][w]; Bv += red[1][w]; G += red[2][w]; }
-          const T nab = sqrt(A * Bv);
-          int go = (G != T(0)) && (fabs(G) > tol * nab);
+          // |G| > tol sqrt(A Bv), compared in squares (no square root)
+          const T g2 = G * G, ab = A * Bv;
+          int go = (G != T(0)) && (g2 > tol * tol * ab);
           if (go) {
-            const T zeta = (Bv - A) / (T(2) * G);
-            const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-            const T c = T(1) / sqrt(T(1) + t * t);
+            // The angle is taken in FP32 (GB300 runs FP64 square roots and
+            // divides as long dependent chains on a narrow pipe, and this is
+            // the serial part of every round); c and s are formed in T from
+            // that t, c = 1/sqrt(1 + t^2), s = c t, so the rotation is
+            // orthogonal to T's precision whatever t is.  A t off by FP32
+            // rounding leaves an off-diagonal ~1e-7 of G, which the next
+            // sweep removes like any other; the stopping test is unchanged.
+            const T zeta_t = (Bv - A) / (T(2) * G);
+            const float z = (float)zeta_t, az = fabsf(z);
+            // |zeta| beyond FP32's comfortable range: t = 1/(2 zeta) in T
+            const T t = az < 1e18f ? (T)copysignf(1.f / (az + sqrtf(1.f + z * z)), z)
+                                   : T(0.5) / zeta_t;
+            const T c = rsqrt(T(1) + t * t);
             csn[0] = c;
             csn[1] = c * t;
             // rotations whose cosine is within the rounding noise of a dot
             // product of length p are applied but do not keep the sweeps going
-            if (fabs(G) > tol_count * nab) atomicAdd(cnt, 1);
+            if (g2 > tol_count * tol_count * ab) atomicAdd(cnt, 1);
           }
           act = go;
         }
@@ -798,13 +809,12 @@ __global__ void rt_kernel(int q, const double* __restrict__ A, i64 lda, double* 
   }
 }
 // C (p x q) = [Vtx^T; 0]
-__global__ void qr_c0_kernel(int p, int q, const double* __restrict__ Vtx, double* __restrict__ C) {
+__global__ void qr_c0n_kernel(int p, int q, const double* __restrict__ Ux, double* __restrict__ C) {
   for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)p * q; e += (i64)gridDim.x * blockDim.x) {
     const int i = (int)(e % p), k = (int)(e / p);
-    C[e] = i < q ? Vtx[k + (i64)q * i] : 0.0;
+    C[e] = i < q ? Ux[i + (i64)q * k] : 0.0;
   }
 }
-// Vt[k, j] = Ux[rank[j], k]
 __global__ void qr_vt_kernel(int q, const double* __restrict__ Ux, const int* __restrict__ perm,
                              double* __restrict__ Vt) {
   for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)q * q; e += (i64)gridDim.x * blockDim.x) {
@@ -817,8 +827,10 @@ __global__ void qr_vt_kernel(int q, const double* __restrict__ Ux, const int* __
 static size_t svd_qr_work(size_t p, size_t q) {
   const size_t npan = (q + QRP_NB - 1) / QRP_NB;
   const size_t coop = QRP_NB * QRC_GMAX + QRP_NB * QRC_GMAX * QRP_NB + QRC_GMAX * QRP_NB * QRP_NB;
+  // first QR (A, X, Ux, Vtx, Tf, Yp, G1, G2, tau, perm, coop partials), then
+  // the second QR's R2^T, Q2 V2, T factors and tau
   return p * q + 3 * q * q + npan * QRP_NB * QRP_NB + p * QRP_NB + 2 * QRP_NB * q + 2 * q + 256 +
-         coop + 64;
+         coop + 64 + 2 * q * q + npan * QRP_NB * QRP_NB + q + 64;
 }
 
 size_t svd_scratch(int p, int q) {
@@ -836,21 +848,40 @@ static void svd_tall(int p, int q, double* Mw, double* U, double* sigma, double*
                      double* V, double* nrm, int* rank, int* counters, int* status,
                      double* tmp, cudaStream_t s, double* qrwork = nullptr);
 
+// The QR-preconditioned path (q >= SVD_QR_MIN_Q):
+//   M P = Q1 R1        columns sorted by norm, blocked Householder QR
+//   R1^T = Q2 R2       for q >= SVD_QR2_MIN_Q a second QR, of R1^T
+//   R2^T = U2 S V2^T   one-sided Jacobi on R2^T (rotations accumulated in V2)
+// so M = (Q1 U2) S (P Q2 V2)^T; without the second QR (Q2 = I, R2 = R1)
+// the Jacobi runs on R1^T itself and M = (Q1 V2') S (P U2')^T with the roles
+// of the factors exchanged.  The second QR leaves R2^T closer to orthogonal
+// columns: on graded blocks (singular values 1 to 1e-13) the sweeps drop
+// from 9-10 to about 6; measured on GB300 that pays from q ~ 200 (2048 x 512:
+// 59.2 -> 53.8 ms) but not at q = 128 (320 x 128: 7.6 -> 7.3 ms, and the
+// d=20 solve, whose blocks are mostly narrower, slower by its ~30 extra
+// launches per SVD).
+constexpr int SVD_QR2_MIN_Q = 192;
 static void svd_tall_qr(int p, int q, double* Mw, double* U, double* sigma, double* Vt,
                         double* V, double* nrm, int* rank, int* counters, int* status,
                         double* tmp, double* work, cudaStream_t s) {
   const int npan = ceil_div(q, QRP_NB);
   double* A = work;                                     // p x q
-  double* X = A + (size_t)p * q;                        // q x q
+  double* X = A + (size_t)p * q;                        // q x q: R1^T, then its QR
   double* Ux = X + (size_t)q * q;                       // q x q
   double* Vtx = Ux + (size_t)q * q;                     // q x q
-  double* Tf = Vtx + (size_t)q * q;                     // NB x NB per panel
+  double* Tf = Vtx + (size_t)q * q;                     // NB x NB per panel (first QR)
   double* Yp = Tf + (size_t)npan * QRP_NB * QRP_NB;     // p x NB
   double* G1 = Yp + (size_t)p * QRP_NB;                 // NB x q
   double* G2 = G1 + (size_t)QRP_NB * q;                 // NB x q
   double* tau = G2 + (size_t)QRP_NB * q;                // q
   int* perm = (int*)(tau + q);                          // q ints
   double* qpart = tau + 2 * (size_t)q + 64;             // cooperative panel partials
+  const size_t coop = (size_t)QRP_NB * QRC_GMAX + (size_t)QRP_NB * QRC_GMAX * QRP_NB +
+                      (size_t)QRC_GMAX * QRP_NB * QRP_NB;
+  double* X2 = qpart + coop;                            // q x q: R2^T, Jacobi
+  double* W = X2 + (size_t)q * q;                       // q x q: Q2 V2
+  double* Tf2 = W + (size_t)q * q;                      // NB x NB per panel (second QR)
+  double* tau2 = Tf2 + (size_t)npan * QRP_NB * QRP_NB;  // q
   auto gemm = [&](int M, int N, int K, const double* Am, i64 sAm, i64 sAk, const double* Bm,
                   i64 sBk, i64 sBn, double* C, i64 sCm, i64 sCn, double alpha, double beta) {
     GemmF64 g;
@@ -861,6 +892,59 @@ static void svd_tall_qr(int p, int q, double* Mw, double* U, double* sigma, doub
     g.alpha = alpha; g.beta = beta;
     gemm_f64(g, s);
   };
+  // blocked Householder QR of F (rows x q, leading dimension rows) in place:
+  // reflectors below the diagonal, R on and above it, panel T factors in Tk
+  auto qr_factor = [&](int rows, double* F, double* Tfac, double* tv) {
+    for (int k = 0; k < npan; ++k) {
+      const int j0 = k * QRP_NB, w = std::min(QRP_NB, q - j0), m = rows - j0;
+      double* Ap = F + j0 + (i64)rows * j0;
+      double* Tk = Tfac + (size_t)k * QRP_NB * QRP_NB;
+      if (m >= 1024) {
+        static const int coop_max = [] {
+          int dev = 0, nsm = 0, per = 0;
+          cudaGetDevice(&dev);
+          cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, qr_panel_coop_kernel, QRC_NT, 0);
+          return std::max(1, nsm * per);
+        }();
+        int G = std::min(std::min(QRC_GMAX, std::max(1, m / 128)), coop_max);
+        int mm = m, ww = w, ldt = QRP_NB;
+        i64 ld = rows;
+        double* tk = tv + j0;
+        void* args[] = {&mm, &ww, &Ap, &ld, &tk, &Tk, &ldt, &qpart};
+        TTG_CUDA(cudaLaunchCooperativeKernel((const void*)qr_panel_coop_kernel, dim3(G),
+                                             dim3(QRC_NT), args, 0, s));
+        ++g_launches;
+      } else {
+        qr_panel_kernel<<<1, QRP_NT, 0, s>>>(m, w, Ap, rows, tv + j0, Tk, QRP_NB);
+        TTG_CHECK_LAUNCH();
+      }
+      const int n2 = q - j0 - w;
+      if (n2 > 0) {
+        qr_make_y_kernel<<<gbl((i64)m * w), 256, 0, s>>>(m, w, Ap, rows, Yp);
+        TTG_CHECK_LAUNCH();
+        double* A2 = Ap + (i64)rows * w;
+        gemm(w, n2, m, Yp, m, 1, A2, 1, rows, G1, 1, w, 1.0, 0.0);     // G1 = Y^T A2
+        gemm(w, n2, w, Tk, QRP_NB, 1, G1, 1, w, G2, 1, w, 1.0, 0.0);   // G2 = T^T G1
+        gemm(m, n2, w, Yp, 1, m, G2, 1, w, A2, 1, rows, -1.0, 1.0);    // A2 -= Y G2
+      }
+    }
+  };
+  // C (rows x q, leading dimension rows) = Q C, Q the product of F's block
+  // reflectors, applied in reverse order
+  auto qr_apply = [&](int rows, const double* F, const double* Tfac, double* C) {
+    for (int k = npan - 1; k >= 0; --k) {
+      const int j0 = k * QRP_NB, w = std::min(QRP_NB, q - j0), m = rows - j0;
+      const double* Ap = F + j0 + (i64)rows * j0;
+      const double* Tk = Tfac + (size_t)k * QRP_NB * QRP_NB;
+      qr_make_y_kernel<<<gbl((i64)m * w), 256, 0, s>>>(m, w, Ap, rows, Yp);
+      TTG_CHECK_LAUNCH();
+      double* Cs = C + j0;
+      gemm(w, q, m, Yp, m, 1, Cs, 1, rows, G1, 1, w, 1.0, 0.0);        // G1 = Y^T C
+      gemm(w, q, w, Tk, 1, QRP_NB, G1, 1, w, G2, 1, w, 1.0, 0.0);      // G2 = T G1
+      gemm(m, q, w, Yp, 1, m, G2, 1, w, Cs, 1, rows, -1.0, 1.0);      // C -= Y G2
+    }
+  };
   // column norms, descending order (ties by index), permuted copy
   int nb = std::max(1, std::min(1024, ceil_div((i64)q * 32, 256)));
   svd_finish_kernel<<<nb, 256, 0, s>>>(p, q, Mw, nullptr, nullptr, nullptr, nullptr, nrm, perm);
@@ -869,70 +953,46 @@ static void svd_tall_qr(int p, int q, double* Mw, double* U, double* sigma, doub
   TTG_CHECK_LAUNCH();
   permute_cols_kernel<<<gbl((i64)p * q), 256, 0, s>>>(p, q, Mw, perm, A);
   TTG_CHECK_LAUNCH();
-  // blocked Householder QR
-  for (int k = 0; k < npan; ++k) {
-    const int j0 = k * QRP_NB, w = std::min(QRP_NB, q - j0), m = p - j0;
-    double* Ap = A + j0 + (i64)p * j0;
-    double* Tk = Tf + (size_t)k * QRP_NB * QRP_NB;
-    if (m >= 1024) {
-      static const int coop_max = [] {
-        int dev = 0, nsm = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, qr_panel_coop_kernel, QRC_NT, 0);
-        return std::max(1, nsm * per);
-      }();
-      int G = std::min(std::min(QRC_GMAX, std::max(1, m / 128)), coop_max);
-      int mm = m, ww = w, ldt = QRP_NB;
-      i64 ld = p;
-      double* tk = tau + j0;
-      void* args[] = {&mm, &ww, &Ap, &ld, &tk, &Tk, &ldt, &qpart};
-      TTG_CUDA(cudaLaunchCooperativeKernel((const void*)qr_panel_coop_kernel, dim3(G),
-                                           dim3(QRC_NT), args, 0, s));
-      ++g_launches;
-    } else {
-      qr_panel_kernel<<<1, QRP_NT, 0, s>>>(m, w, Ap, p, tau + j0, Tk, QRP_NB);
-      TTG_CHECK_LAUNCH();
-    }
-    const int n2 = q - j0 - w;
-    if (n2 > 0) {
-      qr_make_y_kernel<<<gbl((i64)m * w), 256, 0, s>>>(m, w, Ap, p, Yp);
-      TTG_CHECK_LAUNCH();
-      double* A2 = Ap + (i64)p * w;
-      gemm(w, n2, m, Yp, m, 1, A2, 1, p, G1, 1, w, 1.0, 0.0);          // G1 = Y^T A2
-      gemm(w, n2, w, Tk, QRP_NB, 1, G1, 1, w, G2, 1, w, 1.0, 0.0);      // G2 = T^T G1
-      gemm(m, n2, w, Yp, 1, m, G2, 1, w, A2, 1, p, -1.0, 1.0);         // A2 -= Y G2
-    }
+  qr_factor(p, A, Tf, tau);                             // M P = Q1 R1
+  (void)tmp;
+  const bool qr2 = q >= SVD_QR2_MIN_Q;
+  if (qr2) {
+    rt_kernel<<<gbl((i64)q * q), 256, 0, s>>>(q, A, p, X);   // X = R1^T
+    TTG_CHECK_LAUNCH();
+    qr_factor(q, X, Tf2, tau2);                                // R1^T = Q2 R2
+    rt_kernel<<<gbl((i64)q * q), 256, 0, s>>>(q, X, q, X2);  // X2 = R2^T
+  } else {
+    rt_kernel<<<gbl((i64)q * q), 256, 0, s>>>(q, A, p, X2);  // X2 = R1^T
   }
-  // one-sided Jacobi on R^T, FP64 sweeps over the grid from the identity
+  TTG_CHECK_LAUNCH();
+  // one-sided Jacobi on R2^T, FP64 sweeps over the grid from the identity
   // (FP32 pre-sweeps do not pay here: the preconditioned matrix converges in
   // a few FP64 sweeps, and FP32 cannot resolve its small columns)
-  (void)tmp;
-  rt_kernel<<<gbl((i64)q * q), 256, 0, s>>>(q, A, p, X);
-  TTG_CHECK_LAUNCH();
-  svd_sweeps<double>(q, q, X, V, counters, status, 0, sqrt((double)q) * DBL_EPSILON,
+  svd_sweeps<double>(q, q, X2, V, counters, status, 0, sqrt((double)q) * DBL_EPSILON,
                      (double)q * DBL_EPSILON, SVD_MAX_SWEEPS, s);
-  svd_finish_kernel<<<nb, 256, 0, s>>>(q, q, X, V, nullptr, nullptr, nullptr, nrm, rank);
+  svd_finish_kernel<<<nb, 256, 0, s>>>(q, q, X2, V, nullptr, nullptr, nullptr, nrm, rank);
   TTG_CHECK_LAUNCH();
   svd_rank_kernel<<<ceil_div(q, 256), 256, 0, s>>>(q, nrm, rank);
   TTG_CHECK_LAUNCH();
-  svd_gather_kernel<<<gbl((i64)q * q), 256, 0, s>>>(q, q, X, V, nrm, rank, Ux, sigma, Vtx);
+  // Ux = U2 (sorted), sigma, Vtx = V2^T (sorted rows)
+  svd_gather_kernel<<<gbl((i64)q * q), 256, 0, s>>>(q, q, X2, V, nrm, rank, Ux, sigma, Vtx);
   TTG_CHECK_LAUNCH();
-  // U = Q [J; 0], the panels' block reflectors applied in reverse order
-  qr_c0_kernel<<<gbl((i64)p * q), 256, 0, s>>>(p, q, Vtx, U);
-  TTG_CHECK_LAUNCH();
-  for (int k = npan - 1; k >= 0; --k) {
-    const int j0 = k * QRP_NB, w = std::min(QRP_NB, q - j0), m = p - j0;
-    const double* Ap = A + j0 + (i64)p * j0;
-    const double* Tk = Tf + (size_t)k * QRP_NB * QRP_NB;
-    qr_make_y_kernel<<<gbl((i64)m * w), 256, 0, s>>>(m, w, Ap, p, Yp);
+  if (qr2) {
+    // U = Q1 [U2; 0]; W = Q2 V2, Vt = (P W)^T
+    qr_c0n_kernel<<<gbl((i64)p * q), 256, 0, s>>>(p, q, Ux, U);
     TTG_CHECK_LAUNCH();
-    double* Cs = U + j0;
-    gemm(w, q, m, Yp, m, 1, Cs, 1, p, G1, 1, w, 1.0, 0.0);             // G1 = Y^T C
-    gemm(w, q, w, Tk, 1, QRP_NB, G1, 1, w, G2, 1, w, 1.0, 0.0);        // G2 = T G1
-    gemm(m, q, w, Yp, 1, m, G2, 1, w, Cs, 1, p, -1.0, 1.0);           // C -= Y G2
+    qr_apply(p, A, Tf, U);
+    transpose_f64(q, q, Vtx, W, s);
+    qr_apply(q, X, Tf2, W);
+    qr_vt_kernel<<<gbl((i64)q * q), 256, 0, s>>>(q, W, perm, Vt);
+  } else {
+    // R1 = V2 S U2^T: U = Q1 [V2; 0], Vt = (P U2)^T
+    transpose_f64(q, q, Vtx, W, s);
+    qr_c0n_kernel<<<gbl((i64)p * q), 256, 0, s>>>(p, q, W, U);
+    TTG_CHECK_LAUNCH();
+    qr_apply(p, A, Tf, U);
+    qr_vt_kernel<<<gbl((i64)q * q), 256, 0, s>>>(q, Ux, perm, Vt);
   }
-  qr_vt_kernel<<<gbl((i64)q * q), 256, 0, s>>>(q, Ux, perm, Vt);
   TTG_CHECK_LAUNCH();
 }
 
