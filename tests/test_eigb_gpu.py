@@ -89,6 +89,27 @@ def test_eigb_chosen_matches_plain(ctx, d, B, r, rmax):
     assert np.allclose(lam_s, w, rtol=REL, atol=0)
 
 
+def test_eigb_split_sweep_mixes_operator_forms(ctx):
+    """One split-form sweep whose local problems take both forms of the split
+    operator from one workspace: rank caps that are multiples of 8 (the
+    core-contracted form, sized for the caps) and truncated ranks that are
+    not (the four-launch form, with its FP32 intermediate).  The workspace is
+    sized for the larger of the two layouts, and a layout that does not fit
+    is refused before anything is written; the sweep must finish and agree
+    with the plain method to the truncation accuracy."""
+    import ttgpu
+    d, B, rmax = 24, 4, 40
+    n, m, ra, crA = xxz_mpo(d, delta=1.1)
+    _, ry, cr = random_tt(d, 2, 16, last=B, seed=23)
+    lam_s, _, ry_s = ttgpu.tt_eigb(d, n, m, ra, crA, cr, ry, 1e-6, rmax, B, nswp=3,
+                                   max_full_size=100, method="split", ctx=ctx)
+    lam_p, _, ry_p = ttgpu.tt_eigb(d, n, m, ra, crA, cr, ry, 1e-6, rmax, B, nswp=3,
+                                   max_full_size=100, ctx=ctx)
+    assert max(ry_s[:d]) <= rmax
+    assert any(r % 8 for r in ry_s[1:d])      # truncated ranks off the multiples of 8
+    assert np.allclose(lam_s, lam_p, rtol=1e-6, atol=0)
+
+
 def test_eigb_plain_is_bit_reproducible(ctx):
     """The plain FP64 method sums every reduction in a fixed order (split-K
     GEMM partials and column norms through cluster shared memory, no

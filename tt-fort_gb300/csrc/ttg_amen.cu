@@ -402,6 +402,7 @@ class AmenSolver {
   void gmres(const LocalDims& L, int k, const double* b, double* x, double tol);
   void gmres_split(const LocalDims& L, int k, const double* b, double* x, double tol);
   void* split_mem_ = nullptr;
+  size_t split_bytes_ = 0;
   double *ir_r_ = nullptr, *ir_d_ = nullptr;
   long long split_mv_ = 0;
   void trunc(int k, double tol, const double* rhs, double rhs_norm);
@@ -489,7 +490,8 @@ void AmenSolver::gmres_split(const LocalDims& L, int k, const double* b, double*
   const i64 N = L.xsize();
   const int nr = (int)std::min<i64>(std::min<i64>(N, P_.local_restart), 60);
   MatvecFn mvlow;
-  split_matvec_factory(L, pxax_[k], A_[k], pxax_[k + 1], kBatch, split_mem_, s_, &mvlow);
+  split_matvec_factory(L, pxax_[k], A_[k], pxax_[k + 1], kBatch, split_mem_, split_bytes_, s_,
+                       &mvlow);
   auto mvs = [&](const double* in, double* out, int nv) { mvlow(in, out, nv); split_mv_ += nv; };
   const GmresBufs G{V_, w_, gm_, red_, h_};
   const double nb = norm2(b, N);
@@ -526,7 +528,8 @@ void AmenSolver::trunc(int k, double tol, const double* rhs, double rhs_norm) {
   int fail = 0;   // largest candidate rank whose residual exceeds tol (0: none)
   MatvecFn mvlow;
   if (P_.method == TTG_METHOD_SPLIT)
-    split_matvec_factory(L, pxax_[k], A_[k], pxax_[k + 1], kBatch, split_mem_, s_, &mvlow);
+    split_matvec_factory(L, pxax_[k], A_[k], pxax_[k + 1], kBatch, split_mem_, split_bytes_, s_,
+                       &mvlow);
   while (rnew >= 1 && !fail) {
     const int cnt = std::min(kBatch, rnew);
     if (P_.method == TTG_METHOD_SPLIT) {
@@ -674,6 +677,7 @@ void AmenSolver::run(AmenOut& out) {
   dense_ = mem_.take(64 * 64);
   if (P_.method == TTG_METHOD_SPLIT) {
     split_mem_ = (void*)mem_.take(splitb / sizeof(double) + 128);
+    split_bytes_ = splitb;
     ir_r_ = mem_.take(Nmax);
     ir_d_ = mem_.take(Nmax);
   }

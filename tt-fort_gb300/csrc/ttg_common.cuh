@@ -328,8 +328,9 @@ void jac_apply_f64(char p, i64 rx1, i64 n, i64 rx2, const double* jacs, const do
 // ---------------------------------------------------------------------------
 struct SplitOp;   // opaque prepared operator
 size_t split_op_bytes(const LocalDims& L, int nvec_max);
-void split_op_prepare(SplitOp** op, const LocalDims& L, int nvec_max, const double* phi1,
-                      const double* A, const double* phi2, void* mem, cudaStream_t s);
+void split_op_prepare(SplitOp* op, const LocalDims& L, int nvec_max, const double* phi1,
+                      const double* A, const double* phi2, void* mem, size_t mem_bytes,
+                      cudaStream_t s);
 void split_op_apply(SplitOp* op, const double* x, double* y, int nvec, cudaStream_t s);
 bool split_op_supported(const LocalDims& L);
 

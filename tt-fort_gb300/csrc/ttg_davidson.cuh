@@ -18,14 +18,15 @@ namespace ttg {
 using MatvecFn = std::function<void(const double* X, double* Y, int nvec)>;
 
 // Chosen-form local operator y = Phi1 A Phi2 x on the BF16x3 tensor-core
-// kernels (ttg_tc.cu): operands prepared once in mem (split_matvec_bytes),
+// kernels (ttg_tc.cu): operands prepared once in mem (mem_bytes long, sized
+// with split_matvec_bytes for the largest local problem it serves),
 // two prepared operators (slot 0 and 1) per host thread; preparing a slot
 // again replaces its operator.  split_matvec_check reads the bounded-wait
 // flags of slots [0, nslots), which the caller must have prepared itself,
 // and throws when a GEMM gave up waiting.
 void split_matvec_factory(const LocalDims& L, const double* phi1, const double* A,
-                          const double* phi2, int nvec_max, void* mem, cudaStream_t s,
-                          MatvecFn* out, int slot = 0);
+                          const double* phi2, int nvec_max, void* mem, size_t mem_bytes,
+                          cudaStream_t s, MatvecFn* out, int slot = 0);
 size_t split_matvec_bytes(const LocalDims& L, int nvec_max);
 void split_matvec_check(cudaStream_t s, int nslots = 1);
 // Expansion-vector transform: on entry T (N x t) holds residual columns, X

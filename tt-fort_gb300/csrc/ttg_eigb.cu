@@ -268,7 +268,8 @@ static void run_eigb(ttg_ctx* ctx, EigbParams P, EigbOutput& out) {
       const double* p2 = phi[i + 1];
       MatvecFn mv = [=](const double* X, double* Y, int nv) { bfun3_f64(L, p1, Ai, p2, X, Y, nv, bfs, s); };
       MatvecFn mvlow;
-      if (P.method == TTG_METHOD_SPLIT) split_matvec_factory(L, p1, Ai, p2, B, split_mem, s, &mvlow);
+      if (P.method == TTG_METHOD_SPLIT)
+        split_matvec_factory(L, p1, Ai, p2, B, split_mem, split_bytes, s, &mvlow);
       if (P.method == TTG_METHOD_JD64) mvlow = mv;   // ablation: the same solver, FP64 products
       if (pt.on) {
         PhaseTimer* ptp = &pt;
@@ -691,7 +692,8 @@ extern "C" int ttg_local_eig(ttg_ctx* ctx, ttg_int r1, ttg_int n, ttg_int r2, tt
     DavidsonStats st;
     if (jd) {
       MatvecFn mvlow = mv;
-      if (method == TTG_METHOD_SPLIT) split_matvec_factory(L, phi1, A, phi2, (int)B, split_mem, s, &mvlow);
+      if (method == TTG_METHOD_SPLIT)
+        split_matvec_factory(L, phi1, A, phi2, (int)B, split_mem, split_bytes, s, &mvlow);
       int n64 = 0;
       st = chosen_solve(N, (int)B, dav_mem, hb.p, jd_mem, mv, mvlow, X0, tol, maxmv, X,
                         lam.data(), s, nullptr, &n64);

@@ -386,7 +386,8 @@ static void run_ksl(ttg_ctx* ctx, KslParams P, std::vector<std::complex<double>>
           realify_phi2_kernel<<<ebz(4 * Lk.rx2 * Lk.ra2 * Lk.ry2), 256, 0, s>>>(Lk.rx2, Lk.ra2, Lk.ry2, p2, rphi2[k], adj);
           TTG_CHECK_LAUNCH();
           MatvecFn smv;
-          split_matvec_factory(Lreal(Lk), rphi1[k], rA[k], rphi2[k], kNvecSplit, smem[k], s, &smv, k);
+          split_matvec_factory(Lreal(Lk), rphi1[k], rA[k], rphi2[k], kNvecSplit, smem[k],
+                               split_bytes, s, &smv, k);
           const i64 Nk = Lk.xsize();
           return [=](const double2* X, double2* Y, int t) {
             for (int v0 = 0; v0 < t; v0 += kNvecSplit) {

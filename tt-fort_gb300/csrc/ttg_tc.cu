@@ -1760,12 +1760,15 @@ struct SplitOp {
 // ~11k cycles (about 1.8k instructions per thread at ~6 cycles each), GEMM3
 // with its streamed Phi1 tiles ~6.7k, the FP64 stores ~6k; the general path
 // spreads the X split and the core over many CTAs instead.
-static bool fused_plan(const LocalDims& L, int nvec, int& bn1, int& n3p, int& C, int& ntiles) {
+static bool fused_enabled() {
   static const bool enabled = [] {
     const char* v = std::getenv("TTG_FUSED");
     return v && v[0] == '1';
   }();
-  if (!enabled) return false;
+  return enabled;
+}
+static bool fused_plan(const LocalDims& L, int nvec, int& bn1, int& n3p, int& C, int& ntiles) {
+  if (!fused_enabled()) return false;
   if (L.n != L.m || 128 % L.m != 0 || L.rx1 * L.m > 128 || L.rx2 > 64 || L.ry1 > 128) return false;
   if (L.m * L.ra2 > 16 || L.n * L.ra1 > 16) return false;
   const int k3tiles = ceil_div(L.rx1 * L.ra1, tc::TK);
@@ -1804,39 +1807,22 @@ static bool pre_plan(const LocalDims& L) {
 }
 
 // Sizing (op == nullptr) takes the widest tile padding so that the bytes
-// bound every tile width the autotuner may pick at layout time.
+// bound every tile width the autotuner may pick at layout time, and the
+// larger of the two forms' layouts: callers size one buffer from the largest
+// ranks a sweep may reach, and a smaller local problem may take the other
+// form (the core-contracted one needs rx1 % 8 == 0).
 static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* base,
-                           cudaStream_t s = nullptr) {
+                           cudaStream_t s = nullptr);
+static size_t split_layout_pre(const LocalDims& L, int nvec_max, SplitOp* op, char* base,
+                               cudaStream_t s);
+
+static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* base,
+                           cudaStream_t s) {
+  const bool sizing0 = !(op && base);
   {
     int b_, n_, c_, t_;
-    if (!fused_plan(L, nvec_max, b_, n_, c_, t_) && pre_plan(L)) {
-      const int MQ = (int)(L.n * L.ry2 * L.ra1), KQ = (int)(L.m * L.rx2);
-      const int NX = (int)(L.rx1 * nvec_max);
-      const int M3 = (int)L.ry1, N3 = (int)(L.n * L.ry2 * nvec_max), K3 = (int)(L.rx1 * L.ra1);
-      const bool sizing = !(op && base);
-      const int bnq = sizing ? 256 : tc::tuned_bn(MQ, NX, KQ, false, s);
-      const int bn3 = sizing ? 256 : tc::tuned_bn(M3, N3, K3, true, s);
-      size_t tot = tc::tiled_bytes(MQ, KQ, tc::TM) + tc::tiled_bytes(NX, KQ, bnq) +
-                   tc::tiled_bytes(M3, K3, tc::TM) + tc::tiled_bytes(N3, K3, bn3) + 1024 +
-                   sizeof(SplitOp) + 1024;
-      if (op && base) {
-        char* p = base;
-        op->L = L;
-        op->nvec_max = nvec_max;
-        op->bn1 = bnq; op->bn3 = bn3;
-        op->pre = true;
-        op->fused = false;
-        op->Q = tc::make_tiled(MQ, KQ, tc::TM, p);
-        op->X = tc::make_tiled(NX, KQ, bnq, p);
-        op->P1 = tc::make_tiled(M3, K3, tc::TM, p);
-        op->T2 = tc::make_tiled(N3, K3, bn3, p);
-        op->T1 = nullptr;
-        op->ld1 = 0;
-        op->err = (int*)p; p += 1024;
-        op->part = nullptr;
-      }
-      return tot;
-    }
+    if (!sizing0 && !fused_plan(L, nvec_max, b_, n_, c_, t_) && pre_plan(L))
+      return split_layout_pre(L, nvec_max, op, base, s);
   }
   const int M1 = (int)(L.rx1 * L.m * nvec_max), N1 = (int)(L.ra2 * L.ry2), K1 = (int)L.rx2;
   const int M3 = (int)L.ry1, N3 = (int)(L.n * L.ry2 * nvec_max), K3 = (int)(L.rx1 * L.ra1);
@@ -1862,11 +1848,13 @@ static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* 
   }
   part = (part + 1023) & ~size_t(1023);
   tot += part;
-  // permuted Phi2 tiles of the fused path (the larger of its two tile plans)
+  // permuted Phi2 tiles of the fused path (the larger of its two tile plans;
+  // when sizing, whenever the path is enabled: a smaller local problem may
+  // take it where the largest does not)
   size_t p2f = 0;
   {
     int b, n3, c, nt;
-    if (fused_plan(L, nvec_max, b, n3, c, nt)) {
+    if (sizing ? fused_enabled() : fused_plan(L, nvec_max, b, n3, c, nt)) {
       for (int bb : {128, 64}) {
         const int cb = (int)std::min<i64>(bb / L.ra2, (bb == 128 ? 64 : 32) / L.n);
         if (cb < 1) continue;
@@ -1899,6 +1887,38 @@ static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* 
     }
     p += p2f;
   }
+  // sizing bounds both forms
+  return sizing ? std::max(tot, split_layout_pre(L, nvec_max, nullptr, nullptr, s)) : tot;
+}
+
+// layout of the core-contracted form (see pre_plan)
+static size_t split_layout_pre(const LocalDims& L, int nvec_max, SplitOp* op, char* base,
+                               cudaStream_t s) {
+  const int MQ = (int)(L.n * L.ry2 * L.ra1), KQ = (int)(L.m * L.rx2);
+  const int NX = (int)(L.rx1 * nvec_max);
+  const int M3 = (int)L.ry1, N3 = (int)(L.n * L.ry2 * nvec_max), K3 = (int)(L.rx1 * L.ra1);
+  const bool sizing = !(op && base);
+  const int bnq = sizing ? 256 : tc::tuned_bn(MQ, NX, KQ, false, s);
+  const int bn3 = sizing ? 256 : tc::tuned_bn(M3, N3, K3, true, s);
+  size_t tot = tc::tiled_bytes(MQ, KQ, tc::TM) + tc::tiled_bytes(NX, KQ, bnq) +
+               tc::tiled_bytes(M3, K3, tc::TM) + tc::tiled_bytes(N3, K3, bn3) + 1024 +
+               sizeof(SplitOp) + 1024;
+  if (op && base) {
+    char* p = base;
+    op->L = L;
+    op->nvec_max = nvec_max;
+    op->bn1 = bnq; op->bn3 = bn3;
+    op->pre = true;
+    op->fused = false;
+    op->Q = tc::make_tiled(MQ, KQ, tc::TM, p);
+    op->X = tc::make_tiled(NX, KQ, bnq, p);
+    op->P1 = tc::make_tiled(M3, K3, tc::TM, p);
+    op->T2 = tc::make_tiled(N3, K3, bn3, p);
+    op->T1 = nullptr;
+    op->ld1 = 0;
+    op->err = (int*)p; p += 1024;
+    op->part = nullptr;
+  }
   return tot;
 }
 
@@ -1913,8 +1933,13 @@ bool split_op_supported(const LocalDims& L) {
 // c1, K (b1,a1)) once per local problem.  The SplitOp header lives in host
 // memory owned by the caller; mem holds the device buffers.
 void split_op_prepare(SplitOp* op, const LocalDims& L, int nvec_max, const double* phi1,
-                      const double* A, const double* phi2, void* mem, cudaStream_t s) {
-  split_layout(L, nvec_max, op, (char*)mem, s);
+                      const double* A, const double* phi2, void* mem, size_t mem_bytes,
+                      cudaStream_t s) {
+  // the layout of this local problem's form must fit the caller's buffer
+  // (sized with split_op_bytes for the largest problem it serves); checked
+  // before anything is written to it
+  const size_t need = split_layout(L, nvec_max, op, (char*)mem, s);
+  TTG_REQUIRE(need <= mem_bytes, "split matvec: workspace too small for this local problem");
   op->A = A;
   if (op->pre) {
     const i64 total = (i64)op->Q.rtiles * tc::TM * op->Q.ktiles * (tc::TK / 8);
@@ -2114,12 +2139,12 @@ static thread_local SplitOp op_store[kSplitSlots];
 static thread_local bool op_store_set[kSplitSlots] = {};
 
 void split_matvec_factory(const LocalDims& L, const double* phi1, const double* A,
-                          const double* phi2, int nvec_max, void* mem, cudaStream_t s,
-                          MatvecFn* out, int slot) {
+                          const double* phi2, int nvec_max, void* mem, size_t mem_bytes,
+                          cudaStream_t s, MatvecFn* out, int slot) {
   TTG_REQUIRE(slot >= 0 && slot < kSplitSlots, "split matvec: bad operator slot");
   TTG_REQUIRE(split_op_supported(L), "split matvec: local problem too large");
   op_store_set[slot] = true;
-  split_op_prepare(&op_store[slot], L, nvec_max, phi1, A, phi2, mem, s);
+  split_op_prepare(&op_store[slot], L, nvec_max, phi1, A, phi2, mem, mem_bytes, s);
   SplitOp* op = &op_store[slot];
   *out = [op, s](const double* X, double* Y, int nv) { split_op_apply(op, X, Y, nv, s); };
 }
@@ -2164,7 +2189,7 @@ extern "C" int ttg_dbfun3_split(ttg_ctx* c, ttg_int rx1, ttg_int m, ttg_int rx2,
     c->ws.reserve(bytes);
     void* mem = c->ws.take(bytes);
     SplitOp op;
-    split_op_prepare(&op, L, (int)nvec, phi1, A, phi2, mem, c->stream);
+    split_op_prepare(&op, L, (int)nvec, phi1, A, phi2, mem, bytes, c->stream);
     split_op_apply(&op, x, y, (int)nvec, c->stream);
     int herr = 0;
     TTG_CUDA(cudaMemcpyAsync(&herr, op.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -2211,7 +2236,7 @@ extern "C" int ttg_localop_create(ttg_ctx* c, ttg_int rx1, ttg_int m, ttg_int rx
     if (method == TTG_METHOD_SPLIT) TTG_REQUIRE(split_op_supported(L), "too large for split");
     TTG_CUDA(cudaMalloc(&op->mem, bytes));
     if (method == TTG_METHOD_SPLIT)
-      split_op_prepare(&op->split, L, (int)nvec_max, phi1, A, phi2, op->mem, c->stream);
+      split_op_prepare(&op->split, L, (int)nvec_max, phi1, A, phi2, op->mem, bytes, c->stream);
     *out = op;
   } catch (const ttg::Error& e) {
     c->last_error = e.msg;
