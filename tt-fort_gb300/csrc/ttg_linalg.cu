@@ -324,7 +324,13 @@ void syev_jacobi(int k, double* A, int lda, double* w, double* V, int ldv, int* 
 // ---------------------------------------------------------------------------
 // one-sided Jacobi SVD (cooperative launch, grid barrier between rounds)
 // ---------------------------------------------------------------------------
-constexpr int SVD_CT = 128;   // one CTA per column pair: four warps share its rows
+#ifndef TTG_SVD_CT
+#define TTG_SVD_CT 128
+#endif
+// one CTA per column pair; its warps share the rows (measured on GB300, 128
+// threads: 7.6 ms at 320x128 and 54 ms at 2048x512; 64: 8.3 and 60; 32: 9.2
+// and 81)
+constexpr int SVD_CT = TTG_SVD_CT;
 constexpr int SVD_MAX_SWEEPS = 60;
 
 template <class T>
@@ -861,6 +867,7 @@ static void svd_tall(int p, int q, double* Mw, double* U, double* sigma, double*
 // d=20 solve, whose blocks are mostly narrower, slower by its ~30 extra
 // launches per SVD).
 constexpr int SVD_QR2_MIN_Q = 192;
+
 static void svd_tall_qr(int p, int q, double* Mw, double* U, double* sigma, double* Vt,
                         double* V, double* nrm, int* rank, int* counters, int* status,
                         double* tmp, double* work, cudaStream_t s) {
@@ -899,6 +906,10 @@ static void svd_tall_qr(int p, int q, double* Mw, double* U, double* sigma, doub
       const int j0 = k * QRP_NB, w = std::min(QRP_NB, q - j0), m = rows - j0;
       double* Ap = F + j0 + (i64)rows * j0;
       double* Tk = Tfac + (size_t)k * QRP_NB * QRP_NB;
+      // panels of 1024+ rows on a grid of CTAs (rows split, two grid
+      // barriers per column); narrower ones in one CTA (grids from 256 rows,
+      // one CTA per 32 or 64 rows, measured no faster on GB300: 7.8 against
+      // 7.55 ms for the 320 x 128 truncation)
       if (m >= 1024) {
         static const int coop_max = [] {
           int dev = 0, nsm = 0, per = 0;
