@@ -159,3 +159,53 @@ def test_split_gemm_each_tile_width_vs_oracle(torch_cuda, bn):
     assert out.returncode == 0, out.stderr[-2000:]
     errs = json.loads(out.stdout.strip().splitlines()[-1])
     assert max(errs) < TOL_SPLIT, errs
+
+
+_PDL_CHILD = r'''
+import json, sys
+import numpy as np, torch
+import ttgpu
+shapes = json.loads(sys.argv[1])
+ctx = ttgpu.Context(0)
+out = []
+for rx1, m, rx2, ry1, n, ry2, ra1, ra2, nvec in shapes:
+    rng = np.random.default_rng(rx1 + 3 * ry2 + nvec)
+    t = lambda a: torch.from_numpy(a).cuda()
+    phi1, A = t(rng.standard_normal(ry1 * rx1 * ra1)), t(rng.standard_normal(ra1 * n * m * ra2))
+    phi2 = t(rng.standard_normal(rx2 * ra2 * ry2))
+    op = ttgpu.LocalOp(rx1, m, rx2, ry1, n, ry2, ra1, ra2, phi1, A, phi2, nvec_max=nvec,
+                       method="split", ctx=ctx)
+    ys = []
+    for rep in range(3):   # back-to-back applies: each launch overlaps the one before
+        X = t(rng.standard_normal(rx1 * m * rx2 * nvec))
+        Y = torch.zeros(ry1 * n * ry2 * nvec, dtype=torch.float64, device="cuda")
+        op.apply(X, Y, nvec)
+        ys.append(Y)
+    ctx.synchronize()
+    out.append([y.cpu().numpy().tolist() for y in ys])
+    op.close()
+print(json.dumps(out))
+'''
+
+
+def test_programmatic_dependent_launch_changes_no_result(torch_cuda):
+    """Programmatic dependent launch lets a kernel's prologue overlap the
+    kernel before it; every kernel waits for its predecessor before touching
+    memory, so results must be bit-identical with it switched off
+    (TTG_PDL=0, read once per process: child processes)."""
+    import json
+    import os
+    import subprocess
+    import sys
+    from conftest import ROOT
+    shapes = [(64, 2, 64, 64, 2, 64, 5, 5, 5), (256, 2, 256, 256, 2, 256, 5, 5, 8),
+              (8, 32, 8, 8, 32, 8, 6, 6, 1)]
+    res = {}
+    for mode in ("0", "1"):
+        env = dict(os.environ, TTG_PDL=mode,
+                   PYTHONPATH=os.pathsep.join([ROOT, os.path.join(ROOT, "tt-fort_gb300")]))
+        out = subprocess.run([sys.executable, "-c", _PDL_CHILD, json.dumps(shapes)],
+                             capture_output=True, text=True, env=env, timeout=600)
+        assert out.returncode == 0, out.stderr[-2000:]
+        res[mode] = json.loads(out.stdout.strip().splitlines()[-1])
+    assert res["0"] == res["1"]
