@@ -126,6 +126,23 @@ def test_eigb_plain_is_bit_reproducible(ctx):
     assert np.array_equal(np.asarray(c0), np.asarray(c1))
 
 
+def test_eigb_chosen_is_bit_reproducible(ctx):
+    """The chosen method's CG correction adds its column dot products with
+    deterministic grid sums (per-block partials added in block order by the
+    last block), and every other reduction of the split path is fixed-order,
+    so two solves of the same input give identical bits."""
+    import ttgpu
+    d, B = 14, 4
+    n, m, ra, crA = xxz_mpo(d, delta=0.8)
+    _, ry, cr = random_tt(d, 2, 8, last=B, seed=11)
+    runs = [ttgpu.tt_eigb(d, n, m, ra, crA, cr, ry, 1e-10, 32, B, nswp=6, max_full_size=100,
+                          method="split", ctx=ctx) for _ in range(2)]
+    (l0, c0, r0), (l1, c1, r1) = runs
+    assert r0 == r1
+    assert np.array_equal(np.asarray(l0), np.asarray(l1))
+    assert np.array_equal(np.asarray(c0), np.asarray(c1))
+
+
 def test_eigb_heisen20_matches_primme_sweep(ctx):
     """The d=20 Heisenberg workload against the sweep whose local eigensolver
     is the reference's own PRIMME (GD+k pinned, tt_eigb's settings;

@@ -22,32 +22,87 @@
 
 namespace ttg {
 
-// out[j] = sum_i U[i,j] V[i,j]   (out pre-zeroed)
+// ---------------------------------------------------------------------------
+// Deterministic grid sums.  The blocks of a group each write one partial sum
+// to part[group * nblk + block]; the block that finishes last (a ticket
+// counter, zero between uses) adds the partials in block order with a fixed
+// lane assignment and shuffle tree, writes the total and resets the counter.
+// The result does not depend on which block finishes first, so the CG
+// correction below is bit-reproducible.
+// ---------------------------------------------------------------------------
+constexpr int CG_MAXT = 16;        // columns of a CG block
+constexpr int CG_MAXBX = 128;      // blocks per column of col_dots / cg_update
+constexpr int CG_MAXPB = 1024;     // blocks of proj_dot
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block sum of v, in thread 0
+__device__ __forceinline__ double block_sum_d(double v, double* red) {
+  v = warp_sum_d(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x < 32) {
+    t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    t = warp_sum_d(t);
+  }
+  return t;
+}
+
+// Called by every thread after thread 0 stored this block's partials
+// (ngroups of them at part[g * nblk + blk]).  Returns true in all threads of
+// the last block to arrive.
+__device__ __forceinline__ bool grid_sum_arrive(unsigned int* count, unsigned int nblk) {
+  __shared__ int last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(count, 1u) == nblk - 1;
+  }
+  __syncthreads();
+  return last != 0;
+}
+
+// In the last block: out[g] = sum_b part[g * nblk + b] for g < ngroups (warp w
+// takes groups w, w + nwarps, ...), then the counter is reset.
+__device__ __forceinline__ void grid_sum_finish(const double* part, int nblk, int ngroups,
+                                                double* out, unsigned int* count) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int g = w; g < ngroups; g += nw) {
+    double v = 0.0;
+    for (int b = lane; b < nblk; b += 32) v += __ldcg(part + (size_t)g * nblk + b);
+    v = warp_sum_d(v);
+    if (lane == 0) out[g] = v;
+  }
+  if (threadIdx.x == 0) *count = 0u;
+}
+
+// out[j] = sum_i U[i,j] V[i,j]; grid (bx, t), deterministic (part: t x bx,
+// count: t counters)
 __global__ void col_dots_kernel(i64 N, const double* __restrict__ U, const double* __restrict__ V,
-                                double* __restrict__ out) {
+                                double* __restrict__ out, double* __restrict__ part,
+                                unsigned int* __restrict__ count) {
   pdl_trigger();
   pdl_wait();
   const int j = blockIdx.y;
   double acc = 0.0;
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < N; i += (i64)gridDim.x * blockDim.x)
     acc = fma(U[i + N * j], V[i + N * j], acc);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   __shared__ double red[32];
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (threadIdx.x == 0) atomicAdd(&out[j], t);
-  }
+  const double t = block_sum_d(acc, red);
+  if (threadIdx.x == 0) part[(size_t)j * gridDim.x + blockIdx.x] = t;
+  if (grid_sum_arrive(count + j, gridDim.x))
+    grid_sum_finish(part + (size_t)j * gridDim.x, gridDim.x, 1, out + j, count + j);
 }
 
-static void col_dots(i64 N, int t, const double* U, const double* V, double* out, cudaStream_t s) {
-  TTG_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * t, s));
-  int bx = (int)std::max<i64>(1, std::min<i64>(128, (N + 2047) / 2048));
-  launch_pdl(col_dots_kernel, dim3(bx, t), dim3(256), 0, s, N, U, V, out);
+static void col_dots(i64 N, int t, const double* U, const double* V, double* out, double* part,
+                     unsigned int* count, cudaStream_t s) {
+  TTG_REQUIRE(t <= CG_MAXT, "col_dots: too many columns");
+  int bx = (int)std::max<i64>(1, std::min<i64>(CG_MAXBX, (N + 2047) / 2048));
+  launch_pdl(col_dots_kernel, dim3(bx, t), dim3(256), 0, s, N, U, V, out, part, count);
 }
 
 // q[:, j] -= theta_j p[:, j]; block 0 also clears the step's accumulators
@@ -65,15 +120,18 @@ __global__ void shift_kernel(i64 N, int t, const double* __restrict__ theta,
     q[e] -= theta[e / N] * p[e];
 }
 
-// q -= X C (X: N x nb, C: nb x t) and pq[j] += p[:, j]^T q[:, j] (pq cleared
-// by shift_kernel): the projection of the CG step fused with its p^T q
+// q -= X C (X: N x nb, C: nb x t) and pq[j] = p[:, j]^T q[:, j]: the
+// projection of the CG step fused with its p^T q (deterministic grid sum:
+// part t x gridDim.x, one counter)
 constexpr int PD_MAXT = 16;
 __global__ void __launch_bounds__(128) proj_dot_kernel(i64 N, int t, int nb,
                                                        const double* __restrict__ X,
                                                        const double* __restrict__ C,
                                                        const double* __restrict__ p,
                                                        double* __restrict__ q,
-                                                       double* __restrict__ pq) {
+                                                       double* __restrict__ pq,
+                                                       double* __restrict__ part,
+                                                       unsigned int* __restrict__ count) {
   __shared__ double Cs[PD_MAXT * PD_MAXT];
   __shared__ double red[4][PD_MAXT];
   pdl_trigger();
@@ -110,17 +168,22 @@ __global__ void __launch_bounds__(128) proj_dot_kernel(i64 N, int t, int nb,
   __syncthreads();
   if (threadIdx.x < t) {
     const double v = red[0][threadIdx.x] + red[1][threadIdx.x] + red[2][threadIdx.x] + red[3][threadIdx.x];
-    atomicAdd(&pq[threadIdx.x], v);
+    part[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = v;
+    __threadfence();
   }
+  __syncthreads();
+  if (grid_sum_arrive(count, gridDim.x)) grid_sum_finish(part, gridDim.x, t, pq, count);
 }
 
 // CG step on column j (frozen when inactive or when p^T q <= 0):
-//   alpha = rr/pq; x += alpha p; r -= alpha q; rr_new += |r|^2
+//   alpha = rr/pq; x += alpha p; r -= alpha q; rr_new = |r|^2 (deterministic
+//   grid sum over the bx blocks of the column)
 __global__ void cg_update_kernel(i64 N, const double* __restrict__ rr, const double* __restrict__ pq,
                                  const double* __restrict__ rr0, double tol2,
                                  const double* __restrict__ p, const double* __restrict__ q,
                                  double* __restrict__ x, double* __restrict__ r,
-                                 double* __restrict__ rr_new) {
+                                 double* __restrict__ rr_new, double* __restrict__ part,
+                                 unsigned int* __restrict__ count) {
   pdl_trigger();
   pdl_wait();
   const int j = blockIdx.y;
@@ -137,17 +200,11 @@ __global__ void cg_update_kernel(i64 N, const double* __restrict__ rr, const dou
     }
     acc = fma(rv, rv, acc);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   __shared__ double red[32];
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (threadIdx.x == 0) atomicAdd(&rr_new[j], t);
-  }
+  const double t = block_sum_d(acc, red);
+  if (threadIdx.x == 0) part[(size_t)j * gridDim.x + blockIdx.x] = t;
+  if (grid_sum_arrive(count + j, gridDim.x))
+    grid_sum_finish(part + (size_t)j * gridDim.x, gridDim.x, 1, rr_new + j, count + j);
 }
 
 // p = r + beta p, beta = rr_new / rr (0 for frozen columns)
@@ -178,12 +235,23 @@ struct JdCg {
   MatvecFn low;        // split-precision operator
   cudaStream_t s;
   double *x, *r, *p, *q, *sc;   // N x Bmax each; sc: scalars
+  double *part_cd, *part_cu, *part_pd;   // partial sums of the grid reductions
+  unsigned int* cnt;                     // their ticket counters (zero between uses)
 
-  static size_t bytes(i64 N, int Bmax) { return (4 * (size_t)N * Bmax + 16 * 64) * sizeof(double) + 4096; }
+  static constexpr size_t kParts = 2 * (size_t)CG_MAXT * CG_MAXBX + (size_t)CG_MAXT * CG_MAXPB;
+  static size_t bytes(i64 N, int Bmax) {
+    return (4 * (size_t)N * Bmax + 16 * 64 + kParts + 64) * sizeof(double) + 4096;
+  }
 
   void bind(void* mem) {
+    TTG_REQUIRE(Bmax <= CG_MAXT, "jd cg: block wider than 16 columns");
     double* m = (double*)mem;
     x = m; r = x + N * Bmax; p = r + N * Bmax; q = p + N * Bmax; sc = q + N * Bmax;
+    part_cd = sc + 16 * 64;
+    part_cu = part_cd + (size_t)CG_MAXT * CG_MAXBX;
+    part_pd = part_cu + (size_t)CG_MAXT * CG_MAXBX;
+    cnt = (unsigned int*)(part_pd + (size_t)CG_MAXT * CG_MAXPB);   // 3 x 16 counters
+    TTG_CUDA(cudaMemsetAsync(cnt, 0, 64 * sizeof(double), s));
   }
 
   // project out X (N x nb): v -= X (X^T v)
@@ -257,7 +325,7 @@ struct JdCg {
     double* rr0 = sc + 3 * 64;
     const double tol2 = rel_tol * rel_tol;
     const size_t bytes_t = sizeof(double) * N * t;
-    int bx = (int)std::max<i64>(1, std::min<i64>(128, (N + 2047) / 2048));
+    int bx = (int)std::max<i64>(1, std::min<i64>(CG_MAXBX, (N + 2047) / 2048));
     int eb = (int)std::min<i64>(4096, (N * t + 255) / 256);
     // x = 0, r = -rhs (already orthogonal to X), p = r
     TTG_CUDA(cudaMemsetAsync(x, 0, bytes_t, s));
@@ -265,10 +333,10 @@ struct JdCg {
     project(r, t, X, nb);
     scale_cols_neg(r, t);
     TTG_CUDA(cudaMemcpyAsync(p, r, bytes_t, cudaMemcpyDeviceToDevice, s));
-    col_dots(N, t, r, r, rr, s);
+    col_dots(N, t, r, r, rr, part_cd, cnt, s);
     TTG_CUDA(cudaMemcpyAsync(rr0, rr, sizeof(double) * t, cudaMemcpyDeviceToDevice, s));
     const bool fused = t <= PD_MAXT && nb <= PD_MAXT;
-    int pb = (int)std::max<i64>(1, std::min<i64>(1024, (N + 127) / 128));
+    int pb = (int)std::max<i64>(1, std::min<i64>(CG_MAXPB, (N + 127) / 128));
     for (int it = 0; it < iters; ++it) {
       low(p, q, t);                                   // q = A~ p
       launch_pdl(shift_kernel, dim3(eb), dim3(256), 0, s, N, t, theta, (const double*)p, q, pq,
@@ -278,15 +346,14 @@ struct JdCg {
         double* c = sc + 6 * 64;
         gemm_tn_small(nb, t, N, X, N, q, N, c, nb, 1.0, 0.0, s);
         launch_pdl(proj_dot_kernel, dim3(pb), dim3(128), 0, s, N, t, nb, X, (const double*)c,
-                   (const double*)p, q, pq);
+                   (const double*)p, q, pq, part_pd, cnt + 2 * CG_MAXT);
       } else {
         project(q, t, X, nb);                         // q = P q
-        col_dots(N, t, p, q, pq, s);
-        TTG_CUDA(cudaMemsetAsync(rr_new, 0, sizeof(double) * t, s));
+        col_dots(N, t, p, q, pq, part_cd, cnt, s);
       }
       launch_pdl(cg_update_kernel, dim3(bx, t), dim3(256), 0, s, N, (const double*)rr,
                  (const double*)pq, (const double*)rr0, tol2, (const double*)p, (const double*)q, x,
-                 r, rr_new);
+                 r, rr_new, part_cu, cnt + CG_MAXT);
       launch_pdl(cg_dir_kernel, dim3(eb), dim3(256), 0, s, N, t, (const double*)rr,
                  (const double*)rr_new, (const double*)pq, (const double*)rr0, tol2,
                  (const double*)r, p);
