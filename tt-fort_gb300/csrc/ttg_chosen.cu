@@ -19,6 +19,7 @@
 // same FP64 residual test as the plain method.
 #include "ttg_davidson.cuh"
 #include <algorithm>
+#include <cstdlib>
 
 namespace ttg {
 
@@ -388,10 +389,17 @@ DavidsonStats chosen_solve(i64 N, int B, void* dav_mem, double* hbuf, void* jd_m
                            double tol, int max_matvecs, double* X, double* theta_host,
                            cudaStream_t s, DavTimer* timer, int* fp64_matvecs) {
   JdCg jd;
-  // 16 CG steps per correction: 12-32 steps give the same solve time on the
-  // d=20 Heisenberg chain (fewer outer iterations and FP64 matvecs balance
-  // the longer inner solves); 4-6 steps are 1.3-3.5x slower
-  jd.N = N; jd.Bmax = B; jd.iters = 16; jd.rel_tol = 1e-3; jd.low = mvlow; jd.s = s;
+  // 16 CG steps per correction.  On the d=20 Heisenberg chain (GB300, the
+  // deterministic solver) 8/10/12/16/20/24/32 steps take 1.08/1.23/1.03/
+  // 0.98/0.98/0.94/1.01 s: fewer outer iterations and FP64 matvecs balance
+  // the longer inner solves, with no clear trend beyond noise of the
+  // iteration path; 4-6 steps were 1.3-3.5x slower
+  static const int cg_steps = [] {
+    const char* v = std::getenv("TTG_JD_CG_STEPS");   // tuning override (default 16)
+    const int k = v ? std::atoi(v) : 0;
+    return k >= 1 && k <= 256 ? k : 16;
+  }();
+  jd.N = N; jd.Bmax = B; jd.iters = cg_steps; jd.rel_tol = 1e-3; jd.low = mvlow; jd.s = s;
   jd.use_graph = timer == nullptr;      // the profiler synchronises inside matvecs
   jd.bind(jd_mem);
   const int maxb2 = (int)std::min<i64>(2 * B, N);
