@@ -418,6 +418,29 @@ def bench_batch(args, torch, ttgpu, ctx):
     print(json.dumps(line))
 
 
+def one_core_baseline(timeout=300):
+    """The same oracle solve on one core (one BLAS/OpenMP thread), in a child
+    process so the thread count is fixed before numpy loads; None when it does
+    not finish within the timeout."""
+    code = ("import sys, time; sys.path[:0] = [%r, %r]\n"
+            "import bench\n"
+            "from oracle.eigb import tt_eigb\n"
+            "n, m, ra, crA, ry, cr = bench.workload()\n"
+            "t0 = time.perf_counter()\n"
+            "tt_eigb(bench.D, n, m, ra, crA, cr, ry, bench.EPS, bench.RMAX, bench.B, nswp=20, "
+            "max_full_size=bench.MFS)\n"
+            "print(time.perf_counter() - t0)\n") % (ROOT, os.path.join(ROOT, "tt-fort_gb300"))
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1", MKL_NUM_THREADS="1")
+    try:
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env,
+                           timeout=timeout)
+        v = float(r.stdout.strip().splitlines()[-1])
+    except Exception:
+        return None
+    return {"value": v, "unit": "s", "cores": 1,
+            "sample": "one full solve with the oracle restatement, one BLAS/OpenMP thread"}
+
+
 def run_reference(args):
     from oracle.eigb import tt_eigb as oracle_eigb
     n, m, ra, crA, ry, cr = workload()
@@ -725,7 +748,8 @@ def main():
         cpu = {"value": tc, "unit": "s", "cores": os.cpu_count(), "kind": "port",
                "sample": "one full solve of the workload with the oracle restatement "
                          "(numpy + OpenBLAS threads)",
-               "lambda_maxrel_vs_gpu": float(np.max(np.abs(ref["lambda"] - lam) / np.abs(ref["lambda"])))}
+               "lambda_maxrel_vs_gpu": float(np.max(np.abs(ref["lambda"] - lam) / np.abs(ref["lambda"]))),
+               "one_core": one_core_baseline()}
     line = {"metric": "tt_eigb sweep time to convergence (d=20 Heisenberg, B=5)",
             "value": t, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": t * 1e3, "higher_is_better": False,
