@@ -453,16 +453,25 @@ def run_reference(args):
         t0 = time.perf_counter()
         out = oracle_eigb(D, n, m, ra, crA, cr, ry, EPS, RMAX, B, nswp=20, max_full_size=MFS)
         ts.append(time.perf_counter() - t0)
-    v = float(np.mean(ts))
-    cores = os.cpu_count()
+    v_all = float(np.mean(ts))
+    all_threads = {"value": v_all, "unit": "s", "cores": os.cpu_count(),
+                   "sample": f"{steps} full solve(s) of the workload with the oracle "
+                             "restatement (numpy + OpenBLAS on all host threads)"}
+    # the same solve on one thread: the workload's dense products are small,
+    # and on some hosts threading costs more than it gains; the faster of the
+    # two is the reference arm's value
+    one = one_core_baseline()
+    best = one if one is not None and one["value"] < v_all else all_threads
+    v = best["value"]
     line = {"metric": "tt_eigb sweep time to convergence (d=20 Heisenberg, B=5)",
             "value": v, "unit": "s", "n_gpus": args.gpus, "steps": steps, "warmup": warm,
             "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
             "config": config(),
-            "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
-                             "sample": f"{steps} full solve(s) of the workload with the oracle "
-                                       "restatement (numpy + OpenBLAS threads)"},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": best["cores"], "kind": "port",
+                             "sample": best["sample"] + " (the faster of all host threads and "
+                                                        "one thread)",
+                             "all_threads": all_threads, "one_core": one},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "lambda": out["lambda"].tolist()}
     print(json.dumps(line))
@@ -745,11 +754,15 @@ def main():
         t0 = time.perf_counter()
         ref = oracle_eigb(D, n, m, ra, crA, cr, ry, EPS, RMAX, B, nswp=20, max_full_size=MFS)
         tc = time.perf_counter() - t0
-        cpu = {"value": tc, "unit": "s", "cores": os.cpu_count(), "kind": "port",
-               "sample": "one full solve of the workload with the oracle restatement "
-                         "(numpy + OpenBLAS threads)",
+        all_threads = {"value": tc, "unit": "s", "cores": os.cpu_count(),
+                       "sample": "one full solve of the workload with the oracle restatement "
+                                 "(numpy + OpenBLAS on all host threads)"}
+        one = one_core_baseline()
+        best = one if one is not None and one["value"] < tc else all_threads
+        cpu = {"value": best["value"], "unit": "s", "cores": best["cores"], "kind": "port",
+               "sample": best["sample"] + " (the faster of all host threads and one thread)",
                "lambda_maxrel_vs_gpu": float(np.max(np.abs(ref["lambda"] - lam) / np.abs(ref["lambda"]))),
-               "one_core": one_core_baseline()}
+               "all_threads": all_threads, "one_core": one}
     line = {"metric": "tt_eigb sweep time to convergence (d=20 Heisenberg, B=5)",
             "value": t, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": t * 1e3, "higher_is_better": False,

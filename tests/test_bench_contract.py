@@ -23,6 +23,10 @@ def test_reference_arm_line_contract(monkeypatch):
     monkeypatch.setattr(bench, "B", 2)
     monkeypatch.setattr(bench, "RMAX", 16)
     monkeypatch.setattr(bench, "MFS", 16)
+    # the one-thread solve runs in a child process on the real workload; here
+    # a fixed stand-in slower than any small-chain solve
+    monkeypatch.setattr(bench, "one_core_baseline",
+                        lambda: {"value": 1e9, "unit": "s", "cores": 1, "sample": "stand-in"})
     args = types.SimpleNamespace(steps=1, warmup=0, gpus=1)
     buf = io.StringIO()
     with redirect_stdout(buf):
@@ -35,7 +39,9 @@ def test_reference_arm_line_contract(monkeypatch):
     assert line["impl"] == "reference" and line["higher_is_better"] is False
     assert line["value"] > 0 and line["e2e"]["value"] == line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
-    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1
+    assert cb["value"] == min(cb["all_threads"]["value"], cb["one_core"]["value"])
     assert "workload" in line["config"]
     assert np.all(np.isfinite(line["lambda"]))
 
