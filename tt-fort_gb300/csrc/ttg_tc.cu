@@ -1835,15 +1835,24 @@ static size_t split_layout(const LocalDims& L, int nvec_max, SplitOp* op, char* 
   const i64 ld1 = (i64)ceil_div(M1, 4) * 4;
   size_t t1 = ((size_t)ld1 * ceil_div(N1, 4) * 4 * sizeof(float) + 1023) & ~size_t(1023);
   tot += t1 + 1024 + sizeof(SplitOp) + 1024;
-  // K-chunk partials of the tiled CORE kernel, the largest over 1..nvec_max
+  // K-chunk partials of the tiled CORE kernel: for this problem the largest
+  // over 1..nvec_max vectors; when sizing, the largest over every row count
+  // up to this problem's (fewer rows split K into more chunks, so a smaller
+  // local problem can need more partials than the largest; K is split only
+  // below 152 row tiles, which bounds the scan)
   const int ja = (int)(L.m * L.ra2), na = (int)(L.n * L.ra1);
   size_t part = 0;
   if (!(ja <= 16 && na <= 16)) {
-    for (int v = 1; v <= nvec_max; ++v) {
+    auto need = [&](i64 rows) {
       int nz, qc;
-      tc::core_chunks(L.rx1 * L.ry2 * v, na, ja, nz, qc);
-      const size_t b = (size_t)(nz * L.rx1 * L.ry2 * v * na) * sizeof(float);
-      if (nz > 1 && b > part) part = b;
+      tc::core_chunks(rows, na, ja, nz, qc);
+      return nz > 1 ? (size_t)(nz * rows * na) * sizeof(float) : (size_t)0;
+    };
+    if (sizing) {
+      const i64 rmax = std::min<i64>(L.rx1 * L.ry2 * nvec_max, (i64)152 * tc::CT_R);
+      for (i64 r = 1; r <= rmax; ++r) part = std::max(part, need(r));
+    } else {
+      for (int v = 1; v <= nvec_max; ++v) part = std::max(part, need(L.rx1 * L.ry2 * v));
     }
   }
   part = (part + 1023) & ~size_t(1023);
